@@ -1,0 +1,412 @@
+"""Benchmark of the kazen GB300 hot path.
+
+Headline workload (one step = one full frame): the plain wavefront path
+tracer on the procedural terrain scene — 1024 x 1024-cell fBm heightfield
+(2,097,152 triangles) + 64 icospheres (1,280 triangles each), Lambert / GGX
+conductor / smooth dielectric materials, 4 quad lights, 1920 x 1080, 64 spp,
+max depth 8, 2M-path wavefront, FP32. Metric: Mpaths*bounces/s (closest-hit
+extension rays traced, camera rays included, per second).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device-resident throughput (scene built, film in HBM, CUDA events
+around each frame on the scene stream, L2 flushed between frames); `e2e` is
+the same metric through the C ABI with a host output buffer (the frame's
+device->host copy inside the timed region). The traversal microbenchmark
+(1,048,576-triangle soup, 16,777,216 incoherent rays) is reported alongside.
+N > 1: independent replicas (the path tracer does not shard: no collective),
+one per GPU, weak scaling, max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Mpaths*bounces/s (plain GPU wavefront PT)"
+UNIT = "Mpaths*bounces/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--small", action="store_true", help="reduced workload (quick checks only)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-traversal", action="store_true")
+    return p.parse_args()
+
+
+def workload(small: bool):
+    if small:
+        return dict(width=320, height=180, spp=8, max_depth=8, cells=256, n_spheres=64, wavefront=1 << 18)
+    return dict(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
+
+
+def config_dict(w, extra=None):
+    c = {"workload": "terrain_pt_%dx%d_%dspp_depth%d" % (w["width"], w["height"], w["spp"], w["max_depth"]),
+         "triangles": None, "resolution": [w["width"], w["height"]], "spp": w["spp"], "max_depth": w["max_depth"],
+         "wavefront": w["wavefront"], "scene": "fBm heightfield %dx%d cells + %d icospheres (subdiv 3) + 4 quad lights"
+         % (w["cells"], w["cells"], w["n_spheres"]),
+         "l2": "flushed between frames (256 MiB write); scene BVH+triangles and path state exceed L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n):
+    if n <= 1 and "WORLD_SIZE" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", n))
+    backend = os.environ.get("KZ_BENCH_BACKEND", "nccl")
+    if backend == "nccl":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist.init_process_group(backend, rank=rank, world_size=world)
+    return rank, world, dist
+
+
+def aggregate(units_local: float, seconds_local: float, dist):
+    """Whole-job throughput of replicas: total units / max-over-ranks time."""
+    if dist is None:
+        return units_local, seconds_local
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds_local], dtype=torch.float64, device=dev)
+    u = torch.tensor([units_local], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()), float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline (restatement)
+def cpu_baseline(desc, w, budget_s=15.0):
+    """The CPU restatement rendering whole rows of the same frame at the same
+    spp on all host cores, until about budget_s of work."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    sc = O.Scene.from_desc(desc)
+    build_s = time.perf_counter() - t0
+    c = desc.camera
+    cam = O.make_camera(c.eye, c.lookat, c.up, c.fov, c.flip)
+    cores = os.cpu_count() or 1
+    H = w["height"]
+    bounces, secs, rows = 0, 0.0, 0
+    r0 = H // 2 - 8
+    while secs < budget_s and rows < H:
+        a = r0 + rows
+        if a >= H:
+            break
+        ts = time.perf_counter()
+        _, st = sc.render(cam, w["width"], H, w["spp"], w["max_depth"], seed=0, nthreads=cores, rows=(a, a + 2))
+        secs += time.perf_counter() - ts
+        bounces += st["path_bounces"]
+        rows += 2
+    return {"value": bounces / secs / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d rows x %d px x %d spp of the same frame (%d path*bounces, %.1f s; oracle BVH build %.1f s "
+                      "untimed)" % (rows, w["width"], w["spp"], bounces, secs, build_s)}
+
+
+# ---------------------------------------------------------------- traversal microbenchmark
+def traversal_bench(steps, warmup):
+    import torch
+
+    from kazen_proto_gb300 import scenes
+    tv = scenes.triangle_soup(1 << 20, seed=1)
+    rays = scenes.soup_rays(1 << 24, seed=2)
+    s = scenes.soup_desc(tv).build()
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream)
+    dr = torch.from_numpy(rays.view(np.float32).reshape(-1, 8)).cuda()
+    n = dr.shape[0]
+    out = {"t": torch.empty(n, dtype=torch.float32, device="cuda"),
+           "prim_id": torch.empty(n, dtype=torch.int32, device="cuda")}
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    nodes, tris = s.intersect_stats(dr)
+    res = {}
+    for name, fn in (("closest", lambda: s.intersect(dr, out=out)), ("any", lambda: s.occluded(dr, out=occ))):
+        for _ in range(warmup):
+            fn()
+        s.synchronize()
+        ms = 0.0
+        for _ in range(steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        s.synchronize()
+        res[name + "_grays_per_s"] = n * steps / (ms / 1e3) / 1e9
+        res[name + "_ms"] = ms / steps
+    res["node_fetches_per_ray"] = nodes / n
+    res["tri_fetches_per_ray"] = tris / n
+    bytes_per_ray = 32 + 8 + 64 * nodes / n + 48 * tris / n
+    res["closest_alg_bytes_per_ray"] = bytes_per_ray
+    res["closest_alg_gbs"] = bytes_per_ray * n / (res["closest_ms"] / 1e3) / 1e9
+    res["workload"] = "1,048,576-triangle soup, 16,777,216 incoherent rays, device-resident"
+    info = s.info()
+    res["bvh_nodes"] = info["n_bvh_nodes"]
+    res["bvh_depth"] = info["bvh_depth"]
+    s.close()
+    return res
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        try:
+            return json.load(open(path))
+        except Exception:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+
+    rank, world, dist = dist_setup(args.gpus)
+    from kazen_proto_gb300 import _native as N
+    from kazen_proto_gb300 import api, build as kbuild, scenes
+    kbuild.build()
+    dev_index = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev_index)
+    w = workload(args.small)
+    desc = scenes.terrain_scene(w["width"], w["height"], w["spp"], w["max_depth"], w["cells"], w["n_spheres"])
+    s = desc.build()
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream)
+    W, H = w["width"], w["height"]
+    seed = 1000 * rank
+    r = api.Renderer(spp=w["spp"], max_depth=w["max_depth"], seed=seed, wavefront_size=w["wavefront"],
+                     flags=N.KZ_RENDER_FLAG_TIMING)
+    rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # fetch counts for the roofline: one counted frame at reduced spp (untimed)
+    cnt = api.Renderer(spp=max(1, w["spp"] // 16), max_depth=w["max_depth"], seed=seed,
+                       wavefront_size=w["wavefront"], flags=N.KZ_RENDER_FLAG_COUNT)
+    cnt.render(s, desc.camera, W, H, device_out=(rgb, None))
+    cs = cnt.last_stats
+    nodes_per_ray = cs["closest_node_fetches"] / max(1, cs["path_bounces"])
+    tris_per_ray = cs["closest_tri_fetches"] / max(1, cs["path_bounces"])
+
+    for _ in range(args.warmup):
+        r.render(s, desc.camera, W, H, device_out=(rgb, None))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev_index)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    total_ms, bounces, shadow, launches, iterations = 0.0, 0, 0, 0, 0
+    stage = {"generate_ms": 0.0, "trace_ms": 0.0, "shade_ms": 0.0, "shadow_ms": 0.0}
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r.render(s, desc.camera, W, H, device_out=(rgb, None))
+        b.record(stream)
+        torch.cuda.synchronize()
+        total_ms += a.elapsed_time(b)
+        st = r.last_stats
+        bounces += st["path_bounces"]
+        shadow += st["shadow_rays"]
+        launches += st["kernel_launches"] + 1  # + the film scale kernel
+        iterations += st["iterations"]
+        for k in stage:
+            stage[k] += st[k]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    units, secs = aggregate(bounces, total_ms / 1e3, dist)
+
+    # e2e through the C ABI with a host output buffer
+    img = None
+    e2e_bounces, e2e_s = 0, 0.0
+    for k in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        img = r.render(s, desc.camera, W, H)
+        e2e_s += time.perf_counter() - t0
+        e2e_bounces += r.last_stats["path_bounces"]
+    e_units, e_secs = aggregate(e2e_bounces, e2e_s, dist)
+
+    trav = None
+    if rank == 0 and not args.no_traversal and not args.small:
+        trav = traversal_bench(max(3, args.steps), max(3, args.warmup))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    trace_ms_frame = stage["trace_ms"] / args.steps
+    rays_frame = bounces / args.steps
+    alg_bytes_ray = 32 + 16 + 64 * nodes_per_ray + 48 * tris_per_ray
+    alg_bytes_frame = alg_bytes_ray * rays_frame
+    achieved = alg_bytes_frame / (trace_ms_frame / 1e3) / 1e9
+    iters_frame = iterations / args.steps
+    rays_launch = rays_frame / iters_frame
+    tr = load_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == "k_trace_paths" and tr.get("dram_bytes_per_ray"):
+        traffic = round(tr["dram_bytes_per_ray"] * rays_launch)
+    value = units / secs / 1e6
+    frame_ms = total_ms / args.steps
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(frame_ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": config_dict(w, {"triangles": desc.n_triangles(), "parallelism": "replicas" if world > 1 else "1gpu"}),
+        "e2e": {"value": round(e_units / e_secs / 1e6, 3), "unit": UNIT,
+                "h2d_bytes_per_step": 64 + 40, "d2h_bytes_per_step": W * H * 12,
+                "note": "kz_render with a host film buffer: camera+config in, W*H*3 float out per frame"},
+        "roofline": {"bound": "hbm", "kernel": "k_trace_paths", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "alg_bytes_per_launch": round(alg_bytes_ray * rays_launch),
+                     "launch_ms": round(trace_ms_frame / iters_frame, 4),
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                     "alg_bytes_per_ray": round(alg_bytes_ray, 1),
+                     "node_fetches_per_ray": round(nodes_per_ray, 2), "tri_fetches_per_ray": round(tris_per_ray, 2),
+                     "note": "algorithmic bytes = 32 B ray + 16 B hit + 64 B per node fetch + 48 B per triangle "
+                             "fetch; node/triangle fetches are served mostly from L1/L2"},
+        "stages_ms_per_frame": {k: round(v / args.steps, 3) for k, v in stage.items()},
+        "mrays_per_s": round((bounces + shadow) / (total_ms / 1e3) / 1e6, 2),
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "traversal": trav,
+    }
+    if img is not None:
+        line["image_mean"] = float(np.mean(img))
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args):
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return
+    from kazen_proto_gb300 import scenes
+    from oracle import oracle as O
+    w = workload(args.small)
+    desc = scenes.terrain_scene(w["width"], w["height"], w["spp"], w["max_depth"], w["cells"], w["n_spheres"])
+    sc = O.Scene.from_desc(desc)
+    c = desc.camera
+    cam = O.make_camera(c.eye, c.lookat, c.up, c.fov, c.flip)
+    cores = os.cpu_count() or 1
+    rows = 2
+    H = w["height"]
+    for k in range(args.warmup):
+        a = (H // 2 + 2 * k) % (H - rows)
+        sc.render(cam, w["width"], H, w["spp"], w["max_depth"], seed=0, nthreads=cores, rows=(a, a + rows))
+    secs, bounces = 0.0, 0
+    for k in range(args.steps):
+        a = (H // 3 + 2 * k) % (H - rows)
+        t0 = time.perf_counter()
+        _, st = sc.render(cam, w["width"], H, w["spp"], w["max_depth"], seed=0, nthreads=cores, rows=(a, a + rows))
+        secs += time.perf_counter() - t0
+        bounces += st["path_bounces"]
+    v = bounces / secs / 1e6
+    sample = "%d rows x %d px x %d spp per step of the same frame" % (rows, w["width"], w["spp"])
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene)", "config": config_dict(w, {"triangles": desc.n_triangles()}),
+            "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                             "note": "the reference itself cannot be built here (Embree 4, OSL, OIIO, TBB, boost, "
+                                     "pcg32 absent); this is the CPU restatement of its hot path"},
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

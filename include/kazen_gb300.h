@@ -1,0 +1,263 @@
+/*
+ * kazen_gb300.h — C ABI of the GB300-native kazen rendering hot path.
+ *
+ * One shared library (libkazen_gb300.so) exports these entry points. Every
+ * call returns a kz_status; kz_last_error_string() gives the message of the
+ * last failing call on the calling thread. Buffers are caller-owned: inputs
+ * are read, outputs are written, nothing is retained across calls except by
+ * the scene handle (which owns its device copy of the geometry, BVH,
+ * materials and lights). Pointers are host pointers when `mem` is
+ * KZ_MEM_HOST (the library stages them through pinned memory) and device
+ * pointers on the current CUDA device when `mem` is KZ_MEM_DEVICE.
+ *
+ * Calls on one scene handle are serialised by the library (a mutex per
+ * handle) and run on that handle's CUDA stream; distinct handles may be used
+ * from different threads. KZ_MEM_HOST calls are synchronous. KZ_MEM_DEVICE
+ * calls are asynchronous on the scene stream; kz_scene_synchronize() waits
+ * and returns any device-side status (e.g. KZ_ERR_STACK) raised since the
+ * last synchronisation.
+ *
+ * Reference interfaces replaced (kazen_proto, paths within that project):
+ *   HitableInterface::intersect / occluded ........ src/core/hitable.h:10-37
+ *   Accelerator::add_trianglemesh / build ......... src/core/accel.h:13-41
+ *   EmbreeAccel::intersect (closest, t-only) ...... src/core/accel.cpp:348-432
+ *   Integrator::setup / Li ......................... src/core/integrator.h:23-39
+ *   Renderer::render (per-pixel spp average) ....... src/core/renderer.cpp:18-90
+ *   ClosureID / *Params / CompositeClosure ......... src/shading/bsdf.h:16-196,
+ *                                                    src/shading/bsdfs.h:18-119
+ *   Camera(position, lookat, up, near, far, fov) ... src/core/camera.h:31-96
+ */
+#ifndef KAZEN_GB300_H
+#define KAZEN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KZ_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+typedef int32_t kz_status;
+#define KZ_OK               0
+#define KZ_ERR_INVALID_ARG  1  /* bad pointer, size, id or non-finite input     */
+#define KZ_ERR_OOM          2  /* device or pinned allocation failed           */
+#define KZ_ERR_CUDA         3  /* a CUDA runtime call failed                   */
+#define KZ_ERR_TIMEOUT      4  /* a bounded device-side wait gave up           */
+#define KZ_ERR_STACK        5  /* a traversal stack overflowed (ray aborted)   */
+#define KZ_ERR_STATE        6  /* call out of order (e.g. intersect before build) */
+#define KZ_ERR_NO_DEVICE    7  /* no CUDA device is visible                    */
+
+/* ---- memory kinds ------------------------------------------------------ */
+#define KZ_MEM_HOST   0
+#define KZ_MEM_DEVICE 1
+
+#define KZ_INVALID_ID 0xFFFFFFFFu
+
+/* ---- closure ids: the reference ClosureID values (src/shading/bsdf.h:16-75) */
+#define KZ_CLOSURE_DIFFUSE                        0   /* DiffuseID                       */
+#define KZ_CLOSURE_EMISSION                       10  /* EmissionID (Le only)            */
+#define KZ_CLOSURE_KP_MIRROR                      14  /* KpMirrorID                      */
+#define KZ_CLOSURE_KP_DIELECTRIC                  15  /* KpDielectricID                  */
+#define KZ_CLOSURE_KP_EMITTER                     17  /* KpEmitterID (Le only)           */
+#define KZ_CLOSURE_KP_GLOSS                       18  /* KpGlossID  (microfacet, refract 0) */
+#define KZ_CLOSURE_KP_GLASS                       19  /* KpGlassID  (microfacet, refract 1/2) */
+#define KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL     24  /* KpPrincipleSpecularReflectionID */
+/* Not in the reference: GGX conductor with an RGB Schlick F0, built from the
+ * reference GGX D/G/VNDF (src/shading/microfacet.h:95-291) and
+ * fresnel_schlick(RGB F0) (src/shading/fresnel.h:185-187). */
+#define KZ_CLOSURE_CONDUCTOR_GGX                  64
+
+/* Microfacet distribution selector stored in params[0] of GLOSS / GLASS. */
+#define KZ_DIST_GGX      0
+#define KZ_DIST_BECKMANN 1
+
+/*
+ * One closure lobe (64 bytes). Parameter layouts, all in the y-up local
+ * shading frame the reference shades in (N = (0,1,0)):
+ *   DIFFUSE            params[0..2] = N
+ *   KP_DIELECTRIC      params[0] = int_ior, params[1] = ext_ior
+ *   KP_GLOSS/KP_GLASS  params[0] = dist, [1..3] = N, [4..6] = U,
+ *                      [7] = xalpha, [8] = yalpha, [9] = eta, [10] = refract
+ *   KP_PRINCIPLE_SPECULAR_REFL  [0..2] = F0, [3..5] = N, [6] = xalpha,
+ *                      [7] = yalpha, [8] = eta, [9] = metallic
+ *   CONDUCTOR_GGX      [0..2] = F0, [3] = xalpha, [4] = yalpha
+ *   KP_MIRROR          none
+ */
+typedef struct kz_lobe {
+    uint32_t closure_id;
+    float    weight[3];
+    float    params[12];
+} kz_lobe;
+
+#define KZ_MAX_LOBES 8   /* reference max_closure, src/shading/bsdf.h:77 */
+
+/* A lowered surface shader: emitted radiance + up to 8 weighted lobes
+ * (the reference ShadingResult{Le, surface}, src/shading/bsdf.h:217-229). */
+typedef struct kz_material {
+    float    Le[3];
+    uint32_t n_lobes;
+    kz_lobe  lobes[KZ_MAX_LOBES];
+} kz_material;
+
+/* Ray record, 32 bytes (two 16-byte halves). Directions must be unit length:
+ * the reference Ray ctor normalises (src/core/ray.h:12-22); callers normalise
+ * once on the host so every consumer sees identical FP32 bits. */
+typedef struct kz_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} kz_ray;
+
+/* Hit outputs, structure of arrays. Any pointer except t and prim_id may be
+ * NULL. A miss writes t = tmax of the ray, prim_id = geom_id = KZ_INVALID_ID.
+ * prim_id is the triangle index within its mesh; geom_id the mesh index
+ * returned by kz_scene_add_mesh. u, v are the barycentrics of vertices 1, 2. */
+typedef struct kz_hits {
+    float*    t;
+    uint32_t* prim_id;
+    uint32_t* geom_id;
+    float*    u;
+    float*    v;
+} kz_hits;
+
+/* Pinhole camera, reference Camera(position, lookat, up, near, far, fov, flip)
+ * (src/core/camera.h:31-96): fov is the horizontal field of view in degrees. */
+typedef struct kz_camera {
+    float   eye[3];
+    float   lookat[3];
+    float   up[3];
+    float   fov_deg;
+    float   near_clip;
+    float   far_clip;
+    int32_t flip;
+} kz_camera;
+
+typedef struct kz_film_desc {
+    uint32_t width;
+    uint32_t height;
+} kz_film_desc;
+
+#define KZ_RENDER_DEFAULT_WAVEFRONT (1u << 21)
+
+typedef struct kz_render_config {
+    uint32_t spp;            /* samples per pixel                              */
+    uint32_t max_depth;      /* maximum number of shaded path vertices         */
+    uint64_t seed;           /* PCG32 seed; stream = pixel * spp + sample      */
+    uint32_t wavefront_size; /* paths in flight; 0 = KZ_RENDER_DEFAULT_WAVEFRONT */
+    uint32_t rr_min_depth;   /* first vertex index that plays roulette (ref: 3) */
+    uint32_t block_size;     /* threads per block of the stage kernels; 0 = 256 */
+    uint32_t flags;          /* KZ_RENDER_FLAG_* bits, 0 = none                */
+} kz_render_config;
+
+/* Record CUDA events around every stage launch (on the scene stream) and
+ * report per-stage device time in kz_render_stats. */
+#define KZ_RENDER_FLAG_TIMING 1u
+/* Trace with the fetch-counting traversal variant and report BVH node and
+ * triangle fetches (slower; for roofline accounting, not for timing). */
+#define KZ_RENDER_FLAG_COUNT  2u
+
+typedef struct kz_render_stats {
+    uint64_t path_bounces;   /* closest-hit extension rays traced (camera rays included) */
+    uint64_t shadow_rays;    /* any-hit rays traced for next-event estimation  */
+    uint64_t iterations;     /* wavefront iterations                           */
+    uint64_t paths;          /* camera paths started                           */
+    uint64_t kernel_launches;/* kernels launched by the call                   */
+    /* KZ_RENDER_FLAG_COUNT: fetches of 64-byte nodes / 48-byte triangles */
+    uint64_t closest_node_fetches, closest_tri_fetches;
+    uint64_t shadow_node_fetches, shadow_tri_fetches;
+    /* KZ_RENDER_FLAG_TIMING: summed device time per stage, milliseconds */
+    double   generate_ms, trace_ms, shade_ms, shadow_ms;
+} kz_render_stats;
+
+typedef struct kz_scene_info {
+    uint64_t n_meshes;
+    uint64_t n_triangles;
+    uint64_t n_lights;
+    uint64_t n_bvh_nodes;
+    uint64_t bvh_bytes;       /* node array bytes on the device              */
+    uint64_t triangle_bytes;  /* leaf-ordered triangle records on the device */
+    uint32_t bvh_depth;
+    uint32_t built;
+} kz_scene_info;
+
+typedef struct kz_scene kz_scene;
+
+/* ---- library --------------------------------------------------------- */
+int32_t     kz_abi_version(void);
+const char* kz_last_error_string(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+int32_t     kz_device_count(void);
+
+/* ---- scene (replaces Accelerator::add_trianglemesh / build,
+ *      src/core/accel.h:22-32, and Scene::add_mesh / build_bvh,
+ *      src/core/scene.h:144-164) ------------------------------------------ */
+kz_status kz_scene_create(kz_scene** out_scene);
+kz_status kz_scene_destroy(kz_scene* scene);
+/* xyz: nverts*3 floats; idx: ntris*3 vertex indices; xform12: optional
+ * row-major 3x4 object-to-world matrix (NULL = identity), applied on the host
+ * at add time. Host pointers only. */
+kz_status kz_scene_add_mesh(kz_scene* scene, const float* xyz, uint32_t nverts,
+                            const uint32_t* idx, uint32_t ntris,
+                            const float* xform12, int32_t material_id,
+                            int32_t is_light, int32_t* out_geom_id);
+kz_status kz_scene_set_materials(kz_scene* scene, const kz_material* materials,
+                                 uint32_t n_materials);
+/* Builds the BVH and uploads geometry, materials and the light table. */
+kz_status kz_scene_build(kz_scene* scene);
+kz_status kz_scene_get_info(kz_scene* scene, kz_scene_info* out_info);
+/* Use an external cudaStream_t (NULL = the library-created stream). */
+kz_status kz_scene_set_stream(kz_scene* scene, void* cuda_stream);
+kz_status kz_scene_synchronize(kz_scene* scene);
+
+/* ---- intersector (replaces HitableInterface::intersect / occluded,
+ *      src/core/hitable.h:10-37, EmbreeAccel::intersect,
+ *      src/core/accel.cpp:348-432) --------------------------------------- */
+/* Closest hit in (tmin, tmax]; equal t resolves to the smaller global
+ * triangle index. */
+kz_status kz_intersect_closest(kz_scene* scene, const kz_ray* rays, uint64_t n,
+                               kz_hits hits, int32_t mem);
+/* occluded[i] = 1 when any triangle is hit in (tmin, tmax], else 0. */
+kz_status kz_intersect_any(kz_scene* scene, const kz_ray* rays, uint64_t n,
+                           uint8_t* occluded, int32_t mem);
+/* Closest-hit traversal that also counts, per ray, BVH nodes fetched and
+ * triangles tested (device-side counters; for roofline accounting). */
+kz_status kz_intersect_stats(kz_scene* scene, const kz_ray* rays, uint64_t n,
+                             int32_t mem, uint64_t* out_node_fetches,
+                             uint64_t* out_triangle_fetches);
+
+/* ---- closures (reference per-lobe eval/pdf/sample, src/shading/bsdfs.cpp) */
+#define KZ_CONVENTION_REFERENCE  0  /* value and pdf exactly as the reference lobe returns them */
+#define KZ_CONVENTION_INTEGRATOR 1  /* f*|cos(wo)| and solid-angle pdf of wo, as the path loop uses them */
+/* One lobe per query (lobes[i]); wi, wo: n*3 floats (local frame, y-up).
+ * out_f: n*3 floats (weight not applied), out_pdf: n floats. */
+kz_status kz_closure_eval_batch(const kz_lobe* lobes, const float* wi,
+                                const float* wo, uint64_t n, int32_t convention,
+                                float* out_f, float* out_pdf, int32_t mem);
+/* u: n*3 uniforms in [0,1). Outputs: wo (n*3), weight = f*|cos|/pdf (n*3, lobe
+ * weight not applied), pdf (n, 0 for delta), flags (n: bit0 = valid,
+ * bit1 = delta/specular). */
+kz_status kz_closure_sample_batch(const kz_lobe* lobes, const float* wi,
+                                  const float* u, uint64_t n, float* out_wo,
+                                  float* out_weight, float* out_pdf,
+                                  uint8_t* out_flags, int32_t mem);
+
+/* ---- integrator (replaces PathIntegrator::Li, src/core/integrator.cpp:362-561,
+ *      driven per pixel sample by Renderer::render, src/core/renderer.cpp:53-62) */
+/* Li of n camera rays; path i draws from PCG32 stream (cfg.seed, i). */
+kz_status kz_li_batch(kz_scene* scene, const kz_ray* rays, uint64_t n,
+                      const kz_render_config* cfg, float* out_rgb, int32_t mem,
+                      kz_render_stats* out_stats);
+/* Full frame: out_rgb (W*H*3 floats, spp average, row 0 = top) and optional
+ * out_rgb64 (FP64 accumulation of the same samples). */
+kz_status kz_render(kz_scene* scene, const kz_camera* camera,
+                    const kz_film_desc* film, const kz_render_config* cfg,
+                    float* out_rgb, double* out_rgb64, int32_t mem,
+                    kz_render_stats* out_stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KAZEN_GB300_H */

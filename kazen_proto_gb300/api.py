@@ -1,0 +1,354 @@
+"""Python host API over the C ABI, mirroring kazen_proto's hot-path interfaces.
+
+Reference interfaces mirrored (paths within kazen_proto):
+  * Scene.add_mesh / build_bvh ........ src/core/scene.h:144-164, src/binding/api.cpp:121-170
+  * Scene.intersect / occluded ........ HitableInterface, src/core/hitable.h:10-37
+  * PathIntegrator.setup / Li .......... src/core/integrator.h:23-39, src/core/integrator.cpp:362-561
+  * Renderer(spp).render ............... src/core/renderer.cpp:18-90
+  * closure lobes ...................... ClosureID / *Params, src/shading/bsdf.h:16-75, src/shading/bsdfs.h:18-119
+
+Arrays may be numpy arrays (host memory; the library stages the copies) or
+CUDA torch tensors (device memory, used in place). Every call goes to the
+CUDA library; a missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from ._native import check, lib
+
+try:  # torch is optional plumbing for device buffers
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_cuda_tensor(x) -> bool:
+    return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_cuda_tensor(x):
+        return C.c_void_p(x.data_ptr())
+    return x.ctypes.data_as(C.c_void_p)
+
+
+# ---------------------------------------------------------------- closures / materials
+def lobe(closure_id: int, weight=(1.0, 1.0, 1.0), params=()) -> np.ndarray:
+    rec = np.zeros((), dtype=N.LOBE_DTYPE)
+    rec["closure_id"] = closure_id
+    rec["weight"] = np.asarray(weight, np.float32)
+    p = np.zeros(12, np.float32)
+    p[: len(params)] = np.asarray(params, np.float32)
+    rec["params"] = p
+    return rec
+
+
+def diffuse(albedo=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`Cs * diffuse(N)`: Diffuse lobe (bsdfs.cpp:27-41)."""
+    return lobe(N.KZ_CLOSURE_DIFFUSE, albedo, N_local)
+
+
+def mirror(weight=(1.0, 1.0, 1.0)):
+    """`Cs * kp_mirror()` (bsdfs.cpp:254-266)."""
+    return lobe(N.KZ_CLOSURE_KP_MIRROR, weight)
+
+
+def dielectric(int_ior=1.5046, ext_ior=1.000277, weight=(1.0, 1.0, 1.0)):
+    """`Cs * kp_dielectric(int_ior, ext_ior)` (bsdfs.cpp:268-298)."""
+    return lobe(N.KZ_CLOSURE_KP_DIELECTRIC, weight, (int_ior, ext_ior))
+
+
+def microfacet(dist="ggx", xalpha=0.2, yalpha=None, eta=1.5, refract=0, weight=(1.0, 1.0, 1.0)):
+    """`microfacet(dist, N, U, xalpha, yalpha, eta, refract)` lowered as the
+    reference's process_closure does (bsdf.cpp:227-254): refract 0 -> KpGloss,
+    1 or 2 -> KpGlass."""
+    d = N.KZ_DIST_BECKMANN if dist == "beckmann" or dist == "default" else N.KZ_DIST_GGX
+    ya = xalpha if yalpha is None else yalpha
+    cid = N.KZ_CLOSURE_KP_GLOSS if refract == 0 else N.KZ_CLOSURE_KP_GLASS
+    return lobe(cid, weight, (d, 0, 1, 0, 1, 0, 0, xalpha, ya, eta, refract))
+
+
+def conductor_ggx(F0=(0.95, 0.64, 0.54), alpha=0.2, weight=(1.0, 1.0, 1.0)):
+    """GGX conductor with RGB Schlick F0 (not a reference lobe; built from the
+    reference GGX terms and fresnel_schlick(F0), fresnel.h:185-187)."""
+    return lobe(N.KZ_CLOSURE_CONDUCTOR_GGX, weight, (F0[0], F0[1], F0[2], alpha, alpha))
+
+
+def principle_specular(F0=(0.04, 0.04, 0.04), alpha=0.2, eta=1.5, metallic=0.0, weight=(1.0, 1.0, 1.0)):
+    """`kp_principle_specular_reflection(F0, N, xalpha, yalpha, eta, metallic)` (bsdfs.cpp:688-730)."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL, weight,
+                (F0[0], F0[1], F0[2], 0, 1, 0, alpha, alpha, eta, metallic))
+
+
+def material(lobes=(), Le=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """A lowered surface shader: Le plus up to 8 lobes (ShadingResult, bsdf.h:217-229).
+    An emitter shader `Cs * kp_emitter(a)` lowers to Le = Cs with no lobe."""
+    if len(lobes) > N.KZ_MAX_LOBES:
+        raise ValueError("at most 8 lobes")
+    m = np.zeros((), dtype=N.MATERIAL_DTYPE)
+    m["Le"] = np.asarray(Le, np.float32)
+    m["n_lobes"] = len(lobes)
+    for i, l in enumerate(lobes):
+        m["lobes"][i] = l
+    return m
+
+
+# ---------------------------------------------------------------- rays
+def make_rays(o, d, tmin=1e-4, tmax=np.inf) -> np.ndarray:
+    """Ray records (32 B). Directions are normalised here, once, in FP32."""
+    o = np.asarray(o, np.float32).reshape(-1, 3)
+    d = np.asarray(d, np.float32).reshape(-1, 3)
+    n = max(len(o), len(d))
+    o = np.broadcast_to(o, (n, 3))
+    d = np.broadcast_to(d, (n, 3))
+    ln = np.sqrt((d * d).sum(axis=1, dtype=np.float32), dtype=np.float32)
+    dn = (d / ln[:, None]).astype(np.float32)
+    r = np.zeros(n, dtype=N.RAY_DTYPE)
+    r["ox"], r["oy"], r["oz"] = o[:, 0], o[:, 1], o[:, 2]
+    r["dx"], r["dy"], r["dz"] = dn[:, 0], dn[:, 1], dn[:, 2]
+    r["tmin"] = np.float32(tmin)
+    r["tmax"] = np.float32(tmax)
+    return r
+
+
+@dataclass
+class Camera:
+    """Camera(position, lookat, up, near, far, fov, flip) (camera.h:31-48); fov is horizontal, degrees."""
+    eye: tuple = (0.0, 0.0, 0.0)
+    lookat: tuple = (0.0, 0.0, -1.0)
+    up: tuple = (0.0, 1.0, 0.0)
+    fov: float = 40.0
+    near: float = 1e-3
+    far: float = 1e4
+    flip: bool = False
+
+    def to_c(self) -> N.KzCamera:
+        c = N.KzCamera()
+        c.eye[:] = [float(v) for v in self.eye]
+        c.lookat[:] = [float(v) for v in self.lookat]
+        c.up[:] = [float(v) for v in self.up]
+        c.fov_deg = self.fov
+        c.near_clip = self.near
+        c.far_clip = self.far
+        c.flip = 1 if self.flip else 0
+        return c
+
+
+def render_config(spp=16, max_depth=5, seed=0, wavefront_size=0, rr_min_depth=3, block_size=0,
+                  flags=0) -> N.KzRenderConfig:
+    c = N.KzRenderConfig()
+    c.spp = spp
+    c.max_depth = max_depth
+    c.seed = seed
+    c.wavefront_size = wavefront_size
+    c.rr_min_depth = rr_min_depth
+    c.block_size = block_size
+    c.flags = flags
+    return c
+
+
+# ---------------------------------------------------------------- scene
+class Scene:
+    """Scene handle: meshes + lowered materials + BVH on the GPU."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().kz_scene_create(C.byref(h)))
+        self._h = h
+        self._materials = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().kz_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_mesh(self, verts, indices, material_id=0, is_light=False, xform=None) -> int:
+        """Scene::add_mesh(world, verts, ..., idx, name, shader, is_light) (scene.h:144-160)."""
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        x = None if xform is None else np.ascontiguousarray(xform, np.float32).reshape(12)
+        gid = C.c_int32(-1)
+        check(lib().kz_scene_add_mesh(self._h, _ptr(v), len(v), _ptr(i), len(i), _ptr(x), int(material_id),
+                                      1 if is_light else 0, C.byref(gid)))
+        return gid.value
+
+    def set_materials(self, materials) -> None:
+        m = np.ascontiguousarray(np.asarray(materials, dtype=N.MATERIAL_DTYPE).reshape(-1))
+        self._materials = m
+        check(lib().kz_scene_set_materials(self._h, _ptr(m), len(m)))
+
+    def build_bvh(self) -> None:
+        """Scene::build_bvh / Accelerator::build (accel.h:22-32)."""
+        check(lib().kz_scene_build(self._h))
+
+    build = build_bvh
+
+    def info(self) -> dict:
+        inf = N.KzSceneInfo()
+        check(lib().kz_scene_get_info(self._h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in N.KzSceneInfo._fields_}
+
+    def set_stream(self, stream) -> None:
+        """Run on an external CUDA stream (torch.cuda.Stream or raw handle); None = own stream."""
+        raw = None
+        if stream is not None:
+            raw = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        check(lib().kz_scene_set_stream(self._h, C.c_void_p(raw) if raw else None))
+
+    def synchronize(self) -> None:
+        check(lib().kz_scene_synchronize(self._h))
+
+    # -- intersector ------------------------------------------------------
+    def intersect(self, rays, want_uv=True, out=None):
+        """Closest hits. numpy ray records -> numpy outputs; a CUDA float32
+        tensor (n, 8) -> CUDA tensors (asynchronous; call synchronize())."""
+        if _is_cuda_tensor(rays):
+            n = rays.shape[0]
+            dev = rays.device
+            if out is None:
+                out = {"t": torch.empty(n, dtype=torch.float32, device=dev),
+                       "prim_id": torch.empty(n, dtype=torch.int32, device=dev),
+                       "geom_id": torch.empty(n, dtype=torch.int32, device=dev)}
+                if want_uv:
+                    out["u"] = torch.empty(n, dtype=torch.float32, device=dev)
+                    out["v"] = torch.empty(n, dtype=torch.float32, device=dev)
+            hits = N.KzHits(out["t"].data_ptr(), out["prim_id"].data_ptr(),
+                            out["geom_id"].data_ptr() if "geom_id" in out else None,
+                            out["u"].data_ptr() if "u" in out else None, out["v"].data_ptr() if "v" in out else None)
+            check(lib().kz_intersect_closest(self._h, C.c_void_p(rays.data_ptr()), n, hits, N.KZ_MEM_DEVICE))
+            return out
+        r = np.ascontiguousarray(rays, dtype=N.RAY_DTYPE)
+        n = len(r)
+        res = {"t": np.empty(n, np.float32), "prim_id": np.empty(n, np.uint32), "geom_id": np.empty(n, np.uint32)}
+        if want_uv:
+            res["u"] = np.empty(n, np.float32)
+            res["v"] = np.empty(n, np.float32)
+        hits = N.KzHits(res["t"].ctypes.data, res["prim_id"].ctypes.data, res["geom_id"].ctypes.data,
+                        res["u"].ctypes.data if want_uv else None, res["v"].ctypes.data if want_uv else None)
+        check(lib().kz_intersect_closest(self._h, _ptr(r), n, hits, N.KZ_MEM_HOST))
+        return res
+
+    def occluded(self, rays, out=None):
+        """Any hit in (tmin, tmax] per ray (HitableInterface::occluded, hitable.h:15-33)."""
+        if _is_cuda_tensor(rays):
+            n = rays.shape[0]
+            if out is None:
+                out = torch.empty(n, dtype=torch.uint8, device=rays.device)
+            check(lib().kz_intersect_any(self._h, C.c_void_p(rays.data_ptr()), n, C.c_void_p(out.data_ptr()),
+                                         N.KZ_MEM_DEVICE))
+            return out
+        r = np.ascontiguousarray(rays, dtype=N.RAY_DTYPE)
+        occ = np.empty(len(r), np.uint8)
+        check(lib().kz_intersect_any(self._h, _ptr(r), len(r), _ptr(occ), N.KZ_MEM_HOST))
+        return occ.astype(bool)
+
+    def intersect_stats(self, rays):
+        """(BVH node fetches, triangle fetches) summed over the closest-hit traversal of `rays`."""
+        a, b = C.c_uint64(), C.c_uint64()
+        if _is_cuda_tensor(rays):
+            check(lib().kz_intersect_stats(self._h, C.c_void_p(rays.data_ptr()), rays.shape[0], N.KZ_MEM_DEVICE,
+                                           C.byref(a), C.byref(b)))
+        else:
+            r = np.ascontiguousarray(rays, dtype=N.RAY_DTYPE)
+            check(lib().kz_intersect_stats(self._h, _ptr(r), len(r), N.KZ_MEM_HOST, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+
+# ---------------------------------------------------------------- integrator / renderer
+class PathIntegrator:
+    """PathIntegrator (integrator.cpp:362-561): NEE + power-heuristic MIS + roulette, batched."""
+
+    def __init__(self, max_depth=5, rr_min_depth=3, seed=0, wavefront_size=0, block_size=0):
+        self.cfg = render_config(1, max_depth, seed, wavefront_size, rr_min_depth, block_size)
+        self.scene = None
+        self.last_stats = None
+
+    def setup(self, scene: Scene) -> None:
+        """Integrator::setup(Scene*) (integrator.cpp:20-23)."""
+        self.scene = scene
+
+    def Li(self, rays):
+        """Radiance of each camera ray; ray i uses PCG32 stream (seed, i)."""
+        st = N.KzRenderStats()
+        if _is_cuda_tensor(rays):
+            n = rays.shape[0]
+            out = torch.empty((n, 3), dtype=torch.float32, device=rays.device)
+            check(lib().kz_li_batch(self.scene.handle, C.c_void_p(rays.data_ptr()), n, C.byref(self.cfg),
+                                    C.c_void_p(out.data_ptr()), N.KZ_MEM_DEVICE, C.byref(st)))
+        else:
+            r = np.ascontiguousarray(rays, dtype=N.RAY_DTYPE)
+            out = np.empty((len(r), 3), np.float32)
+            check(lib().kz_li_batch(self.scene.handle, _ptr(r), len(r), C.byref(self.cfg), _ptr(out), N.KZ_MEM_HOST,
+                                    C.byref(st)))
+        self.last_stats = {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_}
+        return out
+
+
+class Renderer:
+    """Renderer(spp).render(scene): per-pixel spp average (renderer.cpp:18-90)."""
+
+    def __init__(self, spp=16, max_depth=5, seed=0, wavefront_size=0, rr_min_depth=3, block_size=0, flags=0):
+        self.cfg = render_config(spp, max_depth, seed, wavefront_size, rr_min_depth, block_size, flags)
+        self.last_stats = None
+
+    def render(self, scene: Scene, camera: Camera, width: int, height: int, fp64: bool = False, device_out=None):
+        """Returns an (H, W, 3) float32 image (and the FP64 accumulation when fp64)."""
+        film = N.KzFilmDesc(width, height)
+        cam = camera.to_c()
+        st = N.KzRenderStats()
+        if device_out is not None:
+            rgb, rgb64 = device_out
+            check(lib().kz_render(scene.handle, C.byref(cam), C.byref(film), C.byref(self.cfg),
+                                  C.c_void_p(rgb.data_ptr()), C.c_void_p(rgb64.data_ptr()) if rgb64 is not None else None,
+                                  N.KZ_MEM_DEVICE, C.byref(st)))
+            self.last_stats = {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_}
+            return rgb, rgb64
+        img = np.empty((height, width, 3), np.float32)
+        img64 = np.empty((height, width, 3), np.float64) if fp64 else None
+        check(lib().kz_render(scene.handle, C.byref(cam), C.byref(film), C.byref(self.cfg), _ptr(img), _ptr(img64),
+                              N.KZ_MEM_HOST, C.byref(st)))
+        self.last_stats = {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_}
+        return (img, img64) if fp64 else img
+
+
+# ---------------------------------------------------------------- closure batches
+def closure_eval(lobes, wi, wo, convention=N.KZ_CONVENTION_REFERENCE):
+    lb = np.ascontiguousarray(lobes, dtype=N.LOBE_DTYPE).reshape(-1)
+    a = np.ascontiguousarray(wi, np.float32).reshape(-1, 3)
+    b = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+    n = len(lb)
+    f = np.empty((n, 3), np.float32)
+    pdf = np.empty(n, np.float32)
+    check(lib().kz_closure_eval_batch(_ptr(lb), _ptr(a), _ptr(b), n, convention, _ptr(f), _ptr(pdf), N.KZ_MEM_HOST))
+    return f, pdf
+
+
+def closure_sample(lobes, wi, u):
+    lb = np.ascontiguousarray(lobes, dtype=N.LOBE_DTYPE).reshape(-1)
+    a = np.ascontiguousarray(wi, np.float32).reshape(-1, 3)
+    uu = np.ascontiguousarray(u, np.float32).reshape(-1, 3)
+    n = len(lb)
+    wo = np.empty((n, 3), np.float32)
+    w = np.empty((n, 3), np.float32)
+    pdf = np.empty(n, np.float32)
+    fl = np.empty(n, np.uint8)
+    check(lib().kz_closure_sample_batch(_ptr(lb), _ptr(a), _ptr(uu), n, _ptr(wo), _ptr(w), _ptr(pdf), _ptr(fl),
+                                        N.KZ_MEM_HOST))
+    return wo, w, pdf, fl

@@ -1,0 +1,862 @@
+// kz_api.cu — the C ABI of include/kazen_gb300.h: scene management, host
+// validation, device memory, and the wavefront render loop driver.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kz_bvh.h"
+#include "kz_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+kz_status fail(kz_status code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define KZ_CUDA(call)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            if (e_ == cudaErrorMemoryAllocation)                                             \
+                return fail(KZ_ERR_OOM, "%s: %s", #call, cudaGetErrorString(e_));           \
+            return fail(KZ_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));              \
+        }                                                                                    \
+    } while (0)
+
+#define KZ_TRY(expr)                   \
+    do {                               \
+        kz_status s_ = (expr);         \
+        if (s_ != KZ_OK) return s_;    \
+    } while (0)
+
+// A growable device allocation.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    kz_status ensure(size_t want) {
+        if (want <= bytes) return KZ_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t b = std::max<size_t>(want, 256);
+        cudaError_t e = cudaMalloc(&ptr, b);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? KZ_ERR_OOM : KZ_ERR_CUDA, "cudaMalloc(%zu): %s", b,
+                        cudaGetErrorString(e));
+        }
+        bytes = b;
+        return KZ_OK;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(ptr);
+    }
+};
+
+struct HostMesh {
+    std::vector<float> verts;  // world space, nverts * 3
+    std::vector<uint32_t> idx;
+    int32_t material;
+    int32_t is_light;
+};
+
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+kz_status validate_lobe(const kz_lobe& l, uint32_t m, uint32_t k) {
+    for (int c = 0; c < 3; ++c)
+        if (!std::isfinite(l.weight[c]) || l.weight[c] < 0.f)
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: weight must be finite and >= 0", m, k);
+    for (int c = 0; c < 12; ++c)
+        if (!std::isfinite(l.params[c]))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: non-finite parameter %d", m, k, c);
+    switch (l.closure_id) {
+    case KZ_CLOSURE_DIFFUSE:
+    case KZ_CLOSURE_KP_MIRROR:
+        return KZ_OK;
+    case KZ_CLOSURE_KP_DIELECTRIC:
+        if (!(l.params[0] > 0.f) || !(l.params[1] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: dielectric iors must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_KP_GLOSS:
+    case KZ_CLOSURE_KP_GLASS:
+        if (l.params[0] != (float)KZ_DIST_GGX && l.params[0] != (float)KZ_DIST_BECKMANN)
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: unknown microfacet distribution", m, k);
+        if (!(l.params[7] > 0.f) || !(l.params[8] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL:
+        if (!(l.params[6] > 0.f) || !(l.params[7] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_CONDUCTOR_GGX:
+        if (!(l.params[3] > 0.f) || !(l.params[4] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_EMISSION:
+    case KZ_CLOSURE_KP_EMITTER:
+        return fail(KZ_ERR_INVALID_ARG,
+                    "material %u lobe %u: emission closures are lowered into kz_material.Le, not lobes", m, k);
+    default:
+        return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: unsupported closure id %u", m, k, l.closure_id);
+    }
+}
+
+}  // namespace
+
+struct kz_scene {
+    std::mutex mu;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<HostMesh> meshes;
+    std::vector<kz_material> materials;
+    bool built = false;
+    kz_scene_info info{};
+
+    // device scene
+    DevBuf nodes, tris, geom_offset, geom_light, mats, lights, light_cdf, light_tris;
+    kz::DevScene dev;
+    DevBuf status;        // uint32 device status word for batch calls
+    uint32_t* status_host = nullptr;  // pinned
+
+    // batch scratch (host-memory calls)
+    DevBuf s_rays, s_t, s_prim, s_geom, s_u, s_v, s_occ, s_ctr;
+
+    // wavefront buffers
+    DevBuf pa[5], pb[5], sh[3], ctr, film, film64;
+    kz::DevCounters* ctr_host = nullptr;  // pinned
+
+    bool cuda_ready = false;
+
+    ~kz_scene() {
+        if (!cuda_ready) return;
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        DevBuf* all[] = {&nodes, &tris, &geom_offset, &geom_light, &mats, &lights, &light_cdf, &light_tris,
+                         &status, &s_rays, &s_t, &s_prim, &s_geom, &s_u, &s_v, &s_occ, &s_ctr, &ctr, &film, &film64};
+        for (DevBuf* b : all) b->release();
+        for (auto& b : pa) b.release();
+        for (auto& b : pb) b.release();
+        for (auto& b : sh) b.release();
+        if (status_host) cudaFreeHost(status_host);
+        if (ctr_host) cudaFreeHost(ctr_host);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+};
+
+namespace {
+
+template <typename T>
+kz_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    KZ_TRY(b.ensure(std::max<size_t>(v.size() * sizeof(T), sizeof(T))));
+    if (!v.empty()) KZ_CUDA(cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return KZ_OK;
+}
+
+kz_status check_scene(kz_scene* s) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    if (!s->built) return fail(KZ_ERR_STATE, "kz_scene_build has not been called since the last change");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return fail(KZ_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return KZ_OK;
+}
+
+kz_status check_mem(int32_t mem) {
+    if (mem != KZ_MEM_HOST && mem != KZ_MEM_DEVICE) return fail(KZ_ERR_INVALID_ARG, "mem must be KZ_MEM_HOST or KZ_MEM_DEVICE");
+    return KZ_OK;
+}
+
+// Waits for the stream and folds the device status word into the result.
+kz_status sync_and_status(kz_scene* s) {
+    KZ_CUDA(cudaMemcpyAsync(s->status_host, s->status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    KZ_CUDA(cudaStreamSynchronize(s->stream));
+    KZ_CUDA(cudaGetLastError());
+    uint32_t st = *s->status_host;
+    if (st != 0) {
+        KZ_CUDA(cudaMemsetAsync(s->status.ptr, 0, sizeof(uint32_t), s->stream));
+        KZ_CUDA(cudaStreamSynchronize(s->stream));
+        if (st == KZ_ERR_STACK) return fail(KZ_ERR_STACK, "traversal stack overflow: affected rays were reported as misses");
+        return fail((kz_status)st, "device reported status %u", st);
+    }
+    return KZ_OK;
+}
+
+// Host-side camera basis (the same float expressions as Camera::init,
+// src/core/camera.h:50-96, restated for a horizontal field of view).
+struct H3 {
+    float x, y, z;
+};
+H3 h_sub(H3 a, H3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+H3 h_cross(H3 a, H3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+H3 h_norm(H3 a) {
+    float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return {a.x / l, a.y / l, a.z / l};
+}
+
+kz_status make_camera(const kz_camera* c, uint32_t W, uint32_t H, kz::DevCamera& out) {
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(c->eye[k]) || !std::isfinite(c->lookat[k]) || !std::isfinite(c->up[k]))
+            return fail(KZ_ERR_INVALID_ARG, "camera vectors must be finite");
+    if (!(c->fov_deg > 0.f && c->fov_deg < 180.f)) return fail(KZ_ERR_INVALID_ARG, "fov_deg must be in (0, 180)");
+    H3 eye{c->eye[0], c->eye[1], c->eye[2]}, look{c->lookat[0], c->lookat[1], c->lookat[2]};
+    H3 up = h_norm(H3{c->up[0], c->up[1], c->up[2]});
+    H3 z = h_norm(h_sub(eye, look));
+    H3 x = h_norm(h_cross(up, z));
+    H3 y = h_cross(z, x);
+    if (!std::isfinite(x.x) || !std::isfinite(z.x)) return fail(KZ_ERR_INVALID_ARG, "degenerate camera basis");
+    out.eye[0] = eye.x; out.eye[1] = eye.y; out.eye[2] = eye.z;
+    out.x[0] = x.x; out.x[1] = x.y; out.x[2] = x.z;
+    out.y[0] = y.x; out.y[1] = y.y; out.y[2] = y.z;
+    out.z[0] = z.x; out.z[1] = z.y; out.z[2] = z.z;
+    out.tan_half = (float)std::tan((double)c->fov_deg * 0.5 * M_PI / 180.0);
+    out.aspect = (float)W / (float)H;
+    out.flip = c->flip ? -1.f : 1.f;
+    out.W = W;
+    out.H = H;
+    return KZ_OK;
+}
+
+kz_status alloc_paths(DevBuf* b, uint32_t cap, kz::PathSoA& p) {
+    const size_t f4 = (size_t)cap * sizeof(float4);
+    for (int k = 0; k < 4; ++k) KZ_TRY(b[k].ensure(f4));
+    KZ_TRY(b[4].ensure((size_t)cap * sizeof(unsigned long long)));
+    p.o4 = b[0].as<float4>();
+    p.d4 = b[1].as<float4>();
+    p.b4 = b[2].as<float4>();
+    p.hit = b[3].as<float4>();
+    p.rng = b[4].as<unsigned long long>();
+    return KZ_OK;
+}
+
+// Wavefront path tracing of `total` paths; contributions are summed into
+// film (and film64) on the device.
+kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* rays_dev, uint64_t total,
+                        const kz_render_config* cfg, float* film, double* film64, kz_render_stats* stats) {
+    kz::PathParams pp;
+    pp.spp = cam ? cfg->spp : 1u;
+    pp.max_depth = cfg->max_depth;
+    pp.rr_min = cfg->rr_min_depth;
+    pp.seed = cfg->seed;
+    pp.camera = cam ? 1u : 0u;
+    uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
+    const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(want, total), 1u << 30));
+    const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
+    if (block % 32 != 0 || block > 1024) return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
+    kz::PathSoA A, B;
+    KZ_TRY(alloc_paths(s->pa, cap, A));
+    KZ_TRY(alloc_paths(s->pb, cap, B));
+    for (int k = 0; k < 3; ++k) KZ_TRY(s->sh[k].ensure((size_t)cap * sizeof(float4)));
+    kz::ShadowSoA sq{s->sh[0].as<float4>(), s->sh[1].as<float4>(), s->sh[2].as<float4>()};
+    KZ_TRY(s->ctr.ensure(sizeof(kz::DevCounters)));
+    kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
+    KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), s->stream));
+    kz_render_stats st{};
+    st.paths = total;
+    uint64_t next = 0;
+    uint32_t nA = 0;
+    cudaStream_t strm = s->stream;
+    const bool timing = (cfg->flags & KZ_RENDER_FLAG_TIMING) != 0;
+    const bool count = (cfg->flags & KZ_RENDER_FLAG_COUNT) != 0;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (timing)
+        for (auto& e : ev) KZ_CUDA(cudaEventCreate(&e));
+    struct EvGuard {
+        cudaEvent_t* e;
+        ~EvGuard() {
+            for (int k = 0; k < 5; ++k)
+                if (e[k]) cudaEventDestroy(e[k]);
+        }
+    } guard{ev};
+    auto mark = [&](int k) -> kz_status {
+        if (timing) KZ_CUDA(cudaEventRecord(ev[k], strm));
+        return KZ_OK;
+    };
+    for (;;) {
+        const uint32_t n_new = (uint32_t)std::min<uint64_t>(cap - nA, total - next);
+        KZ_TRY(mark(0));
+        if (n_new) {
+            if (cam) kz::launch_generate_camera(*cam, pp, A, nA, next, n_new, block, strm);
+            else kz::launch_generate_rays(rays_dev, pp, A, nA, next, n_new, block, strm);
+            st.kernel_launches += 1;
+            nA += n_new;
+            next += n_new;
+        }
+        if (nA == 0) break;
+        KZ_TRY(mark(1));
+        kz::launch_trace_paths(s->dev, A, nA, ctr, count, block, strm);
+        KZ_TRY(mark(2));
+        KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
+        kz::launch_shade(s->dev, pp, A, nA, B, sq, ctr, film, film64, block, strm);
+        KZ_TRY(mark(3));
+        kz::launch_trace_shadow(s->dev, sq, nA, ctr, count, film, film64, block, strm);
+        KZ_TRY(mark(4));
+        st.kernel_launches += 3;
+        KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
+        KZ_CUDA(cudaStreamSynchronize(strm));
+        KZ_CUDA(cudaGetLastError());
+        if (timing) {
+            float ms[4];
+            for (int k = 0; k < 4; ++k) KZ_CUDA(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
+            st.generate_ms += ms[0];
+            st.trace_ms += ms[1];
+            st.shade_ms += ms[2];
+            st.shadow_ms += ms[3];
+        }
+        st.path_bounces += nA;
+        st.shadow_rays += s->ctr_host->n_shadow;
+        st.iterations += 1;
+        if (s->ctr_host->status) {
+            uint32_t code = s->ctr_host->status;
+            return fail((kz_status)code, "device status %u during rendering", code);
+        }
+        nA = s->ctr_host->n_next;
+        std::swap(A, B);
+    }
+    if (count) {
+        st.closest_node_fetches = s->ctr_host->fetch[0];
+        st.closest_tri_fetches = s->ctr_host->fetch[1];
+        st.shadow_node_fetches = s->ctr_host->fetch[2];
+        st.shadow_tri_fetches = s->ctr_host->fetch[3];
+    }
+    if (stats) *stats = st;
+    return KZ_OK;
+}
+
+kz_status init_cuda(kz_scene* s) {
+    if (s->cuda_ready) return KZ_OK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(KZ_ERR_NO_DEVICE, "no CUDA device is visible");
+    }
+    KZ_CUDA(cudaGetDevice(&s->device));
+    s->cuda_ready = true;  // from here on the destructor releases what exists
+    KZ_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+    KZ_CUDA(cudaMallocHost((void**)&s->status_host, sizeof(uint32_t)));
+    KZ_CUDA(cudaMallocHost((void**)&s->ctr_host, sizeof(kz::DevCounters)));
+    if (!s->stream) s->stream = s->own_stream;
+    KZ_TRY(s->status.ensure(sizeof(uint32_t)));
+    KZ_CUDA(cudaMemset(s->status.ptr, 0, sizeof(uint32_t)));
+    return KZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t kz_abi_version(void) { return KZ_ABI_VERSION; }
+
+const char* kz_last_error_string(void) { return g_last_error.c_str(); }
+
+int32_t kz_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// Scene handles are created without touching CUDA, so meshes and materials
+// can be described (and validated) on any host; the CUDA context, stream and
+// device buffers are set up by the first kz_scene_build on the then-current
+// device.
+kz_status kz_scene_create(kz_scene** out_scene) {
+    if (!out_scene) return fail(KZ_ERR_INVALID_ARG, "out_scene is NULL");
+    *out_scene = new kz_scene();
+    return KZ_OK;
+}
+
+kz_status kz_scene_destroy(kz_scene* scene) {
+    if (!scene) return KZ_OK;
+    delete scene;
+    return KZ_OK;
+}
+
+kz_status kz_scene_add_mesh(kz_scene* s, const float* xyz, uint32_t nverts, const uint32_t* idx, uint32_t ntris,
+                            const float* xform12, int32_t material_id, int32_t is_light, int32_t* out_geom_id) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if ((nverts && !xyz) || (ntris && !idx)) return fail(KZ_ERR_INVALID_ARG, "NULL vertex or index array");
+    if (material_id < 0) return fail(KZ_ERR_INVALID_ARG, "material_id must be >= 0");
+    if (xform12)
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(xform12[k])) return fail(KZ_ERR_INVALID_ARG, "transform has a non-finite entry");
+    HostMesh m;
+    m.material = material_id;
+    m.is_light = is_light ? 1 : 0;
+    m.verts.resize((size_t)nverts * 3);
+    for (uint32_t i = 0; i < nverts; ++i) {
+        const float* p = xyz + (size_t)i * 3;
+        if (!finite3(p)) return fail(KZ_ERR_INVALID_ARG, "vertex %u is not finite", i);
+        float* q = &m.verts[(size_t)i * 3];
+        if (xform12) {
+            for (int r = 0; r < 3; ++r) {
+                const float* row = xform12 + r * 4;
+                q[r] = row[0] * p[0] + row[1] * p[1] + row[2] * p[2] + row[3];
+            }
+            if (!finite3(q)) return fail(KZ_ERR_INVALID_ARG, "transformed vertex %u is not finite", i);
+        } else {
+            q[0] = p[0];
+            q[1] = p[1];
+            q[2] = p[2];
+        }
+    }
+    m.idx.assign(idx, idx + (size_t)ntris * 3);
+    for (size_t k = 0; k < m.idx.size(); ++k)
+        if (m.idx[k] >= nverts) return fail(KZ_ERR_INVALID_ARG, "index %zu (= %u) is out of range", k, m.idx[k]);
+    s->meshes.push_back(std::move(m));
+    s->built = false;
+    if (out_geom_id) *out_geom_id = (int32_t)s->meshes.size() - 1;
+    return KZ_OK;
+}
+
+kz_status kz_scene_set_materials(kz_scene* s, const kz_material* materials, uint32_t n) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    if (n && !materials) return fail(KZ_ERR_INVALID_ARG, "materials is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (uint32_t m = 0; m < n; ++m) {
+        const kz_material& mt = materials[m];
+        if (mt.n_lobes > KZ_MAX_LOBES) return fail(KZ_ERR_INVALID_ARG, "material %u: more than %d lobes", m, KZ_MAX_LOBES);
+        for (int c = 0; c < 3; ++c)
+            if (!std::isfinite(mt.Le[c]) || mt.Le[c] < 0.f)
+                return fail(KZ_ERR_INVALID_ARG, "material %u: Le must be finite and >= 0", m);
+        for (uint32_t k = 0; k < mt.n_lobes; ++k) KZ_TRY(validate_lobe(mt.lobes[k], m, k));
+    }
+    s->materials.assign(materials, materials + n);
+    s->built = false;
+    return KZ_OK;
+}
+
+kz_status kz_scene_build(kz_scene* s) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    // validate everything on the host before any device work
+    for (size_t g = 0; g < s->meshes.size(); ++g)
+        if ((size_t)s->meshes[g].material >= s->materials.size())
+            return fail(KZ_ERR_INVALID_ARG, "mesh %zu uses material %d but only %zu are set", g,
+                        s->meshes[g].material, s->materials.size());
+    KZ_TRY(init_cuda(s));
+    KZ_CUDA(cudaSetDevice(s->device));
+    // global triangle order = mesh order
+    uint64_t total = 0;
+    for (const auto& m : s->meshes) total += m.idx.size() / 3;
+    if (total > 0x7fffffffull) return fail(KZ_ERR_INVALID_ARG, "too many triangles (%llu)", (unsigned long long)total);
+    std::vector<float> tv((size_t)total * 9);
+    std::vector<uint32_t> tgeom((size_t)total);
+    std::vector<uint32_t> goff(s->meshes.size() + 1);
+    std::vector<int32_t> gmat(s->meshes.size());
+    size_t t = 0;
+    for (size_t g = 0; g < s->meshes.size(); ++g) {
+        const HostMesh& m = s->meshes[g];
+        if ((size_t)m.material >= s->materials.size())
+            return fail(KZ_ERR_INVALID_ARG, "mesh %zu uses material %d but only %zu are set", g, m.material,
+                        s->materials.size());
+        goff[g] = (uint32_t)t;
+        gmat[g] = m.material;
+        for (size_t k = 0; k < m.idx.size() / 3; ++k, ++t) {
+            for (int c = 0; c < 3; ++c) {
+                const float* p = &m.verts[(size_t)m.idx[k * 3 + c] * 3];
+                tv[t * 9 + c * 3] = p[0];
+                tv[t * 9 + c * 3 + 1] = p[1];
+                tv[t * 9 + c * 3 + 2] = p[2];
+            }
+            tgeom[t] = (uint32_t)g;
+        }
+    }
+    goff[s->meshes.size()] = (uint32_t)t;
+    kz::BvhBuildInput in{tv.data(), (uint32_t)total, tgeom.data(), gmat.data()};
+    kz::BvhBuildOutput out;
+    kz::build_bvh(in, 4, out);
+
+    // lights: one per emissive mesh with triangles, area CDF in triangle order
+    std::vector<kz::DevLight> lights;
+    std::vector<float> cdf, ltris;
+    std::vector<int32_t> glight(s->meshes.size(), -1);
+    for (size_t g = 0; g < s->meshes.size(); ++g) {
+        const HostMesh& m = s->meshes[g];
+        const uint32_t nt = (uint32_t)(m.idx.size() / 3);
+        if (!m.is_light || nt == 0) continue;
+        kz::DevLight L{};
+        L.tri_begin = (uint32_t)(ltris.size() / 12);
+        L.tri_count = nt;
+        L.cdf_begin = (uint32_t)cdf.size();
+        L.geom = (uint32_t)g;
+        const kz_material& mt = s->materials[(size_t)m.material];
+        L.Le[0] = mt.Le[0];
+        L.Le[1] = mt.Le[1];
+        L.Le[2] = mt.Le[2];
+        std::vector<float> c(1, 0.f);
+        for (uint32_t k = 0; k < nt; ++k) {
+            const float* q = &tv[(size_t)(goff[g] + k) * 9];
+            const float e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+            const float e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+            const float cx = e1[1] * e2[2] - e1[2] * e2[1];
+            const float cy = e1[2] * e2[0] - e1[0] * e2[2];
+            const float cz = e1[0] * e2[1] - e1[1] * e2[0];
+            const float area = 0.5f * std::sqrt(cx * cx + cy * cy + cz * cz);
+            c.push_back(c.back() + area);
+            for (int v = 0; v < 3; ++v) {
+                ltris.push_back(q[v * 3]);
+                ltris.push_back(q[v * 3 + 1]);
+                ltris.push_back(q[v * 3 + 2]);
+                ltris.push_back(0.f);
+            }
+        }
+        const float sum = c.back();
+        if (!(sum > 0.f)) return fail(KZ_ERR_INVALID_ARG, "light mesh %zu has zero area", g);
+        const float nrm = 1.f / sum;
+        for (size_t k = 1; k < c.size(); ++k) c[k] *= nrm;
+        c.back() = 1.f;
+        L.area = sum;
+        cdf.insert(cdf.end(), c.begin(), c.end());
+        glight[g] = (int32_t)lights.size();
+        lights.push_back(L);
+    }
+
+    cudaStream_t st = s->stream;
+    KZ_TRY(upload(s->nodes, out.nodes, st));
+    KZ_TRY(upload(s->tris, out.tris, st));
+    KZ_TRY(upload(s->geom_offset, goff, st));
+    KZ_TRY(upload(s->geom_light, glight, st));
+    KZ_TRY(upload(s->mats, s->materials, st));
+    KZ_TRY(upload(s->lights, lights, st));
+    KZ_TRY(upload(s->light_cdf, cdf, st));
+    KZ_TRY(upload(s->light_tris, ltris, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+
+    kz::DevScene& d = s->dev;
+    d.nodes = s->nodes.as<float4>();
+    d.tris = s->tris.as<float4>();
+    d.n_nodes = out.n_nodes;
+    d.n_tris = (uint32_t)total;
+    d.geom_offset = s->geom_offset.as<uint32_t>();
+    d.geom_light = s->geom_light.as<int32_t>();
+    d.materials = s->mats.as<kz_material>();
+    d.n_materials = (uint32_t)s->materials.size();
+    d.lights = s->lights.as<kz::DevLight>();
+    d.light_cdf = s->light_cdf.as<float>();
+    d.light_tris = s->light_tris.as<float4>();
+    d.n_lights = (uint32_t)lights.size();
+
+    s->info.n_meshes = s->meshes.size();
+    s->info.n_triangles = total;
+    s->info.n_lights = lights.size();
+    s->info.n_bvh_nodes = out.n_nodes;
+    s->info.bvh_bytes = (uint64_t)out.n_nodes * 64;
+    s->info.triangle_bytes = total * 48;
+    s->info.bvh_depth = out.depth;
+    s->info.built = 1;
+    s->built = true;
+    return KZ_OK;
+}
+
+kz_status kz_scene_get_info(kz_scene* s, kz_scene_info* out) {
+    if (!s || !out) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->info;
+    out->built = s->built ? 1 : 0;
+    return KZ_OK;
+}
+
+kz_status kz_scene_set_stream(kz_scene* s, void* cuda_stream) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->cuda_ready) KZ_CUDA(cudaStreamSynchronize(s->stream));
+    s->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : s->own_stream;
+    return KZ_OK;
+}
+
+kz_status kz_scene_synchronize(kz_scene* s) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->cuda_ready) return KZ_OK;
+    KZ_CUDA(cudaSetDevice(s->device));
+    return sync_and_status(s);
+}
+
+kz_status kz_intersect_closest(kz_scene* s, const kz_ray* rays, uint64_t n, kz_hits hits, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    if (n == 0) return KZ_OK;
+    if (!rays || !hits.t || !hits.prim_id) return fail(KZ_ERR_INVALID_ARG, "rays, hits.t and hits.prim_id are required");
+    cudaStream_t st = s->stream;
+    if (s->dev.n_tris == 0) {
+        // nothing to hit: every ray misses
+        std::vector<kz_ray> hr;
+        const kz_ray* src = rays;
+        if (mem == KZ_MEM_DEVICE) {
+            hr.resize(n);
+            KZ_CUDA(cudaMemcpyAsync(hr.data(), rays, n * sizeof(kz_ray), cudaMemcpyDeviceToHost, st));
+            KZ_CUDA(cudaStreamSynchronize(st));
+            src = hr.data();
+        }
+        std::vector<float> t(n);
+        std::vector<uint32_t> inv(n, KZ_INVALID_ID);
+        std::vector<float> z(n, 0.f);
+        for (uint64_t i = 0; i < n; ++i) t[i] = src[i].tmax;
+        auto put = [&](void* dst, const void* srcp, size_t bytes) -> kz_status {
+            if (!dst) return KZ_OK;
+            if (mem == KZ_MEM_DEVICE) KZ_CUDA(cudaMemcpyAsync(dst, srcp, bytes, cudaMemcpyHostToDevice, st));
+            else std::memcpy(dst, srcp, bytes);
+            return KZ_OK;
+        };
+        KZ_TRY(put(hits.t, t.data(), n * 4));
+        KZ_TRY(put(hits.prim_id, inv.data(), n * 4));
+        KZ_TRY(put(hits.geom_id, inv.data(), n * 4));
+        KZ_TRY(put(hits.u, z.data(), n * 4));
+        KZ_TRY(put(hits.v, z.data(), n * 4));
+        KZ_CUDA(cudaStreamSynchronize(st));
+        return KZ_OK;
+    }
+    if (mem == KZ_MEM_DEVICE) {
+        kz::launch_intersect_closest(s->dev, rays, n, hits, s->status.as<uint32_t>(), st);
+        KZ_CUDA(cudaGetLastError());
+        return KZ_OK;
+    }
+    KZ_TRY(s->s_rays.ensure(n * sizeof(kz_ray)));
+    KZ_TRY(s->s_t.ensure(n * 4));
+    KZ_TRY(s->s_prim.ensure(n * 4));
+    if (hits.geom_id) KZ_TRY(s->s_geom.ensure(n * 4));
+    if (hits.u) KZ_TRY(s->s_u.ensure(n * 4));
+    if (hits.v) KZ_TRY(s->s_v.ensure(n * 4));
+    KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
+    kz_hits dh{s->s_t.as<float>(), s->s_prim.as<uint32_t>(), hits.geom_id ? s->s_geom.as<uint32_t>() : nullptr,
+               hits.u ? s->s_u.as<float>() : nullptr, hits.v ? s->s_v.as<float>() : nullptr};
+    kz::launch_intersect_closest(s->dev, s->s_rays.as<kz_ray>(), n, dh, s->status.as<uint32_t>(), st);
+    KZ_CUDA(cudaGetLastError());
+    KZ_CUDA(cudaMemcpyAsync(hits.t, dh.t, n * 4, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaMemcpyAsync(hits.prim_id, dh.prim_id, n * 4, cudaMemcpyDeviceToHost, st));
+    if (hits.geom_id) KZ_CUDA(cudaMemcpyAsync(hits.geom_id, dh.geom_id, n * 4, cudaMemcpyDeviceToHost, st));
+    if (hits.u) KZ_CUDA(cudaMemcpyAsync(hits.u, dh.u, n * 4, cudaMemcpyDeviceToHost, st));
+    if (hits.v) KZ_CUDA(cudaMemcpyAsync(hits.v, dh.v, n * 4, cudaMemcpyDeviceToHost, st));
+    return sync_and_status(s);
+}
+
+kz_status kz_intersect_any(kz_scene* s, const kz_ray* rays, uint64_t n, uint8_t* occluded, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    if (n == 0) return KZ_OK;
+    if (!rays || !occluded) return fail(KZ_ERR_INVALID_ARG, "rays and occluded are required");
+    cudaStream_t st = s->stream;
+    if (s->dev.n_tris == 0) {
+        if (mem == KZ_MEM_DEVICE) KZ_CUDA(cudaMemsetAsync(occluded, 0, n, st));
+        else std::memset(occluded, 0, n);
+        return KZ_OK;
+    }
+    if (mem == KZ_MEM_DEVICE) {
+        kz::launch_intersect_any(s->dev, rays, n, occluded, s->status.as<uint32_t>(), st);
+        KZ_CUDA(cudaGetLastError());
+        return KZ_OK;
+    }
+    KZ_TRY(s->s_rays.ensure(n * sizeof(kz_ray)));
+    KZ_TRY(s->s_occ.ensure(n));
+    KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
+    kz::launch_intersect_any(s->dev, s->s_rays.as<kz_ray>(), n, s->s_occ.as<uint8_t>(), s->status.as<uint32_t>(), st);
+    KZ_CUDA(cudaGetLastError());
+    KZ_CUDA(cudaMemcpyAsync(occluded, s->s_occ.ptr, n, cudaMemcpyDeviceToHost, st));
+    return sync_and_status(s);
+}
+
+kz_status kz_intersect_stats(kz_scene* s, const kz_ray* rays, uint64_t n, int32_t mem, uint64_t* out_nodes,
+                             uint64_t* out_tris) {
+    KZ_TRY(check_mem(mem));
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    if (!out_nodes || !out_tris) return fail(KZ_ERR_INVALID_ARG, "output counters are required");
+    *out_nodes = *out_tris = 0;
+    if (n == 0 || s->dev.n_tris == 0) return KZ_OK;
+    if (!rays) return fail(KZ_ERR_INVALID_ARG, "rays is NULL");
+    cudaStream_t st = s->stream;
+    const kz_ray* dr = rays;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(s->s_rays.ensure(n * sizeof(kz_ray)));
+        KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
+        dr = s->s_rays.as<kz_ray>();
+    }
+    KZ_TRY(s->s_ctr.ensure(2 * sizeof(unsigned long long)));
+    KZ_CUDA(cudaMemsetAsync(s->s_ctr.ptr, 0, 2 * sizeof(unsigned long long), st));
+    kz::launch_intersect_stats(s->dev, dr, n, s->s_ctr.as<unsigned long long>(), s->status.as<uint32_t>(), st);
+    KZ_CUDA(cudaGetLastError());
+    unsigned long long h[2];
+    KZ_CUDA(cudaMemcpyAsync(h, s->s_ctr.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    KZ_TRY(sync_and_status(s));
+    *out_nodes = h[0];
+    *out_tris = h[1];
+    return KZ_OK;
+}
+
+kz_status kz_closure_eval_batch(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n, int32_t convention,
+                                float* out_f, float* out_pdf, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (convention != KZ_CONVENTION_REFERENCE && convention != KZ_CONVENTION_INTEGRATOR)
+        return fail(KZ_ERR_INVALID_ARG, "unknown convention %d", convention);
+    if (n == 0) return KZ_OK;
+    if (!lobes || !wi || !wo || !out_f || !out_pdf) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    if (kz_device_count() == 0) return fail(KZ_ERR_NO_DEVICE, "no CUDA device is visible");
+    cudaStream_t st = cudaStreamPerThread;
+    if (mem == KZ_MEM_DEVICE) {
+        kz::launch_closure_eval(lobes, wi, wo, n, convention, out_f, out_pdf, st);
+        KZ_CUDA(cudaGetLastError());
+        KZ_CUDA(cudaStreamSynchronize(st));
+        return KZ_OK;
+    }
+    DevBuf bl, bi, bo, bf, bp;
+    KZ_TRY(bl.ensure(n * sizeof(kz_lobe)));
+    KZ_TRY(bi.ensure(n * 12));
+    KZ_TRY(bo.ensure(n * 12));
+    KZ_TRY(bf.ensure(n * 12));
+    KZ_TRY(bp.ensure(n * 4));
+    KZ_CUDA(cudaMemcpyAsync(bl.ptr, lobes, n * sizeof(kz_lobe), cudaMemcpyHostToDevice, st));
+    KZ_CUDA(cudaMemcpyAsync(bi.ptr, wi, n * 12, cudaMemcpyHostToDevice, st));
+    KZ_CUDA(cudaMemcpyAsync(bo.ptr, wo, n * 12, cudaMemcpyHostToDevice, st));
+    kz::launch_closure_eval(bl.as<kz_lobe>(), bi.as<float>(), bo.as<float>(), n, convention, bf.as<float>(),
+                            bp.as<float>(), st);
+    KZ_CUDA(cudaGetLastError());
+    KZ_CUDA(cudaMemcpyAsync(out_f, bf.ptr, n * 12, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaMemcpyAsync(out_pdf, bp.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    bl.release(); bi.release(); bo.release(); bf.release(); bp.release();
+    return KZ_OK;
+}
+
+kz_status kz_closure_sample_batch(const kz_lobe* lobes, const float* wi, const float* u, uint64_t n, float* out_wo,
+                                  float* out_weight, float* out_pdf, uint8_t* out_flags, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (n == 0) return KZ_OK;
+    if (!lobes || !wi || !u || !out_wo || !out_weight || !out_pdf || !out_flags)
+        return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    if (kz_device_count() == 0) return fail(KZ_ERR_NO_DEVICE, "no CUDA device is visible");
+    cudaStream_t st = cudaStreamPerThread;
+    if (mem == KZ_MEM_DEVICE) {
+        kz::launch_closure_sample(lobes, wi, u, n, out_wo, out_weight, out_pdf, out_flags, st);
+        KZ_CUDA(cudaGetLastError());
+        KZ_CUDA(cudaStreamSynchronize(st));
+        return KZ_OK;
+    }
+    DevBuf bl, bi, bu, bo, bw, bp, bfl;
+    KZ_TRY(bl.ensure(n * sizeof(kz_lobe)));
+    KZ_TRY(bi.ensure(n * 12));
+    KZ_TRY(bu.ensure(n * 12));
+    KZ_TRY(bo.ensure(n * 12));
+    KZ_TRY(bw.ensure(n * 12));
+    KZ_TRY(bp.ensure(n * 4));
+    KZ_TRY(bfl.ensure(n));
+    KZ_CUDA(cudaMemcpyAsync(bl.ptr, lobes, n * sizeof(kz_lobe), cudaMemcpyHostToDevice, st));
+    KZ_CUDA(cudaMemcpyAsync(bi.ptr, wi, n * 12, cudaMemcpyHostToDevice, st));
+    KZ_CUDA(cudaMemcpyAsync(bu.ptr, u, n * 12, cudaMemcpyHostToDevice, st));
+    kz::launch_closure_sample(bl.as<kz_lobe>(), bi.as<float>(), bu.as<float>(), n, bo.as<float>(), bw.as<float>(),
+                              bp.as<float>(), bfl.as<uint8_t>(), st);
+    KZ_CUDA(cudaGetLastError());
+    KZ_CUDA(cudaMemcpyAsync(out_wo, bo.ptr, n * 12, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaMemcpyAsync(out_weight, bw.ptr, n * 12, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaMemcpyAsync(out_pdf, bp.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaMemcpyAsync(out_flags, bfl.ptr, n, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    bl.release(); bi.release(); bu.release(); bo.release(); bw.release(); bp.release(); bfl.release();
+    return KZ_OK;
+}
+
+static kz_status check_cfg(const kz_render_config* cfg) {
+    if (!cfg) return fail(KZ_ERR_INVALID_ARG, "cfg is NULL");
+    if (cfg->spp == 0) return fail(KZ_ERR_INVALID_ARG, "spp must be >= 1");
+    if (cfg->max_depth == 0 || cfg->max_depth > 255) return fail(KZ_ERR_INVALID_ARG, "max_depth must be in [1, 255]");
+    return KZ_OK;
+}
+
+kz_status kz_li_batch(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_render_config* cfg, float* out_rgb,
+                      int32_t mem, kz_render_stats* out_stats) {
+    KZ_TRY(check_mem(mem));
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    KZ_TRY(check_cfg(cfg));
+    if (n == 0) return KZ_OK;
+    if (n > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "at most 2^32-1 rays per call");
+    if (!rays || !out_rgb) return fail(KZ_ERR_INVALID_ARG, "rays and out_rgb are required");
+    cudaStream_t st = s->stream;
+    const kz_ray* dr = rays;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(s->s_rays.ensure(n * sizeof(kz_ray)));
+        KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
+        dr = s->s_rays.as<kz_ray>();
+    }
+    float* film = out_rgb;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(s->film.ensure(n * 12));
+        film = s->film.as<float>();
+    }
+    KZ_CUDA(cudaMemsetAsync(film, 0, n * 12, st));
+    KZ_TRY(run_wavefront(s, nullptr, dr, n, cfg, film, nullptr, out_stats));
+    if (mem == KZ_MEM_HOST) {
+        KZ_CUDA(cudaMemcpyAsync(out_rgb, film, n * 12, cudaMemcpyDeviceToHost, st));
+        KZ_CUDA(cudaStreamSynchronize(st));
+    }
+    return KZ_OK;
+}
+
+kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd, const kz_render_config* cfg,
+                    float* out_rgb, double* out_rgb64, int32_t mem, kz_render_stats* out_stats) {
+    KZ_TRY(check_mem(mem));
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    KZ_TRY(check_cfg(cfg));
+    if (!camera || !fd) return fail(KZ_ERR_INVALID_ARG, "camera and film are required");
+    if (!out_rgb) return fail(KZ_ERR_INVALID_ARG, "out_rgb is required");
+    if (fd->width == 0 || fd->height == 0) return fail(KZ_ERR_INVALID_ARG, "film size must be > 0");
+    const uint64_t npix = (uint64_t)fd->width * fd->height;
+    const uint64_t total = npix * cfg->spp;
+    if (total > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "width*height*spp must be < 2^32");
+    kz::DevCamera cam;
+    KZ_TRY(make_camera(camera, fd->width, fd->height, cam));
+    cudaStream_t st = s->stream;
+    float* film = out_rgb;
+    double* film64 = out_rgb64;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(s->film.ensure(npix * 12));
+        film = s->film.as<float>();
+        if (out_rgb64) {
+            KZ_TRY(s->film64.ensure(npix * 24));
+            film64 = s->film64.as<double>();
+        }
+    }
+    KZ_CUDA(cudaMemsetAsync(film, 0, npix * 12, st));
+    if (film64) KZ_CUDA(cudaMemsetAsync(film64, 0, npix * 24, st));
+    KZ_TRY(run_wavefront(s, &cam, nullptr, total, cfg, film, film64, out_stats));
+    kz::launch_scale(film, nullptr, npix * 3, 1.0f / (float)cfg->spp, 0.0, st);
+    if (film64) kz::launch_scale(nullptr, film64, npix * 3, 0.f, 1.0 / (double)cfg->spp, st);
+    KZ_CUDA(cudaGetLastError());
+    if (mem == KZ_MEM_HOST) {
+        KZ_CUDA(cudaMemcpyAsync(out_rgb, film, npix * 12, cudaMemcpyDeviceToHost, st));
+        if (out_rgb64) KZ_CUDA(cudaMemcpyAsync(out_rgb64, film64, npix * 24, cudaMemcpyDeviceToHost, st));
+    }
+    KZ_CUDA(cudaStreamSynchronize(st));
+    return KZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// kz_internal.h — device data structures shared by the C-ABI layer
+// (kz_api.cu) and the kernels (kz_kernels.cu). Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/kazen_gb300.h"
+
+namespace kz {
+
+// One GeometryLight (src/core/light.cpp:46-86): an emissive mesh sampled by
+// triangle area (TriangleMesh::sample, src/core/shape.cpp:591-613).
+struct DevLight {
+    uint32_t tri_begin;   // first record in DevScene::light_tris (3 float4 each)
+    uint32_t tri_count;
+    uint32_t cdf_begin;   // tri_count + 1 entries in DevScene::light_cdf
+    uint32_t geom;
+    float area;           // world-space area of the whole mesh
+    float Le[3];
+};
+
+struct DevScene {
+    const float4* nodes = nullptr;      // n_nodes * 4
+    const float4* tris = nullptr;       // n_tris * 3, leaf order
+    uint32_t n_nodes = 0, n_tris = 0;
+    const uint32_t* geom_offset = nullptr;  // first global triangle id per mesh
+    const int32_t* geom_light = nullptr;    // light index per mesh or -1
+    const kz_material* materials = nullptr;
+    uint32_t n_materials = 0;
+    const DevLight* lights = nullptr;
+    const float* light_cdf = nullptr;
+    const float4* light_tris = nullptr;
+    uint32_t n_lights = 0;
+};
+
+// Camera basis computed on the host (same float expressions the CPU
+// restatement uses) and the film size.
+struct DevCamera {
+    float eye[3], x[3], y[3], z[3];
+    float tan_half, aspect, flip;
+    uint32_t W, H;
+};
+
+// Wavefront path state, structure of arrays (capacity entries each):
+//   o4  = (origin.xyz, pdf of the BSDF sample that made this ray)
+//   d4  = (direction.xyz, bits: vertex index | specular flag << 8)
+//   b4  = (throughput.xyz, bits: path id)
+//   hit = (t, u, v, bits: triangle record or -1)
+//   rng = PCG32 state (the stream increment is recomputed from the path id)
+struct PathSoA {
+    float4* o4;
+    float4* d4;
+    float4* b4;
+    float4* hit;
+    unsigned long long* rng;
+};
+
+// Shadow-ray queue: (origin.xyz, tmax), (direction.xyz, bits: film index),
+// (contribution.rgb, unused).
+struct ShadowSoA {
+    float4* o4;
+    float4* d4;
+    float4* c4;
+};
+
+struct PathParams {
+    uint32_t spp;
+    uint32_t max_depth;
+    uint32_t rr_min;
+    uint64_t seed;
+    uint32_t camera;  // 1: paths start at the camera, 0: at rays[] (Li batch)
+};
+
+// Counters the stage kernels update on the device.
+struct DevCounters {
+    uint32_t n_next;     // continuing paths written by shade
+    uint32_t n_shadow;   // shadow rays queued by shade
+    uint32_t status;     // device-side error (KZ_ERR_STACK ...)
+    uint32_t pad;
+    unsigned long long fetch[4];  // closest nodes, closest tris, shadow nodes, shadow tris
+};
+
+// ---- launchers (kz_kernels.cu) -------------------------------------------
+void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
+                              uint32_t* status, cudaStream_t st);
+void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ,
+                          uint32_t* status, cudaStream_t st);
+void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n,
+                            unsigned long long* counters /*2*/, uint32_t* status, cudaStream_t st);
+void launch_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n,
+                         int convention, float* f, float* pdf, cudaStream_t st);
+void launch_closure_sample(const kz_lobe* lobes, const float* wi, const float* u, uint64_t n,
+                           float* wo, float* weight, float* pdf, uint8_t* flags, cudaStream_t st);
+
+void launch_generate_camera(const DevCamera& cam, const PathParams& pp, PathSoA dst, uint32_t dst_offset,
+                            uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st);
+void launch_generate_rays(const kz_ray* rays, const PathParams& pp, PathSoA dst, uint32_t dst_offset,
+                          uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st);
+void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* ctr, bool count, uint32_t block,
+                        cudaStream_t st);
+void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
+                  ShadowSoA sq, DevCounters* ctr, float* film, double* film64, uint32_t block,
+                  cudaStream_t st);
+void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
+                         float* film, double* film64, uint32_t block, cudaStream_t st);
+void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st);
+
+}  // namespace kz

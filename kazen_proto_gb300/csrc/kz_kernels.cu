@@ -1,0 +1,518 @@
+// kz_kernels.cu — sm_103a kernels of the kazen hot path: batch intersection,
+// closure batches, and the wavefront path integrator stages
+// (generate / trace / shade / shadow) over structure-of-arrays path state.
+//
+// The wavefront stages restate PathIntegrator::Li
+// (src/core/integrator.cpp:362-561 in kazen_proto) with the estimator
+// corrections listed at the top of k_shade. Random numbers: PCG32 stream
+// (seed, path id); a camera path first draws the pixel jitter (2 floats,
+// Renderer::render, src/core/renderer.cpp:57), then 9 floats per shaded
+// vertex in a fixed order whatever branches run:
+//   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
+//   [5] lobe pick   [6,7,8] lobe sample
+#include "kz_internal.h"
+#include "kz_traverse.cuh"
+
+namespace kz {
+namespace {
+
+constexpr uint32_t kSpecularFlag = 1u << 8;
+
+__device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
+    if (status) atomicCAS(status, 0u, code);
+}
+
+__device__ __forceinline__ f3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
+__device__ __forceinline__ uint32_t warp_append(bool pred, uint32_t* counter) {
+    const unsigned mask = __activemask();
+    const unsigned ballot = __ballot_sync(mask, pred);
+    if (!pred) return 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(ballot, base, leader);
+    return base + (uint32_t)__popc(ballot & ((1u << lane) - 1u));
+}
+
+// ------------------------------------------------------------------ batch intersection
+__global__ void k_intersect_closest(DevScene s, const kz_ray* __restrict__ rays, uint64_t n, kz_hits hits,
+                                    uint32_t* status) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(rays + i);
+    const float4 a = __ldg(rp), b = __ldg(rp + 1);
+    TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
+    HitRec h;
+    uint32_t dn = 0, dt = 0;
+    if (!trace_closest<false>(s, r, b.w, h, dn, dt)) {
+        set_status(status, KZ_ERR_STACK);
+        h.t = b.w;
+        h.prim = KZ_INVALID_ID;
+        h.rec = -1;
+    }
+    hits.t[i] = h.t;
+    uint32_t geom = KZ_INVALID_ID, local = KZ_INVALID_ID;
+    if (h.rec >= 0) {
+        geom = __float_as_uint(__ldg(s.tris + (size_t)h.rec * 3 + 1).w);
+        local = h.prim - __ldg(s.geom_offset + geom);
+    }
+    hits.prim_id[i] = local;
+    if (hits.geom_id) hits.geom_id[i] = geom;
+    if (hits.u) hits.u[i] = h.u;
+    if (hits.v) hits.v[i] = h.v;
+}
+
+__global__ void k_intersect_any(DevScene s, const kz_ray* __restrict__ rays, uint64_t n, uint8_t* occ,
+                                uint32_t* status) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(rays + i);
+    const float4 a = __ldg(rp), b = __ldg(rp + 1);
+    TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
+    bool overflow;
+    uint32_t dn = 0, dt = 0;
+    bool hit = trace_any<false>(s, r, b.w, overflow, dn, dt);
+    if (overflow) set_status(status, KZ_ERR_STACK);
+    occ[i] = hit ? 1 : 0;
+}
+
+__global__ void k_intersect_stats(DevScene s, const kz_ray* __restrict__ rays, uint64_t n,
+                                  unsigned long long* counters, uint32_t* status) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nn = 0, nt = 0;
+    if (i < n) {
+        const float4* rp = reinterpret_cast<const float4*>(rays + i);
+        const float4 a = __ldg(rp), b = __ldg(rp + 1);
+        TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
+        HitRec h;
+        if (!trace_closest<true>(s, r, b.w, h, nn, nt)) set_status(status, KZ_ERR_STACK);
+    }
+    // warp reduction, one atomic per warp
+    unsigned long long a0 = nn, a1 = nt;
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counters, a0);
+        atomicAdd(counters + 1, a1);
+    }
+}
+
+// ------------------------------------------------------------------ closures
+__global__ void k_closure_eval(const kz_lobe* __restrict__ lobes, const float* __restrict__ wi,
+                               const float* __restrict__ wo, uint64_t n, int conv, float* f, float* pdf) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const kz_lobe l = lobes[i];
+    const f3 a = ld3(wi + 3 * i), b = ld3(wo + 3 * i);
+    LobeEval e = conv == KZ_CONVENTION_REFERENCE ? lobe_eval_reference(l, a, b) : lobe_eval(l, a, b);
+    f[3 * i] = e.f.x;
+    f[3 * i + 1] = e.f.y;
+    f[3 * i + 2] = e.f.z;
+    pdf[i] = e.pdf;
+}
+
+__global__ void k_closure_sample(const kz_lobe* __restrict__ lobes, const float* __restrict__ wi,
+                                 const float* __restrict__ u, uint64_t n, float* wo, float* weight, float* pdf,
+                                 uint8_t* flags) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const kz_lobe l = lobes[i];
+    LobeSample s = lobe_sample(l, ld3(wi + 3 * i), u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+    wo[3 * i] = s.wo.x;
+    wo[3 * i + 1] = s.wo.y;
+    wo[3 * i + 2] = s.wo.z;
+    weight[3 * i] = s.weight.x;
+    weight[3 * i + 1] = s.weight.y;
+    weight[3 * i + 2] = s.weight.z;
+    pdf[i] = s.pdf;
+    flags[i] = (uint8_t)((s.valid ? 1 : 0) | (s.delta ? 2 : 0));
+}
+
+// ------------------------------------------------------------------ wavefront stages
+__global__ void k_generate_camera(DevCamera cam, PathParams pp, PathSoA dst, uint32_t dst_offset,
+                                  uint64_t first_path, uint32_t n_new) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_new) return;
+    const uint64_t pid = first_path + j;
+    const uint64_t pix = pid / pp.spp;
+    const uint32_t px = (uint32_t)(pix % cam.W), py = (uint32_t)(pix / cam.W);
+    Pcg rng;
+    rng.seed(pp.seed, pid);
+    const float jx = rng.nextf(), jy = rng.nextf();
+    // Camera::generate_ray (src/core/camera.cpp:5-37): horizontal fov,
+    // row 0 at the top unless flipped.
+    const float sx = ((float)px + jx) / (float)cam.W;
+    const float sy = ((float)py + jy) / (float)cam.H;
+    const float nx = 2.0f * sx - 1.0f;
+    const float ny = cam.flip * ((1.0f - 2.0f * sy) / cam.aspect);
+    const float cx = nx * cam.tan_half;
+    const float cy = ny * cam.tan_half;
+    const f3 d = normalize(ld3(cam.x) * cx + ld3(cam.y) * cy + ld3(cam.z) * (-1.0f));
+    const uint32_t k = dst_offset + j;
+    dst.o4[k] = make_float4(cam.eye[0], cam.eye[1], cam.eye[2], 0.f);
+    dst.d4[k] = make_float4(d.x, d.y, d.z, __uint_as_float(kSpecularFlag));
+    dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
+    dst.rng[k] = rng.state;
+}
+
+__global__ void k_generate_rays(const kz_ray* __restrict__ rays, PathParams pp, PathSoA dst, uint32_t dst_offset,
+                                uint64_t first_path, uint32_t n_new) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_new) return;
+    const uint64_t pid = first_path + j;
+    Pcg rng;
+    rng.seed(pp.seed, pid);
+    const kz_ray r = rays[pid];
+    const uint32_t k = dst_offset + j;
+    dst.o4[k] = make_float4(r.ox, r.oy, r.oz, 0.f);
+    dst.d4[k] = make_float4(r.dx, r.dy, r.dz, __uint_as_float(kSpecularFlag));
+    dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
+    dst.rng[k] = rng.state;
+}
+
+// Sums two per-thread counters over the warp; one 64-bit atomic each.
+__device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long long* dst) {
+    unsigned long long x = a, y = b;
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, o);
+        y += __shfl_down_sync(0xffffffffu, y, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(dst, x);
+        atomicAdd(dst + 1, y);
+    }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint32_t n, DevCounters* ctr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t dn = 0, dt = 0;
+    if (i < n) {
+        const float4 o = p.o4[i], d = p.d4[i];
+        TRay r = make_tray(xyz(o), xyz(d), kRayEps);
+        HitRec h;
+        if (!trace_closest<kCount>(s, r, __int_as_float(0x7f800000), h, dn, dt)) {
+            set_status(&ctr->status, KZ_ERR_STACK);
+            h.rec = -1;
+        }
+        p.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec));
+    }
+    if (kCount) warp_count(dn, dt, &ctr->fetch[0]);
+}
+
+__device__ __forceinline__ void film_add(float* film, double* film64, uint32_t idx, f3 c) {
+    atomicAdd(film + 3 * (size_t)idx, c.x);
+    atomicAdd(film + 3 * (size_t)idx + 1, c.y);
+    atomicAdd(film + 3 * (size_t)idx + 2, c.z);
+    if (film64) {
+        atomicAdd(film64 + 3 * (size_t)idx, (double)c.x);
+        atomicAdd(film64 + 3 * (size_t)idx + 1, (double)c.y);
+        atomicAdd(film64 + 3 * (size_t)idx + 2, (double)c.z);
+    }
+}
+
+// DiscrectPDF::sample (src/base/dpdf.h:31-36): lower_bound over cdf[0..n].
+__device__ __forceinline__ uint32_t cdf_sample(const float* cdf, uint32_t n, float u) {
+    uint32_t lo = 0, cnt = n + 1;
+    while (cnt > 0) {
+        uint32_t step = cnt / 2, it = lo + step;
+        if (__ldg(cdf + it) < u) {
+            lo = it + 1;
+            cnt -= step + 1;
+        } else {
+            cnt = step;
+        }
+    }
+    int idx = (int)lo - 1;
+    if (idx < 0) idx = 0;
+    return min((uint32_t)idx, n - 1);
+}
+
+// One shaded vertex per thread. Estimator corrections relative to the
+// reference loop (each one keeps the estimator unbiased):
+//  * NEE uses f*|cos| once (the reference multiplies Diffuse's f*cos by cos
+//    again, integrator.cpp:475-480) and divides by the light pick pdf inside
+//    the MIS weight as well as outside;
+//  * BSDF sampling divides by the direction pdf (integrator.cpp:503-505
+//    multiplies by f only) and picks the lobe by its selection probability;
+//  * emission hits weigh against the light pdf of the sampled direction
+//    (integrator.cpp:452-462 reuses the previous light sample's pdf);
+//  * max_depth counts shaded vertices (the reference steps depth twice per
+//    loop, integrator.cpp:420,555).
+__global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
+                                               ShadowSoA sq, DevCounters* ctr, float* film, double* film64) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool cont = false, shadow = false;
+    float4 o_next, d_next, b_next, s_o, s_d, s_c;
+    unsigned long long rng_next = 0;
+    if (i < n_in) {
+        const float4 hit = in.hit[i];
+        const int rec = __float_as_int(hit.w);
+        if (rec >= 0) {
+            const float4 o4 = in.o4[i], d4 = in.d4[i], b4 = in.b4[i];
+            const uint32_t pid = __float_as_uint(b4.w);
+            const uint32_t film_idx = pid / pp.spp;
+            const uint32_t flags = __float_as_uint(d4.w);
+            const uint32_t depth = flags & 0xffu;
+            const bool prev_spec = (flags & kSpecularFlag) != 0;
+            const float prev_pdf = o4.w;
+            Pcg rng;
+            rng.state = in.rng[i];
+            rng.inc = ((uint64_t)pid << 1u) | 1u;
+            float u[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
+
+            const float4* tp = s.tris + (size_t)rec * 3;
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            const uint32_t geom = __float_as_uint(tb.w);
+            const kz_material& mat = s.materials[__float_as_uint(tc.w)];
+            const f3 v0 = xyz(ta), v1 = xyz(tb), v2 = xyz(tc);
+            const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
+            const f3 d = xyz(d4);
+            const f3 P = xyz(o4) + d * hit.x;
+            const Frame fr(Ng);
+            const f3 wi = -fr.to_local(d);
+            f3 beta = xyz(b4);
+            f3 Lsum = mk(0.f, 0.f, 0.f);
+            const uint32_t nl = s.n_lights;
+
+            // 1. emission (front face only: single_emissive_surface)
+            const f3 Le = ld3(mat.Le);
+            if (!is_zero(Le) && dot(d, Ng) < 0.f) {
+                float w = 1.f;
+                if (!prev_spec) {
+                    const int li = __ldg(s.geom_light + geom);
+                    if (li >= 0) {
+                        const float cos_l = -dot(d, Ng);
+                        const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
+                        w = power_heuristic(prev_pdf, lpdf);
+                    }
+                }
+                Lsum = Lsum + hmul(beta, Le) * w;
+            }
+
+            // lobe selection probabilities (CompositeClosure::compute_pdfs)
+            const uint32_t nlobes = min(mat.n_lobes, (uint32_t)KZ_MAX_LOBES);
+            float lp[KZ_MAX_LOBES];
+            const float winv = 1.f / (beta.x + beta.y + beta.z);
+            float wsum = 0.f;
+            bool any_smooth = false;
+            for (uint32_t k = 0; k < nlobes; ++k) {
+                const kz_lobe& lb = mat.lobes[k];
+                lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
+                wsum += lp[k];
+                any_smooth |= !lobe_is_delta(lb.closure_id);
+            }
+            if (wsum > 0.f)
+                for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
+
+            // 2. next-event estimation
+            if (nl > 0 && any_smooth && wsum > 0.f) {
+                const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
+                const DevLight lt = s.lights[li];
+                const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
+                const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
+                const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
+                const float su0 = sqrtf(u[2]);
+                const float bu0 = 1.f - su0;
+                const float bv0 = u[3] * su0;
+                const f3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+                const f3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+                const f3 lv = p - P;
+                const float dist2 = dot(lv, lv);
+                const float dist = sqrtf(dist2);
+                const f3 ldir = mk(lv.x / dist, lv.y / dist, lv.z / dist);
+                const float cos_l = -dot(ldir, nlgt);
+                if (cos_l > 0.f) {
+                    const float pdf_solid = dist2 / (cos_l * lt.area);
+                    const float lpdf = pdf_solid * (1.0f / (float)nl);
+                    const f3 wo = fr.to_local(ldir);
+                    f3 f = mk(0.f, 0.f, 0.f);
+                    float bpdf = 0.f;
+                    for (uint32_t k = 0; k < nlobes; ++k) {
+                        const kz_lobe& lb = mat.lobes[k];
+                        if (lobe_is_delta(lb.closure_id)) continue;
+                        const LobeEval e = lobe_eval(lb, wi, wo);
+                        f = f + hmul(ld3(lb.weight), e.f);
+                        bpdf += lp[k] * e.pdf;
+                    }
+                    if (!is_zero(f)) {
+                        const float w = power_heuristic(lpdf, bpdf);
+                        const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
+                        shadow = true;
+                        s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
+                        s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
+                        s_c = make_float4(c.x, c.y, c.z, 0.f);
+                    }
+                }
+            }
+
+            bool alive = depth + 1 < pp.max_depth;
+            // 3. Russian roulette (integrator.cpp:491-498)
+            if (alive && depth >= pp.rr_min) {
+                const float prob = fminf(max_comp(beta) * 0.9025f, 0.99f);
+                if (prob < u[4]) alive = false;
+                else beta = beta * (1.f / prob);
+            }
+            // 4. BSDF sample (one-sample mixture over the non-delta lobes)
+            if (alive && wsum > 0.f) {
+                uint32_t sel = nlobes - 1;
+                float acc = 0.f;
+                for (uint32_t k = 0; k < nlobes; ++k) {
+                    acc += lp[k];
+                    if (u[5] < acc) {
+                        sel = k;
+                        break;
+                    }
+                }
+                while (sel > 0 && lp[sel] == 0.f) --sel;
+                const kz_lobe& ls = mat.lobes[sel];
+                const LobeSample smp = lobe_sample(ls, wi, u[6], u[7], u[8]);
+                alive = smp.valid;
+                f3 weight = mk(0.f, 0.f, 0.f);
+                float pdf_dir = 0.f;
+                if (alive) {
+                    if (smp.delta) {
+                        weight = hmul(ld3(ls.weight), smp.weight) * (1.f / lp[sel]);
+                    } else {
+                        f3 f = mk(0.f, 0.f, 0.f);
+                        float pdf = 0.f;
+                        for (uint32_t k = 0; k < nlobes; ++k) {
+                            const kz_lobe& lb = mat.lobes[k];
+                            if (lobe_is_delta(lb.closure_id)) continue;
+                            const LobeEval e = lobe_eval(lb, wi, smp.wo);
+                            f = f + hmul(ld3(lb.weight), e.f);
+                            pdf += lp[k] * e.pdf;
+                        }
+                        alive = pdf > 0.f;
+                        if (alive) weight = f * (1.f / pdf);
+                        pdf_dir = pdf;
+                    }
+                }
+                if (alive) {
+                    beta = hmul(beta, weight);
+                    alive = !is_zero(beta);
+                }
+                if (alive) {
+                    const f3 dn = normalize(fr.to_world(smp.wo));
+                    cont = true;
+                    o_next = make_float4(P.x, P.y, P.z, pdf_dir);
+                    d_next = make_float4(dn.x, dn.y, dn.z,
+                                         __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u)));
+                    b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
+                    rng_next = rng.state;
+                }
+            }
+            if (!is_zero(Lsum)) film_add(film, film64, film_idx, Lsum);
+        }
+    }
+    const uint32_t slot = warp_append(cont, &ctr->n_next);
+    if (cont) {
+        out.o4[slot] = o_next;
+        out.d4[slot] = d_next;
+        out.b4[slot] = b_next;
+        out.rng[slot] = rng_next;
+    }
+    const uint32_t sslot = warp_append(shadow, &ctr->n_shadow);
+    if (shadow) {
+        sq.o4[sslot] = s_o;
+        sq.d4[sslot] = s_d;
+        sq.c4[sslot] = s_c;
+    }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, DevCounters* ctr, float* film,
+                                                      double* film64) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t dn = 0, dt = 0;
+    if (i < ctr->n_shadow) {
+        const float4 o = sq.o4[i], d = sq.d4[i];
+        TRay r = make_tray(xyz(o), xyz(d), kRayEps);
+        bool overflow;
+        const bool occluded = trace_any<kCount>(s, r, o.w, overflow, dn, dt);
+        if (overflow) set_status(&ctr->status, KZ_ERR_STACK);
+        if (!occluded && !overflow) {
+            const float4 c = sq.c4[i];
+            film_add(film, film64, __float_as_uint(d.w), xyz(c));
+        }
+    }
+    if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
+}
+
+__global__ void k_scale(float* film, double* film64, uint64_t n, float sf, double sd) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (film) film[i] *= sf;
+    if (film64) film64[i] *= sd;
+}
+
+inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits, uint32_t* status,
+                              cudaStream_t st) {
+    if (!n) return;
+    k_intersect_closest<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, hits, status);
+}
+void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ, uint32_t* status,
+                          cudaStream_t st) {
+    if (!n) return;
+    k_intersect_any<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, occ, status);
+}
+void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n, unsigned long long* counters,
+                            uint32_t* status, cudaStream_t st) {
+    if (!n) return;
+    k_intersect_stats<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, counters, status);
+}
+void launch_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n, int convention,
+                         float* f, float* pdf, cudaStream_t st) {
+    if (!n) return;
+    k_closure_eval<<<grid_for(n, 128), 128, 0, st>>>(lobes, wi, wo, n, convention, f, pdf);
+}
+void launch_closure_sample(const kz_lobe* lobes, const float* wi, const float* u, uint64_t n, float* wo,
+                           float* weight, float* pdf, uint8_t* flags, cudaStream_t st) {
+    if (!n) return;
+    k_closure_sample<<<grid_for(n, 128), 128, 0, st>>>(lobes, wi, u, n, wo, weight, pdf, flags);
+}
+void launch_generate_camera(const DevCamera& cam, const PathParams& pp, PathSoA dst, uint32_t dst_offset,
+                            uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st) {
+    if (!n_new) return;
+    k_generate_camera<<<grid_for(n_new, block), block, 0, st>>>(cam, pp, dst, dst_offset, first_path, n_new);
+}
+void launch_generate_rays(const kz_ray* rays, const PathParams& pp, PathSoA dst, uint32_t dst_offset,
+                          uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st) {
+    if (!n_new) return;
+    k_generate_rays<<<grid_for(n_new, block), block, 0, st>>>(rays, pp, dst, dst_offset, first_path, n_new);
+}
+void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* ctr, bool count, uint32_t block,
+                        cudaStream_t st) {
+    if (!n) return;
+    if (count) k_trace_paths<true><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr);
+    else k_trace_paths<false><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr);
+}
+void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
+                  DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
+    if (!n_in) return;
+    k_shade<<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64);
+}
+void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count, float* film,
+                         double* film64, uint32_t block, cudaStream_t st) {
+    if (!n_max) return;
+    if (count) k_trace_shadow<true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64);
+    else k_trace_shadow<false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64);
+}
+void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
+    if (!n) return;
+    k_scale<<<grid_for(n, 256), 256, 0, st>>>(film, film64, n, sf, sd);
+}
+
+}  // namespace kz

@@ -1,0 +1,1386 @@
+// kz_oracle.cpp — CPU restatement of the kazen_proto rendering hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This library is the parity checker for the CUDA
+// path in kazen_proto_gb300/ and the timed CPU baseline of bench.py. Nothing
+// in the product links, loads or calls it.
+//
+// Parity status: the reference (kazen_proto) cannot be compiled here — its
+// hot path depends on Embree 4, OSL, boost and pcg32, none of which are
+// present — so this restatement is pinned against the reference's own
+// known-answer tests (microfacet white-furnace integrals,
+// tests/render_tests/microfacet_tests.cpp:8-21; the Embree single-triangle
+// hit, tests/libusage_tests/embree_tests.cpp:19-76) and against analytic
+// identities in tests/. Formula-level parity with the reference binary is
+// otherwise unpinned.
+//
+// Written independently of the product's device code: its own BVH (object
+// median split), its own traversal, its own closure code. Compile with
+// -ffp-contract=off so FP32 expressions round exactly as written.
+//
+// Reference files restated (paths within kazen_proto):
+//   ray epsilon ............ src/core/ray.h:10-45, src/base/basic_types.h:9
+//   shading frame .......... src/base/utils.h:83-210
+//   closures ............... src/shading/bsdfs.cpp:27-41, 254-298, 359-554, 688-730
+//   glass helpers .......... src/shading/bsdfs.h:541-599
+//   microfacet ............. src/shading/microfacet.h:60-291
+//   fresnel ................ src/shading/fresnel.h:12-187, src/base/utils.h:153-177
+//   mixture ................ src/shading/bsdf.h:132-196, src/shading/bsdf.cpp:17-74
+//   lights ................. src/core/light.cpp:46-86, src/core/shape.cpp:591-613,
+//                            src/base/dpdf.h:8-58, src/core/integrator.cpp:25-34
+//   path loop .............. src/core/integrator.cpp:362-561
+//   camera ................. src/core/camera.h:50-96, src/core/camera.cpp:5-37
+//   furnace tests .......... src/shading/white_furnace.h:12-38, white_furnace.cpp:3-36
+// Ray/triangle: the watertight test of Woop, Benthin & Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013, double-sided, closest hit in
+// (tmin, tmax], equal t resolved to the smaller triangle index.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "../include/kazen_gb300.h"
+
+namespace {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.318309886183790671538f;
+constexpr float kRayEps = 1e-4f;  // epsilon<float>, src/base/basic_types.h:9
+
+struct V3 {
+    float x, y, z;
+    V3() : x(0), y(0), z(0) {}
+    V3(float a, float b, float c) : x(a), y(b), z(c) {}
+    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
+inline V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline V3 mul(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 normalize(V3 a) {
+    float l = std::sqrt(dot(a, a));
+    return {a.x / l, a.y / l, a.z / l};
+}
+inline float sq(float a) { return a * a; }
+inline bool is_zero(V3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
+inline float max_comp(V3 a) { return std::max(a.x, std::max(a.y, a.z)); }
+
+// ---------------------------------------------------------------- PCG32
+// PCG-XSH-RR 64/32 (O'Neill 2014), seeded like pcg32_srandom(initstate, initseq).
+struct Pcg32 {
+    uint64_t state, inc;
+    void seed(uint64_t initstate, uint64_t initseq) {
+        state = 0u;
+        inc = (initseq << 1u) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+    }
+    // pcg32::nextFloat (Jakob's pcg32.h, used by Sampler, src/core/sampler.cpp:22-27):
+    // 23 random mantissa bits in [1, 2), minus 1.
+    float nextf() {
+        uint32_t u = (next() >> 9) | 0x3f800000u;
+        float f;
+        std::memcpy(&f, &u, 4);
+        return f - 1.0f;
+    }
+};
+
+// ---------------------------------------------------------------- triangle test
+struct RayPre {
+    V3 o, d;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+inline RayPre ray_pre(V3 o, V3 d) {
+    RayPre r;
+    r.o = o;
+    r.d = d;
+    float ad[3] = {std::fabs(d.x), std::fabs(d.y), std::fabs(d.z)};
+    int kz = 0;
+    if (ad[1] > ad[kz]) kz = 1;
+    if (ad[2] > ad[kz]) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (d[kz] < 0.f) std::swap(kx, ky);
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = d[kx] / d[kz];
+    r.Sy = d[ky] / d[kz];
+    r.Sz = 1.0f / d[kz];
+    return r;
+}
+
+// Returns true with (t, u, v) when the triangle is hit at t in (tmin, +inf).
+inline bool tri_hit(const RayPre& r, V3 v0, V3 v1, V3 v2, float& t, float& bu, float& bv) {
+    const V3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+    const float Ax = A[r.kx] - r.Sx * A[r.kz];
+    const float Ay = A[r.ky] - r.Sy * A[r.kz];
+    const float Bx = B[r.kx] - r.Sx * B[r.kz];
+    const float By = B[r.ky] - r.Sy * B[r.kz];
+    const float Cx = C[r.kx] - r.Sx * C[r.kz];
+    const float Cy = C[r.ky] - r.Sy * C[r.kz];
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    const float det = U + V + W;
+    if (det == 0.f) return false;
+    const float Az = r.Sz * A[r.kz];
+    const float Bz = r.Sz * B[r.kz];
+    const float Cz = r.Sz * C[r.kz];
+    const float T = U * Az + V * Bz + W * Cz;
+    t = T / det;
+    bu = V / det;
+    bv = W / det;
+    return true;
+}
+
+// ---------------------------------------------------------------- oracle BVH
+// Binary BVH: binned SAH (16 bins on the largest centroid axis), leaves of at
+// most 4 triangles, object median when the bins cannot separate; traversal
+// visits the nearer child first and skips stacked nodes whose entry distance
+// is beyond the current closest hit. Written independently of the product's
+// builder and traversal.
+struct OBox {
+    float lo[3], hi[3];
+};
+struct ONode {
+    OBox box;
+    int32_t left, right;     // children (internal) or -1
+    uint32_t first, count;   // leaf triangle range in `order`
+};
+
+struct OBvh {
+    std::vector<float> verts;  // ntris * 9, world space
+    uint32_t ntris = 0;
+    std::vector<ONode> nodes;
+    std::vector<uint32_t> order;
+
+    V3 v(uint32_t tri, int k) const {
+        const float* p = &verts[(size_t)tri * 9 + k * 3];
+        return {p[0], p[1], p[2]};
+    }
+
+    static float half_area(const OBox& b) {
+        if (b.lo[0] > b.hi[0]) return 0.f;
+        float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    }
+    static OBox empty_box() {
+        OBox b;
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = std::numeric_limits<float>::infinity();
+            b.hi[a] = -std::numeric_limits<float>::infinity();
+        }
+        return b;
+    }
+    static void grow(OBox& b, const OBox& c) {
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = std::min(b.lo[a], c.lo[a]);
+            b.hi[a] = std::max(b.hi[a], c.hi[a]);
+        }
+    }
+
+    void build() {
+        order.resize(ntris);
+        for (uint32_t i = 0; i < ntris; ++i) order[i] = i;
+        std::vector<float> cen((size_t)ntris * 3);
+        std::vector<OBox> tb(ntris);
+        for (uint32_t i = 0; i < ntris; ++i) {
+            OBox b = empty_box();
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::min(b.lo[a], v(i, k)[a]);
+                    b.hi[a] = std::max(b.hi[a], v(i, k)[a]);
+                }
+            tb[i] = b;
+            for (int a = 0; a < 3; ++a) cen[(size_t)i * 3 + a] = (v(i, 0)[a] + v(i, 1)[a] + v(i, 2)[a]) * (1.0f / 3.0f);
+        }
+        nodes.clear();
+        nodes.reserve(ntris ? ntris : 1);
+        struct Task { uint32_t node, first, count; };
+        std::vector<Task> stack;
+        nodes.push_back(ONode{});
+        stack.push_back({0, 0, ntris});
+        constexpr int kB = 16;
+        while (!stack.empty()) {
+            Task tk = stack.back();
+            stack.pop_back();
+            OBox b = empty_box(), cb = empty_box();
+            for (uint32_t i = tk.first; i < tk.first + tk.count; ++i) {
+                uint32_t tri = order[i];
+                grow(b, tb[tri]);
+                for (int a = 0; a < 3; ++a) {
+                    float c = cen[(size_t)tri * 3 + a];
+                    cb.lo[a] = std::min(cb.lo[a], c);
+                    cb.hi[a] = std::max(cb.hi[a], c);
+                }
+            }
+            nodes[tk.node].box = b;
+            if (tk.count <= 4) {
+                nodes[tk.node].left = nodes[tk.node].right = -1;
+                nodes[tk.node].first = tk.first;
+                nodes[tk.node].count = tk.count;
+                continue;
+            }
+            int axis = 0;
+            for (int a = 1; a < 3; ++a)
+                if (cb.hi[a] - cb.lo[a] > cb.hi[axis] - cb.lo[axis]) axis = a;
+            const float ext = cb.hi[axis] - cb.lo[axis];
+            uint32_t mid = tk.first + tk.count / 2;
+            bool done = false;
+            if (ext > 0.f) {
+                OBox bins[kB];
+                uint32_t cnt[kB] = {0};
+                for (int k = 0; k < kB; ++k) bins[k] = empty_box();
+                const float sc = (float)kB / ext;
+                auto bin_of = [&](uint32_t tri) {
+                    int k = (int)((cen[(size_t)tri * 3 + axis] - cb.lo[axis]) * sc);
+                    return std::min(std::max(k, 0), kB - 1);
+                };
+                for (uint32_t i = tk.first; i < tk.first + tk.count; ++i) {
+                    int k = bin_of(order[i]);
+                    cnt[k]++;
+                    grow(bins[k], tb[order[i]]);
+                }
+                float best = std::numeric_limits<float>::infinity();
+                int best_k = -1;
+                for (int k = 0; k < kB - 1; ++k) {
+                    OBox l = empty_box(), r = empty_box();
+                    uint32_t nl = 0, nr = 0;
+                    for (int j = 0; j <= k; ++j) { grow(l, bins[j]); nl += cnt[j]; }
+                    for (int j = k + 1; j < kB; ++j) { grow(r, bins[j]); nr += cnt[j]; }
+                    if (!nl || !nr) continue;
+                    float c = half_area(l) * nl + half_area(r) * nr;
+                    if (c < best) { best = c; best_k = k; }
+                }
+                if (best_k >= 0) {
+                    auto it = std::partition(order.begin() + tk.first, order.begin() + tk.first + tk.count,
+                                             [&](uint32_t t) { return bin_of(t) <= best_k; });
+                    mid = (uint32_t)(it - order.begin());
+                    done = mid > tk.first && mid < tk.first + tk.count;
+                }
+            }
+            if (!done) {
+                mid = tk.first + tk.count / 2;
+                std::nth_element(order.begin() + tk.first, order.begin() + mid,
+                                 order.begin() + tk.first + tk.count, [&](uint32_t p, uint32_t q) {
+                                     float cp = cen[(size_t)p * 3 + axis], cq = cen[(size_t)q * 3 + axis];
+                                     return cp < cq || (cp == cq && p < q);
+                                 });
+            }
+            int32_t l = (int32_t)nodes.size();
+            nodes.push_back(ONode{});
+            int32_t r = (int32_t)nodes.size();
+            nodes.push_back(ONode{});
+            nodes[tk.node].left = l;
+            nodes[tk.node].right = r;
+            nodes[tk.node].first = nodes[tk.node].count = 0;
+            stack.push_back({(uint32_t)l, tk.first, mid - tk.first});
+            stack.push_back({(uint32_t)r, mid, tk.first + tk.count - mid});
+        }
+    }
+
+    // Conservative slab test: box distances are widened by a relative margin
+    // far larger than their rounding error, so a box that holds a triangle hit
+    // at t <= tbest is never culled.
+    static bool box_hit(const OBox& b, const V3& o, const V3& inv, float tmin, float tbest, float& tnear) {
+        float t0 = -std::numeric_limits<float>::infinity(), t1 = std::numeric_limits<float>::infinity();
+        for (int a = 0; a < 3; ++a) {
+            float ta = (b.lo[a] - o[a]) * inv[a];
+            float tb = (b.hi[a] - o[a]) * inv[a];
+            if (ta > tb) std::swap(ta, tb);
+            t0 = std::max(t0, ta);
+            t1 = std::min(t1, tb);
+        }
+        t0 = t0 > 0.f ? t0 * (1.0f - 1e-4f) : t0 * (1.0f + 1e-4f);
+        t1 = t1 > 0.f ? t1 * (1.0f + 1e-4f) : t1 * (1.0f - 1e-4f);
+        tnear = std::max(t0, tmin);
+        return tnear <= std::min(t1, tbest);
+    }
+
+    static V3 inv_dir(V3 d) {
+        auto f = [](float c) {
+            if (std::fabs(c) < 1e-30f) c = std::copysign(1e-30f, c);
+            return 1.0f / c;
+        };
+        return {f(d.x), f(d.y), f(d.z)};
+    }
+
+    // Closest hit in (tmin, tmax]; ties in t go to the smaller triangle index.
+    bool closest(V3 o, V3 d, float tmin, float tmax, float& t_out, uint32_t& prim, float& u_out, float& v_out) const {
+        prim = KZ_INVALID_ID;
+        t_out = tmax;
+        if (ntris == 0) return false;
+        RayPre rp = ray_pre(o, d);
+        V3 inv = inv_dir(d);
+        uint32_t stack[128];
+        float stack_t[128];
+        int sp = 0;
+        float tn;
+        if (!box_hit(nodes[0].box, o, inv, tmin, t_out, tn)) return false;
+        stack[sp] = 0;
+        stack_t[sp++] = tn;
+        while (sp) {
+            --sp;
+            if (stack_t[sp] > t_out) continue;
+            const ONode& nd = nodes[stack[sp]];
+            if (nd.left < 0) {
+                for (uint32_t i = nd.first; i < nd.first + nd.count; ++i) {
+                    uint32_t tri = order[i];
+                    float t, bu, bv;
+                    if (!tri_hit(rp, v(tri, 0), v(tri, 1), v(tri, 2), t, bu, bv)) continue;
+                    if (!(t > tmin) || !(t <= tmax)) continue;
+                    if (t < t_out || (t == t_out && tri < prim)) {
+                        t_out = t; prim = tri; u_out = bu; v_out = bv;
+                    }
+                }
+                continue;
+            }
+            float tl, tr;
+            bool hl = box_hit(nodes[nd.left].box, o, inv, tmin, t_out, tl);
+            bool hr = box_hit(nodes[nd.right].box, o, inv, tmin, t_out, tr);
+            if (hl && hr) {
+                if (tl <= tr) {
+                    stack[sp] = nd.right; stack_t[sp++] = tr;
+                    stack[sp] = nd.left; stack_t[sp++] = tl;
+                } else {
+                    stack[sp] = nd.left; stack_t[sp++] = tl;
+                    stack[sp] = nd.right; stack_t[sp++] = tr;
+                }
+            } else if (hl) {
+                stack[sp] = nd.left; stack_t[sp++] = tl;
+            } else if (hr) {
+                stack[sp] = nd.right; stack_t[sp++] = tr;
+            }
+        }
+        return prim != KZ_INVALID_ID;
+    }
+
+    bool any(V3 o, V3 d, float tmin, float tmax) const {
+        if (ntris == 0) return false;
+        RayPre rp = ray_pre(o, d);
+        V3 inv = inv_dir(d);
+        uint32_t stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp) {
+            const ONode& nd = nodes[stack[--sp]];
+            float tn;
+            if (!box_hit(nd.box, o, inv, tmin, tmax, tn)) continue;
+            if (nd.left < 0) {
+                for (uint32_t i = nd.first; i < nd.first + nd.count; ++i) {
+                    uint32_t tri = order[i];
+                    float t, bu, bv;
+                    if (!tri_hit(rp, v(tri, 0), v(tri, 1), v(tri, 2), t, bu, bv)) continue;
+                    if (t > tmin && t <= tmax) return true;
+                }
+            } else {
+                stack[sp++] = (uint32_t)nd.right;
+                stack[sp++] = (uint32_t)nd.left;
+            }
+        }
+        return false;
+    }
+};
+
+template <typename F>
+void parallel_for(uint64_t n, int nthreads, F&& fn) {
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (n < 2 || nthreads == 1) {
+        for (uint64_t i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<uint64_t> next{0};
+    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(256, n / (8 * (uint64_t)nthreads)));
+    std::vector<std::thread> th;
+    for (int k = 0; k < nthreads; ++k)
+        th.emplace_back([&]() {
+            for (;;) {
+                uint64_t b = next.fetch_add(chunk);
+                if (b >= n) break;
+                uint64_t e = std::min(n, b + chunk);
+                for (uint64_t i = b; i < e; ++i) fn(i);
+            }
+        });
+    for (auto& t : th) t.join();
+}
+
+// ---------------------------------------------------------------- shading frame
+// Frame(n): src/base/utils.h:191-201 (normal -> y, tangent t, s = cross(t, n)).
+struct Frame {
+    V3 s, t, n;
+    explicit Frame(V3 nn) : n(nn) {
+        if (std::fabs(n.x) > std::fabs(n.y)) {
+            float inv_len = 1.f / std::sqrt(n.x * n.x + n.z * n.z);
+            t = V3(n.z * inv_len, 0.f, -n.x * inv_len);
+        } else {
+            float inv_len = 1.f / std::sqrt(n.y * n.y + n.z * n.z);
+            t = V3(0.f, n.z * inv_len, -n.y * inv_len);
+        }
+        s = cross(t, n);
+    }
+    V3 to_local(V3 v) const { return V3(dot(v, s), dot(v, n), dot(v, t)); }
+    V3 to_world(V3 v) const { return s * v.x + n * v.y + t * v.z; }
+};
+
+// ---------------------------------------------------------------- fresnel
+// fresnel(cos, ext, int): src/base/utils.h:153-177
+float fresnel_utils(float cos_theta_i, float ext_ior, float int_ior) {
+    float etai = ext_ior, etat = int_ior;
+    if (ext_ior == int_ior) return 0.f;
+    if (cos_theta_i < 0.f) {
+        std::swap(etai, etat);
+        cos_theta_i = -cos_theta_i;
+    }
+    float eta = etai / etat;
+    float sin_theta_t2 = (float)(eta * eta * (1. - cos_theta_i * cos_theta_i));
+    if (sin_theta_t2 > 1.f) return 1.f;
+    float cos_theta_t = std::sqrt(1.f - sin_theta_t2);
+    float Rs = (etai * cos_theta_i - etat * cos_theta_t) / (etai * cos_theta_i + etat * cos_theta_t);
+    float Rp = (etat * cos_theta_i - etai * cos_theta_t) / (etat * cos_theta_i + etai * cos_theta_t);
+    return (Rs * Rs + Rp * Rp) / 2.f;
+}
+
+// fresnel_refl_dielectric(eta, cos_i, cos_t) / (eta, cos_i): src/shading/fresnel.h:75-131
+float fr_p(float eta, float ci, float ct) {
+    float fac = eta * ct;
+    float r = (ci - fac) / (ci + fac);
+    return r * r;
+}
+float fr_s(float eta, float ci, float ct) {
+    float fac = eta * ci;
+    float r = (ct - fac) / (ct + fac);
+    return r * r;
+}
+float fresnel_refl3(float eta, float ci, float ct) {
+    if (ci == 0.f && ct == 0.f) return 0.f;
+    return 0.5f * (fr_p(eta, ci, ct) + fr_s(eta, ci, ct));
+}
+float fresnel_refl(float eta, float ci) {
+    const float sin_i2 = 1.f - sq(ci);
+    const float sin_t2 = sin_i2 * sq(eta);
+    const float cos_t2 = 1.f - sin_t2;
+    if (cos_t2 < 0.f) return 1.f;
+    return fresnel_refl3(eta, ci, std::sqrt(cos_t2));
+}
+// fresnel_schlick(eta, cos): fresnel.h:180-183 (computed in double like the reference)
+float fresnel_schlick_eta(float eta, float c) {
+    double F0 = ((1. - eta) / (1. + eta)) * ((1. - eta) / (1. + eta));
+    return (float)(F0 + (1. - F0) * std::pow(1. - c, 5.));
+}
+// schlick_weight / fresnel_schlick(RGB F0, cos): fresnel.h:176-187
+float schlick_weight(float c) {
+    double x = std::min(std::max(1. - (double)c, 0.), 1.);
+    return (float)std::pow(x, 5.);
+}
+
+// ---------------------------------------------------------------- microfacet
+// src/shading/microfacet.h:60-291
+enum Dist { GGX = 0, BECKMANN = 1 };
+
+float stretched_roughness(V3 m, float sin_v, float ax, float ay) {
+    if (ax == ay) return 1.f / sq(ax);
+    const float c = sq(m.x / (sin_v * ax));
+    const float s = sq(m.z / (sin_v * ay));
+    return c + s;
+}
+float projected_roughness(V3 m, float sin_v, float ax, float ay) {
+    if (ax == ay || sin_v == 0.f) return ax;
+    const float c = sq((m.x * ax) / sin_v);
+    const float s = sq((m.z * ay) / sin_v);
+    return std::sqrt(c + s);
+}
+float dist_D(int dist, float tan2m_a) {
+    if (dist == GGX) {
+        float tmp = 1 + tan2m_a;
+        return 1.f / (kPi * tmp * tmp);
+    }
+    return kInvPi * std::exp(-tan2m_a);
+}
+float dist_lambda(int dist, float a_rcp) {
+    if (dist == GGX) {
+        const float a2_rcp = sq(a_rcp);
+        return (-1.f + std::sqrt(1.f + a2_rcp)) * 0.5f;
+    }
+    const float a = 1.f / a_rcp;
+    if (a < 1.6f) {
+        const float a2 = sq(a);
+        return (1.f - 1.259f * a + 0.396f * a2) / (3.535f * a + 2.181f * a2);
+    }
+    return 0.f;
+}
+
+struct Mdf {
+    int dist;
+    V3 wi;
+    float ax, ay;
+    float lambda(V3 m) const {
+        float c = m.y;
+        if (c == 0.f) return 0.f;
+        const float s = std::sqrt(std::max(0.f, 1.f - sq(c)));
+        if (s == 0.f) return 0.f;
+        const float alpha = projected_roughness(m, s, ax, ay);
+        const float tan_v = std::fabs(s / c);
+        return dist_lambda(dist, alpha * tan_v);
+    }
+    float G(V3 wo) const { return 1.f / (lambda(wi) + lambda(wo) + 1.f); }
+    float G1(V3 w) const { return 1.f / (lambda(w) + 1.f); }
+    float D(V3 m) const {
+        const float c = m.y;
+        if (c == 0.f) return dist == BECKMANN ? 0.f : sq(ax) * kInvPi;
+        const float c2 = sq(c);
+        const float s = std::sqrt(std::max(0.f, 1.f - c2));
+        const float c4 = sq(c2);
+        const float tan2 = (1.f - c2) / c2;
+        const float A = stretched_roughness(m, s, ax, ay);
+        return dist_D(dist, tan2 * A) / (c4 * ax * ay);
+    }
+    // VNDF pdf of m (no Jacobian), microfacet.h:227-241
+    float pdf(V3 m) const {
+        const float c = wi.y;
+        if (c == 0.f) return 0.f;
+        return G1(wi) * std::fabs(dot(wi, m)) * D(m) / std::fabs(c);
+    }
+};
+
+// inverse error function: Winitzki's closed-form start (2008) refined by Newton
+// steps on erf in double precision.
+double erfinv_d(double x) {
+    if (x <= -1.0) return -std::numeric_limits<double>::infinity();
+    if (x >= 1.0) return std::numeric_limits<double>::infinity();
+    const double a = 0.147;
+    double ln = std::log(1.0 - x * x);
+    double t1 = 2.0 / (M_PI * a) + 0.5 * ln;
+    double y = std::copysign(std::sqrt(std::sqrt(t1 * t1 - ln / a) - t1), x);
+    for (int i = 0; i < 4; ++i) {
+        double err = std::erf(y) - x;
+        y -= err / (2.0 / std::sqrt(M_PI) * std::exp(-y * y));
+    }
+    return y;
+}
+
+// Visible-normal sampling (Heitz & d'Eon 2014 stretch / sample slope / rotate /
+// unstretch). GGX slopes use the exact construction of Heitz 2018 ("Sampling
+// the GGX Distribution of Visible Normals", JCGT 7(4)); Beckmann slopes invert
+// the visible-slope CDF by Newton-bisection in the erf domain.
+V3 sample_vndf(int dist, V3 wi, float ax, float ay, float u1, float u2) {
+    if (dist == GGX) {
+        // z-up working frame: (x, z, y) of the y-up local frame
+        V3 V(wi.x, wi.z, wi.y);
+        V3 Vh = normalize(V3(ax * V.x, ay * V.y, V.z));
+        float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+        V3 T1 = lensq > 0.f ? V3(-Vh.y, Vh.x, 0.f) * (1.f / std::sqrt(lensq)) : V3(1.f, 0.f, 0.f);
+        V3 T2 = cross(Vh, T1);
+        float r = std::sqrt(u1);
+        float phi = 2.f * kPi * u2;
+        float t1 = r * std::cos(phi);
+        float t2 = r * std::sin(phi);
+        float s = 0.5f * (1.f + Vh.z);
+        t2 = (1.f - s) * std::sqrt(1.f - t1 * t1) + s * t2;
+        V3 Nh = T1 * t1 + T2 * t2 + Vh * std::sqrt(std::max(0.f, 1.f - t1 * t1 - t2 * t2));
+        V3 Ne = normalize(V3(ax * Nh.x, ay * Nh.y, std::max(0.f, Nh.z)));
+        return V3(Ne.x, Ne.z, Ne.y);
+    }
+    // Beckmann
+    V3 ws = normalize(V3(wi.x * ax, wi.y, wi.z * ay));
+    float cos_t = ws.y;
+    float sin_t = std::sqrt(std::max(0.f, 1.f - cos_t * cos_t));
+    float sx, sy;
+    if (cos_t > 0.99999f) {
+        double r = std::sqrt(-std::log(std::max(1e-12, 1.0 - (double)u1)));
+        double p = 2.0 * M_PI * u2;
+        sx = (float)(r * std::cos(p));
+        sy = (float)(r * std::sin(p));
+    } else {
+        double tan_t = sin_t / cos_t, cot_t = cos_t / sin_t;
+        double c = std::erf(cot_t);
+        double K = tan_t / std::sqrt(M_PI);
+        double Z = 1.0 + c + K * std::exp(-cot_t * cot_t);
+        double lo = -1.0, hi = c;
+        double uu = std::min(std::max((double)u1, 1e-7), 1.0 - 1e-7);
+        double b = -1.0 + 2.0 * uu * (c + 1.0) * 0.5;
+        for (int it = 0; it < 40; ++it) {
+            if (!(b > lo && b < hi)) b = 0.5 * (lo + hi);
+            double ei = erfinv_d(b);
+            double val = (1.0 + b + K * std::exp(-ei * ei)) / Z - uu;
+            if (std::fabs(val) < 1e-9) break;
+            if (val > 0) hi = b; else lo = b;
+            double der = (1.0 - ei * tan_t) / Z;
+            b -= val / der;
+        }
+        sx = (float)erfinv_d(b);
+        sy = (float)erfinv_d(2.0 * std::min(std::max((double)u2, 1e-7), 1.0 - 1e-7) - 1.0);
+    }
+    float phi = std::atan2(ws.z, ws.x);
+    float cp = std::cos(phi), spn = std::sin(phi);
+    if (sin_t == 0.f) { cp = 1.f; spn = 0.f; }
+    float rx = cp * sx - spn * sy;
+    float ry = spn * sx + cp * sy;
+    return normalize(V3(-rx * ax, 1.f, -ry * ay));
+}
+
+inline V3 reflect_n(V3 wi, V3 n) { return -wi + 2.f * dot(wi, n) * n; }
+// refract(wi, n, eta): src/base/utils.h:142-151
+inline V3 refract_u(V3 wi, V3 n, float eta) {
+    float ci = dot(n, wi);
+    if (ci < 0) eta = 1.f / eta;
+    float co2 = 1 - (1 - ci * ci) * (eta * eta);
+    if (co2 <= 0.f) return V3(0.f, 0.f, 0.f);
+    float sign = ci >= 0.f ? 1.f : -1.f;
+    return n * (-ci * eta + sign * std::sqrt(co2)) + wi * eta;
+}
+
+// ---------------------------------------------------------------- closures
+struct LobeEval {
+    V3 f;       // value (convention dependent)
+    float pdf;  // pdf (convention dependent)
+};
+
+bool lobe_is_delta(uint32_t id) { return id == KZ_CLOSURE_KP_MIRROR || id == KZ_CLOSURE_KP_DIELECTRIC; }
+
+Mdf make_mdf(const kz_lobe& l, V3 wi, int& dist, float& eta) {
+    Mdf m;
+    if (l.closure_id == KZ_CLOSURE_KP_GLOSS || l.closure_id == KZ_CLOSURE_KP_GLASS) {
+        dist = (int)l.params[0];
+        m.ax = l.params[7]; m.ay = l.params[8];
+        eta = l.params[9];
+    } else if (l.closure_id == KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL) {
+        dist = GGX;
+        m.ax = l.params[6]; m.ay = l.params[7];
+        eta = l.params[8];
+    } else {  // CONDUCTOR_GGX
+        dist = GGX;
+        m.ax = l.params[3]; m.ay = l.params[4];
+        eta = 1.f;
+    }
+    m.dist = dist;
+    m.wi = wi;
+    return m;
+}
+
+// Reference-convention value and pdf of one lobe (eval functions of
+// src/shading/bsdfs.cpp; on a rejected configuration the reference leaves
+// its pdf untouched, here it is 0).
+LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
+    LobeEval r{V3(0, 0, 0), 0.f};
+    switch (l.closure_id) {
+    case KZ_CLOSURE_DIFFUSE: {
+        V3 n(l.params[0], l.params[1], l.params[2]);
+        float p = std::max(dot(wo, n), 0.f) * kInvPi;
+        r.f = V3(p, p, p);
+        r.pdf = p;
+        return r;
+    }
+    case KZ_CLOSURE_KP_MIRROR:
+    case KZ_CLOSURE_KP_DIELECTRIC:
+        return r;
+    case KZ_CLOSURE_KP_GLOSS: {
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return r;
+        V3 m = normalize(wi + wo);
+        if (dot(wo, m) == 0.f) return r;
+        float D = mdf.D(m), G = mdf.G(wo);
+        float F = dist == BECKMANN ? fresnel_refl(eta, dot(m, wi)) : fresnel_refl(eta, std::fabs(dot(m, wi)));
+        float v = D * G * F / (4.f * ci * co);
+        r.f = V3(v, v, v);
+        r.pdf = mdf.pdf(m);
+        return r;
+    }
+    case KZ_CLOSURE_KP_GLASS: {
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        float ci = wi.y, co = wo.y;
+        if (eta == 1.f) return r;
+        if (ci < 0) eta = 1.f / eta;
+        if (ci * co >= 0.f) {
+            V3 m = normalize(wi + wo);
+            float cmi = dot(wi, m);
+            float F = fresnel_refl(eta, cmi);
+            // reflection_pdf / eval_reflection, bsdfs.h:541-562
+            r.pdf = cmi == 0.f ? 0.f : (1.f / (4.f * std::fabs(cmi))) * mdf.pdf(m);
+            float denom = std::fabs(4.f * wi.y * wo.y);
+            float v = denom == 0.f ? 0.f : F * mdf.D(m) * mdf.G(wo) / denom;
+            r.f = V3(v, v, v);
+        } else {
+            V3 m = normalize(wi + eta * wo);
+            if (m.y < 0.f) m = -m;
+            float cmi = dot(wi, m);
+            float F = fresnel_refl(eta, cmi);
+            // refraction_pdf / eval_refraction, bsdfs.h:564-599
+            float cmo = dot(m, wo);
+            float dn = cmi + eta * cmo;
+            r.pdf = std::fabs(dn) < 1.0e-6f ? 0.f : std::fabs(cmo) * sq(eta / dn) * mdf.pdf(m);
+            float v = 0.f;
+            if (wi.y != 0.f && wo.y != 0.f) {
+                float c = std::fabs((cmi * cmo) / (wi.y * wo.y));
+                float d2 = sq(dn);
+                if (!(std::fabs(d2) < 1.0e-6f)) v = c * mdf.D(m) * mdf.G(wo) * (1.f - F) * sq(eta) / sq(d2);
+            }
+            r.f = V3(v, v, v);
+        }
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL: {
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        V3 F0(l.params[0], l.params[1], l.params[2]);
+        float co = wo.y, ci = wi.y;
+        if (ci * co < 0.) return r;
+        V3 wh = normalize(wi + wo);
+        float com = dot(wo, wh);
+        if (com == 0.f) return r;
+        float D = std::min(4.f, mdf.D(wh));
+        float G = mdf.G(wo);
+        float s = fresnel_schlick_eta(eta, com);
+        V3 F(F0.x + (1.f - F0.x) * s, F0.y + (1.f - F0.y) * s, F0.z + (1.f - F0.z) * s);
+        r.pdf = std::max(0.f, mdf.pdf(wh));
+        float k = D * G / (4.f * ci * co);
+        r.f = V3(std::min(1.f, k * F.x), std::min(1.f, k * F.y), std::min(1.f, k * F.z));
+        return r;
+    }
+    case KZ_CLOSURE_CONDUCTOR_GGX: {
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return r;
+        V3 m = normalize(wi + wo);
+        float com = dot(wo, m);
+        if (com <= 0.f) return r;
+        float w = schlick_weight(com);
+        V3 F(l.params[0] + (1.f - l.params[0]) * w, l.params[1] + (1.f - l.params[1]) * w,
+             l.params[2] + (1.f - l.params[2]) * w);
+        float k = mdf.D(m) * mdf.G(wo) / (4.f * ci * co);
+        r.f = V3(k * F.x, k * F.y, k * F.z);
+        r.pdf = mdf.pdf(m);
+        return r;
+    }
+    default:
+        return r;
+    }
+}
+
+// Integrator convention: f*|cos(wo)| and the solid-angle pdf of wo under the
+// lobe's own sampling routine.
+LobeEval eval_integrator(const kz_lobe& l, V3 wi, V3 wo) {
+    LobeEval r = eval_reference(l, wi, wo);
+    switch (l.closure_id) {
+    case KZ_CLOSURE_DIFFUSE:
+        return r;  // already f*cos with pdf cos/pi
+    case KZ_CLOSURE_KP_GLOSS:
+    case KZ_CLOSURE_CONDUCTOR_GGX:
+    case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL: {
+        if (r.pdf == 0.f) return LobeEval{V3(0, 0, 0), 0.f};
+        if (wi.y <= 0.f || wo.y <= 0.f) return LobeEval{V3(0, 0, 0), 0.f};
+        V3 m = normalize(wi + wo);
+        float wom = std::fabs(dot(wo, m));
+        if (wom == 0.f) return LobeEval{V3(0, 0, 0), 0.f};
+        r.pdf = r.pdf / (4.f * wom);
+        r.f = r.f * std::fabs(wo.y);
+        return r;
+    }
+    case KZ_CLOSURE_KP_GLASS: {
+        // the sampling routine picks reflection with probability F and
+        // refraction with 1-F (bsdfs.cpp:499-553); fold that into the pdf.
+        float eta = l.params[9];
+        if (eta == 1.f) return LobeEval{V3(0, 0, 0), 0.f};
+        if (wi.y < 0) eta = 1.f / eta;
+        V3 m;
+        if (wi.y * wo.y >= 0.f) m = normalize(wi + wo);
+        else {
+            m = normalize(wi + eta * wo);
+            if (m.y < 0.f) m = -m;
+        }
+        float F = fresnel_refl(eta, std::min(std::max(dot(m, wi), -1.f), 1.f));
+        r.pdf *= (wi.y * wo.y >= 0.f) ? F : (1.f - F);
+        r.f = r.f * std::fabs(wo.y);
+        return r;
+    }
+    default:
+        return LobeEval{V3(0, 0, 0), 0.f};
+    }
+}
+
+struct LobeSample {
+    V3 wo;
+    V3 weight;  // f*|cos|/pdf (or delta weight)
+    float pdf;  // 0 for delta
+    bool valid, delta;
+};
+
+LobeSample sample_lobe(const kz_lobe& l, V3 wi, float u0, float u1, float u2) {
+    LobeSample s{V3(0, 0, 0), V3(0, 0, 0), 0.f, false, false};
+    switch (l.closure_id) {
+    case KZ_CLOSURE_DIFFUSE: {
+        // cosine-weighted hemisphere about +y (the pdf the reference declares)
+        float r = std::sqrt(u0);
+        float phi = 2.f * kPi * u1;
+        float x = r * std::cos(phi), z = r * std::sin(phi);
+        float y = std::sqrt(std::max(0.f, 1.f - x * x - z * z));
+        s.wo = V3(x, y, z);
+        LobeEval e = eval_integrator(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
+        return s;
+    }
+    case KZ_CLOSURE_KP_MIRROR: {
+        s.wo = reflect_n(wi, V3(0, 1, 0));
+        s.weight = V3(1, 1, 1);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_KP_DIELECTRIC: {
+        float ior_in = l.params[0], ior_ex = l.params[1];
+        V3 n(0, 1, 0);
+        float ci = dot(wi, n);
+        float F = fresnel_utils(ci, ior_ex, ior_in);
+        if (u0 < F) {
+            s.wo = reflect_n(wi, n);
+        } else {
+            float fac = ior_in / ior_ex;
+            if (ci < 0.f) {
+                fac = ior_ex / ior_in;
+                n = -n;
+            }
+            s.wo = refract_u(-wi, n, fac);
+            if (is_zero(s.wo)) return s;
+        }
+        s.weight = V3(1, 1, 1);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_KP_GLOSS:
+    case KZ_CLOSURE_CONDUCTOR_GGX:
+    case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL: {
+        if (wi.y <= 0.f) return s;
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        V3 m = sample_vndf(dist, wi, mdf.ax, mdf.ay, u0, u1);
+        s.wo = reflect_n(wi, m);
+        if (s.wo.y <= 0.f) return s;
+        LobeEval e = eval_integrator(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
+        return s;
+    }
+    case KZ_CLOSURE_KP_GLASS: {
+        int dist; float eta;
+        Mdf mdf = make_mdf(l, wi, dist, eta);
+        if (eta == 1.f) return s;
+        if (wi.y < 0.f) eta = 1.f / eta;
+        // sample_m flips wi into the upper hemisphere (microfacet.h:200-203)
+        V3 wis = wi.y < 0.f ? -wi : wi;
+        V3 m = sample_vndf(dist, wis, mdf.ax, mdf.ay, u0, u1);
+        float cmi = std::min(std::max(dot(m, wi), -1.f), 1.f);
+        float F = fresnel_refl(eta, cmi);
+        if (u2 < F) {
+            s.wo = reflect_n(wi, m);
+            if (wi.y * s.wo.y <= 0.f) return s;
+        } else {
+            s.wo = refract_u(wi, m, eta);
+            if (is_zero(s.wo) || wi.y * s.wo.y > 0.f) return s;
+            s.wo = normalize(s.wo);
+        }
+        LobeEval e = eval_integrator(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
+        return s;
+    }
+    default:
+        return s;
+    }
+}
+
+// ---------------------------------------------------------------- scene
+struct OLight {
+    uint32_t geom;
+    std::vector<uint32_t> tris;  // global triangle ids
+    std::vector<float> cdf;      // normalised running sum of areas, cdf[0] = 0
+    float area;
+    V3 Le;
+};
+
+struct OScene {
+    OBvh bvh;
+    std::vector<uint32_t> tri_geom;
+    std::vector<int32_t> geom_material;
+    std::vector<int32_t> geom_light;  // light index or -1
+    std::vector<kz_material> materials;
+    std::vector<OLight> lights;
+};
+
+float tri_area(const OBvh& b, uint32_t tri) {
+    V3 p0 = b.v(tri, 0), p1 = b.v(tri, 1), p2 = b.v(tri, 2);
+    V3 c = cross(p1 - p0, p2 - p0);
+    return 0.5f * std::sqrt(dot(c, c));
+}
+
+// DiscrectPDF::sample, src/base/dpdf.h:31-36 (lower_bound over the cdf)
+uint32_t cdf_sample(const std::vector<float>& cdf, float u) {
+    auto it = std::lower_bound(cdf.begin(), cdf.end(), u);
+    long idx = (long)(it - cdf.begin()) - 1;
+    if (idx < 0) idx = 0;
+    long last = (long)cdf.size() - 2;
+    return (uint32_t)std::min(idx, last);
+}
+
+struct CamBasis {
+    V3 eye, x, y, z;
+    float tan_half, aspect;
+    float flip;
+};
+
+CamBasis cam_basis(const kz_camera& c, uint32_t W, uint32_t H) {
+    CamBasis b;
+    V3 eye(c.eye[0], c.eye[1], c.eye[2]);
+    V3 look(c.lookat[0], c.lookat[1], c.lookat[2]);
+    V3 up = normalize(V3(c.up[0], c.up[1], c.up[2]));
+    b.eye = eye;
+    b.z = normalize(eye - look);
+    b.x = normalize(cross(up, b.z));
+    b.y = cross(b.z, b.x);
+    b.tan_half = (float)std::tan((double)c.fov_deg * 0.5 * M_PI / 180.0);
+    b.aspect = (float)W / (float)H;
+    b.flip = c.flip ? -1.f : 1.f;
+    return b;
+}
+
+V3 cam_dir(const CamBasis& b, uint32_t px, uint32_t py, uint32_t W, uint32_t H, float jx, float jy) {
+    float sx = ((float)px + jx) / (float)W;
+    float sy = ((float)py + jy) / (float)H;
+    float nx = 2.0f * sx - 1.0f;
+    float ny = b.flip * ((1.0f - 2.0f * sy) / b.aspect);
+    float cx = nx * b.tan_half;
+    float cy = ny * b.tan_half;
+    V3 d = b.x * cx + b.y * cy + b.z * (-1.0f);
+    return normalize(d);
+}
+
+inline float power_heuristic(float f, float g) {
+    // power_heuristic(1, f, 1, g), src/core/sampling.h:61-64
+    return (f * f) / (f * f + g * g);
+}
+
+struct PathCounters {
+    uint64_t bounces = 0, shadow = 0;
+};
+
+// One path of the corrected PathIntegrator::Li (src/core/integrator.cpp:362-561).
+// Random numbers: 9 per shaded vertex, in a fixed order, whatever branches run:
+//   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
+//   [5] lobe pick   [6,7,8] lobe sample
+V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_min, PathCounters& pc) {
+    V3 L(0, 0, 0), beta(1, 1, 1);
+    float prev_pdf = 0.f;
+    bool prev_specular = true;
+    const uint32_t nl = (uint32_t)sc.lights.size();
+    for (uint32_t depth = 0; depth < max_depth; ++depth) {
+        float t, bu, bv;
+        uint32_t prim;
+        pc.bounces++;
+        if (!sc.bvh.closest(o, d, kRayEps, std::numeric_limits<float>::infinity(), t, prim, bu, bv)) break;
+        float u[9];
+        for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
+        const uint32_t geom = sc.tri_geom[prim];
+        const kz_material& mat = sc.materials[(size_t)sc.geom_material[geom]];
+        V3 v0 = sc.bvh.v(prim, 0), v1 = sc.bvh.v(prim, 1), v2 = sc.bvh.v(prim, 2);
+        V3 Ng = normalize(cross(v1 - v0, v2 - v0));
+        V3 P = o + d * t;
+        Frame fr(Ng);
+        V3 wi = -fr.to_local(d);
+        // 1. emission on hit (front side only, single_emissive_surface)
+        V3 Le(mat.Le[0], mat.Le[1], mat.Le[2]);
+        if (!is_zero(Le) && dot(d, Ng) < 0.f) {
+            float w = 1.f;
+            if (!prev_specular) {
+                int li = sc.geom_light[geom];
+                if (li >= 0) {
+                    float cos_l = -dot(d, Ng);
+                    float lpdf = (t * t) / (cos_l * sc.lights[(size_t)li].area) * (1.0f / (float)nl);
+                    w = power_heuristic(prev_pdf, lpdf);
+                }
+            }
+            L = L + mul(beta, Le) * w;
+        }
+        // lobe selection probabilities, CompositeClosure::compute_pdfs (bsdf.h:157-176)
+        const uint32_t nlobes = std::min<uint32_t>(mat.n_lobes, KZ_MAX_LOBES);
+        float lp[KZ_MAX_LOBES];
+        float bsum = beta.x + beta.y + beta.z;
+        float winv = 1.f / bsum;
+        float wsum = 0.f;
+        bool any_smooth = false;
+        for (uint32_t i = 0; i < nlobes; ++i) {
+            const kz_lobe& lb = mat.lobes[i];
+            lp[i] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
+            wsum += lp[i];
+            if (!lobe_is_delta(lb.closure_id)) any_smooth = true;
+        }
+        if (wsum > 0.f)
+            for (uint32_t i = 0; i < nlobes; ++i) lp[i] /= wsum;
+        // 2. next-event estimation
+        if (nl > 0 && any_smooth && wsum > 0.f) {
+            uint32_t li = std::min((uint32_t)(u[0] * (float)nl), nl - 1);
+            const OLight& lt = sc.lights[li];
+            uint32_t k = cdf_sample(lt.cdf, u[1]);
+            uint32_t ltri = lt.tris[k];
+            V3 a0 = sc.bvh.v(ltri, 0), a1 = sc.bvh.v(ltri, 1), a2 = sc.bvh.v(ltri, 2);
+            float su0 = std::sqrt(u[2]);
+            float bu0 = 1.f - su0;
+            float bv0 = u[3] * su0;
+            V3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+            V3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+            V3 lv = p - P;
+            float dist2 = dot(lv, lv);
+            float dist = std::sqrt(dist2);
+            V3 ldir(lv.x / dist, lv.y / dist, lv.z / dist);
+            float cos_l = -dot(ldir, nlgt);
+            if (cos_l > 0.f) {
+                float pdf_solid = dist2 / (cos_l * lt.area);
+                float lpdf = pdf_solid * (1.0f / (float)nl);
+                V3 wo = fr.to_local(ldir);
+                V3 f(0, 0, 0);
+                float bpdf = 0.f;
+                for (uint32_t i = 0; i < nlobes; ++i) {
+                    const kz_lobe& lb = mat.lobes[i];
+                    if (lobe_is_delta(lb.closure_id)) continue;
+                    LobeEval e = eval_integrator(lb, wi, wo);
+                    f = f + mul(V3(lb.weight[0], lb.weight[1], lb.weight[2]), e.f);
+                    bpdf += lp[i] * e.pdf;
+                }
+                if (!is_zero(f)) {
+                    pc.shadow++;
+                    if (!sc.bvh.any(P, ldir, kRayEps, dist - kRayEps)) {
+                        float w = power_heuristic(lpdf, bpdf);
+                        V3 c = mul(mul(beta, f), lt.Le) * (w / lpdf);
+                        L = L + c;
+                    }
+                }
+            }
+        }
+        if (depth + 1 >= max_depth) break;
+        // 3. Russian roulette (integrator.cpp:491-498)
+        if (depth >= rr_min) {
+            float prob = std::min(max_comp(beta) * 0.9025f, 0.99f);
+            if (prob < u[4]) break;
+            beta = beta * (1.f / prob);
+        }
+        // 4. BSDF sampling: lobe by its selection probability, then the
+        // one-sample mixture over all non-delta lobes.
+        if (!(wsum > 0.f)) break;
+        uint32_t sel = nlobes - 1;
+        {
+            float acc = 0.f;
+            for (uint32_t i = 0; i < nlobes; ++i) {
+                acc += lp[i];
+                if (u[5] < acc) { sel = i; break; }
+            }
+            while (sel > 0 && lp[sel] == 0.f) --sel;
+        }
+        const kz_lobe& ls = mat.lobes[sel];
+        LobeSample smp = sample_lobe(ls, wi, u[6], u[7], u[8]);
+        if (!smp.valid) break;
+        V3 weight;
+        float pdf_dir;
+        if (smp.delta) {
+            weight = mul(V3(ls.weight[0], ls.weight[1], ls.weight[2]), smp.weight) * (1.f / lp[sel]);
+            pdf_dir = 0.f;
+        } else {
+            V3 f(0, 0, 0);
+            float pdf = 0.f;
+            for (uint32_t i = 0; i < nlobes; ++i) {
+                const kz_lobe& lb = mat.lobes[i];
+                if (lobe_is_delta(lb.closure_id)) continue;
+                LobeEval e = eval_integrator(lb, wi, smp.wo);
+                f = f + mul(V3(lb.weight[0], lb.weight[1], lb.weight[2]), e.f);
+                pdf += lp[i] * e.pdf;
+            }
+            if (!(pdf > 0.f)) break;
+            weight = f * (1.f / pdf);
+            pdf_dir = pdf;
+        }
+        beta = mul(beta, weight);
+        if (is_zero(beta)) break;
+        prev_pdf = pdf_dir;
+        prev_specular = smp.delta;
+        o = P;
+        d = normalize(fr.to_world(smp.wo));
+    }
+    return L;
+}
+
+}  // namespace
+
+// =================================================================== C API
+extern "C" {
+
+void* kzo_bvh_build(const float* tri_verts, uint32_t ntris) {
+    OBvh* b = new OBvh();
+    b->ntris = ntris;
+    b->verts.assign(tri_verts, tri_verts + (size_t)ntris * 9);
+    b->build();
+    return b;
+}
+
+void kzo_bvh_free(void* h) { delete static_cast<OBvh*>(h); }
+
+void kzo_closest(void* h, const kz_ray* rays, uint64_t n, int nthreads, float* t, uint32_t* prim, float* u, float* v) {
+    const OBvh* b = static_cast<const OBvh*>(h);
+    parallel_for(n, nthreads, [&](uint64_t i) {
+        const kz_ray& r = rays[i];
+        float tt, uu = 0.f, vv = 0.f;
+        uint32_t p;
+        b->closest(V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz), r.tmin, r.tmax, tt, p, uu, vv);
+        t[i] = tt;
+        prim[i] = p;
+        if (u) u[i] = p == KZ_INVALID_ID ? 0.f : uu;
+        if (v) v[i] = p == KZ_INVALID_ID ? 0.f : vv;
+    });
+}
+
+void kzo_any(void* h, const kz_ray* rays, uint64_t n, int nthreads, uint8_t* occ) {
+    const OBvh* b = static_cast<const OBvh*>(h);
+    parallel_for(n, nthreads, [&](uint64_t i) {
+        const kz_ray& r = rays[i];
+        occ[i] = b->any(V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz), r.tmin, r.tmax) ? 1 : 0;
+    });
+}
+
+// Brute force over all triangles (small cases only): same tie rule.
+void kzo_closest_brute(const float* tri_verts, uint32_t ntris, const kz_ray* rays, uint64_t n, float* t, uint32_t* prim) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const kz_ray& r = rays[i];
+        RayPre rp = ray_pre(V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz));
+        float best = r.tmax;
+        uint32_t bp = KZ_INVALID_ID;
+        for (uint32_t k = 0; k < ntris; ++k) {
+            const float* p = tri_verts + (size_t)k * 9;
+            float tt, bu, bv;
+            if (!tri_hit(rp, V3(p[0], p[1], p[2]), V3(p[3], p[4], p[5]), V3(p[6], p[7], p[8]), tt, bu, bv)) continue;
+            if (!(tt > r.tmin) || !(tt <= r.tmax)) continue;
+            if (tt < best || (tt == best && k < bp)) { best = tt; bp = k; }
+        }
+        t[i] = best;
+        prim[i] = bp;
+    }
+}
+
+void kzo_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n, int conv, float* f, float* pdf) {
+    for (uint64_t i = 0; i < n; ++i) {
+        V3 a(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]), b(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        LobeEval e = conv == KZ_CONVENTION_REFERENCE ? eval_reference(lobes[i], a, b) : eval_integrator(lobes[i], a, b);
+        f[3 * i] = e.f.x; f[3 * i + 1] = e.f.y; f[3 * i + 2] = e.f.z;
+        pdf[i] = e.pdf;
+    }
+}
+
+void kzo_closure_sample(const kz_lobe* lobes, const float* wi, const float* u, uint64_t n, float* wo, float* weight,
+                        float* pdf, uint8_t* flags) {
+    for (uint64_t i = 0; i < n; ++i) {
+        V3 a(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+        LobeSample s = sample_lobe(lobes[i], a, u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+        wo[3 * i] = s.wo.x; wo[3 * i + 1] = s.wo.y; wo[3 * i + 2] = s.wo.z;
+        weight[3 * i] = s.weight.x; weight[3 * i + 1] = s.weight.y; weight[3 * i + 2] = s.weight.z;
+        pdf[i] = s.pdf;
+        flags[i] = (uint8_t)((s.valid ? 1 : 0) | (s.delta ? 2 : 0));
+    }
+}
+
+// Microfacet white-furnace integrals, src/shading/white_furnace.{h,cpp}.
+// weak test: sum over (theta, phi) grid of sin*D(h)*G1(h)/|4 V.y| (y-up).
+double kzo_furnace_weak(int dist, float theta_deg, float alpha) {
+    float th = theta_deg / 180.f * kPi;
+    Mdf mdf;
+    mdf.dist = dist;
+    mdf.wi = V3(std::sin(th), std::cos(th), 0.f);
+    mdf.ax = mdf.ay = alpha;
+    V3 V = mdf.wi;
+    float integral = 0.f;
+    const float dth = 0.05f, dph = 0.05f;
+    for (int i = 0; i * dth < kPi; ++i) {
+        float theta = i * dth;
+        float st = std::sin(theta), ct = std::cos(theta);
+        for (int j = 0; j * dph < 2.f * kPi; ++j) {
+            float phi = j * dph;
+            float sp = std::sin(phi), cp = std::cos(phi);
+            V3 Lv(cp * st, ct, sp * st);
+            V3 H = normalize(V + Lv);
+            integral += st * mdf.D(H) * mdf.G1(H) / std::fabs(4.f * V.y);
+        }
+    }
+    return (double)(integral * dth * dph);
+}
+
+// fixed_beckmann_white_furnace_test(alpha, theta_o), white_furnace.cpp:3-36 (z-up)
+double kzo_furnace_fixed_beckmann(float alpha, float theta_o) {
+    float so = std::sin(theta_o), co = std::cos(theta_o);
+    V3 V(so, 0.f, co);
+    float a = 1.f / (alpha * std::tan(theta_o));
+    float a2 = a * a;
+    float lambda = 0.f;
+    if (a < 1.6f) lambda = (1 - 1.259f * a + 0.396f * a2) / (3.535f * a + 2.181f * a2);
+    float G = 1.f / (1.f + lambda);
+    float integral = 0.f;
+    const float dth = 0.05f, dph = 0.05f;
+    for (int i = 0; i * dth < kPi; ++i) {
+        float ti = i * dth;
+        for (int j = 0; j * dph < 2.f * kPi; ++j) {
+            float phi = j * dph;
+            float si = std::sin(ti), ci = std::cos(ti), sp = std::sin(phi), cp = std::cos(phi);
+            V3 Lv(cp * si, sp * si, ci);
+            V3 H = normalize(V + Lv);
+            if (H.z <= 0) continue;
+            float th = std::acos(H.z);
+            float D = std::exp(-std::pow(std::tan(th) / alpha, 2.f)) / (kPi * alpha * alpha * std::pow(H.z, 4.f));
+            integral += si * D * G / std::fabs(4 * V.z);
+        }
+    }
+    return (double)(integral * dth * dph);
+}
+
+void* kzo_scene_create(const float* tri_verts, uint32_t ntris, const uint32_t* tri_geom, const int32_t* geom_material,
+                       const int32_t* geom_is_light, uint32_t ngeom, const kz_material* mats, uint32_t nmats) {
+    OScene* s = new OScene();
+    s->bvh.ntris = ntris;
+    s->bvh.verts.assign(tri_verts, tri_verts + (size_t)ntris * 9);
+    s->bvh.build();
+    s->tri_geom.assign(tri_geom, tri_geom + ntris);
+    s->geom_material.assign(geom_material, geom_material + ngeom);
+    s->materials.assign(mats, mats + nmats);
+    s->geom_light.assign(ngeom, -1);
+    // one GeometryLight per emissive mesh, in mesh order; area CDF in triangle
+    // order (TriangleMesh::setup_dpdf, shape.cpp:700-709)
+    for (uint32_t g = 0; g < ngeom; ++g) {
+        if (!geom_is_light[g]) continue;
+        OLight lt;
+        lt.geom = g;
+        const kz_material& m = mats[geom_material[g]];
+        lt.Le = V3(m.Le[0], m.Le[1], m.Le[2]);
+        for (uint32_t k = 0; k < ntris; ++k)
+            if (tri_geom[k] == g) lt.tris.push_back(k);
+        if (lt.tris.empty()) continue;
+        lt.cdf.push_back(0.f);
+        for (uint32_t k : lt.tris) lt.cdf.push_back(lt.cdf.back() + tri_area(s->bvh, k));
+        float sum = lt.cdf.back();
+        lt.area = sum;
+        if (sum > 0.f) {
+            float nrm = 1.f / sum;
+            for (size_t k = 1; k < lt.cdf.size(); ++k) lt.cdf[k] *= nrm;
+            lt.cdf.back() = 1.f;
+        }
+        s->geom_light[g] = (int32_t)s->lights.size();
+        s->lights.push_back(std::move(lt));
+    }
+    return s;
+}
+
+void kzo_scene_free(void* h) { delete static_cast<OScene*>(h); }
+
+// Renders rows [row_begin, row_end) of a W x H frame; out: W*H*3 doubles
+// (spp average, FP64 accumulation); stats[0] = path bounces, stats[1] = shadow rays.
+void kzo_render(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_render_config* cfg, int nthreads,
+                uint32_t row_begin, uint32_t row_end, double* out, uint64_t* stats) {
+    const OScene* sc = static_cast<const OScene*>(h);
+    CamBasis cb = cam_basis(*cam, W, H);
+    row_end = std::min(row_end, H);
+    const uint64_t npix = (uint64_t)(row_end - row_begin) * W;
+    const uint32_t spp = cfg->spp;
+    std::atomic<uint64_t> nb{0}, ns{0};
+    parallel_for(npix, nthreads, [&](uint64_t i) {
+        uint64_t pix = (uint64_t)row_begin * W + i;
+        uint32_t px = (uint32_t)(pix % W), py = (uint32_t)(pix / W);
+        double acc[3] = {0, 0, 0};
+        PathCounters pc;
+        for (uint32_t s = 0; s < spp; ++s) {
+            Pcg32 rng;
+            rng.seed(cfg->seed, pix * spp + s);
+            float jx = rng.nextf(), jy = rng.nextf();
+            V3 d = cam_dir(cb, px, py, W, H, jx, jy);
+            V3 L = Li(*sc, cb.eye, d, rng, cfg->max_depth, cfg->rr_min_depth, pc);
+            acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
+        }
+        for (int c = 0; c < 3; ++c) out[pix * 3 + c] = acc[c] / (double)spp;
+        nb += pc.bounces;
+        ns += pc.shadow;
+    });
+    if (stats) {
+        stats[0] = nb.load();
+        stats[1] = ns.load();
+    }
+}
+
+// Camera rays of a frame, exactly as the renderer generates them (first two
+// draws of each stream); rays: W*H*spp records.
+void kzo_camera_rays(const kz_camera* cam, uint32_t W, uint32_t H, uint32_t spp, uint64_t seed, kz_ray* rays) {
+    CamBasis cb = cam_basis(*cam, W, H);
+    for (uint64_t pix = 0; pix < (uint64_t)W * H; ++pix)
+        for (uint32_t s = 0; s < spp; ++s) {
+            Pcg32 rng;
+            rng.seed(seed, pix * spp + s);
+            float jx = rng.nextf(), jy = rng.nextf();
+            V3 d = cam_dir(cb, (uint32_t)(pix % W), (uint32_t)(pix / W), W, H, jx, jy);
+            kz_ray& r = rays[pix * spp + s];
+            r.ox = cb.eye.x; r.oy = cb.eye.y; r.oz = cb.eye.z; r.tmin = kRayEps;
+            r.dx = d.x; r.dy = d.y; r.dz = d.z; r.tmax = std::numeric_limits<float>::infinity();
+        }
+}
+
+// Li of explicit rays; ray i uses PCG32 stream (seed, i).
+void kzo_li(void* h, const kz_ray* rays, uint64_t n, const kz_render_config* cfg, int nthreads, double* out,
+            uint64_t* stats) {
+    const OScene* sc = static_cast<const OScene*>(h);
+    std::atomic<uint64_t> nb{0}, ns{0};
+    parallel_for(n, nthreads, [&](uint64_t i) {
+        Pcg32 rng;
+        rng.seed(cfg->seed, i);
+        PathCounters pc;
+        const kz_ray& r = rays[i];
+        V3 L = Li(*sc, V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz), rng, cfg->max_depth, cfg->rr_min_depth, pc);
+        out[3 * i] = L.x; out[3 * i + 1] = L.y; out[3 * i + 2] = L.z;
+        nb += pc.bounces;
+        ns += pc.shadow;
+    });
+    if (stats) {
+        stats[0] = nb.load();
+        stats[1] = ns.load();
+    }
+}
+
+// First 16 outputs of a PCG32 stream (known-answer check of the generator).
+void kzo_pcg32_outputs(uint64_t initstate, uint64_t initseq, uint32_t* out, int n) {
+    Pcg32 r;
+    r.seed(initstate, initseq);
+    for (int i = 0; i < n; ++i) out[i] = r.next();
+}
+
+}  // extern "C"

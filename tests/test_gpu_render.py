@@ -1,0 +1,117 @@
+"""GPU wavefront path integrator against the CPU restatement of
+PathIntegrator::Li. Both draw every path from the same PCG32 stream, so the
+images agree far more tightly than two independent renders: the stated bound
+is relMSE <= 1e-3 (spec image tolerance), with the FP64-accumulated CPU
+image as the reference."""
+import numpy as np
+import pytest
+
+from kazen_proto_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+REL_MSE_TOL = 1e-3
+
+
+def rel_mse(img, ref, eps=1e-2):
+    img = np.asarray(img, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
+
+
+def oracle_camera(O, cam):
+    return O.make_camera(cam.eye, cam.lookat, cam.up, cam.fov, cam.flip)
+
+
+@pytest.fixture(scope="module")
+def box():
+    d = scenes.box_scene(64, 64, spp=16, max_depth=5)
+    return d, d.build()
+
+
+def test_box_scene_matches_restatement(gpu, oracle_mod, box):
+    d, s = box
+    W, H, spp = 64, 64, 16
+    r = api.Renderer(spp=spp, max_depth=5, seed=3)
+    img, img64 = r.render(s, d.camera, W, H, fp64=True)
+    osc = oracle_mod.Scene.from_desc(d)
+    ref, st = osc.render(oracle_camera(oracle_mod, d.camera), W, H, spp, 5, seed=3)
+    e = rel_mse(img64, ref)
+    assert e <= REL_MSE_TOL, e
+    assert e <= 1e-5, f"same-stream renders should agree to ~1e-6, got {e}"
+    assert rel_mse(img, img64) < 1e-8
+    # the same paths are traced: bounce and shadow-ray counts agree closely
+    g = r.last_stats
+    assert abs(g["path_bounces"] - st["path_bounces"]) <= 1e-3 * st["path_bounces"]
+    assert abs(g["shadow_rays"] - st["shadow_rays"]) <= 1e-3 * st["shadow_rays"]
+    assert g["paths"] == W * H * spp
+
+
+def test_box_scene_1024spp(gpu, oracle_mod, box):
+    """Converged image at 1024 spp within relMSE 1e-3 of the FP64 CPU render."""
+    d, s = box
+    W, H, spp = 32, 32, 1024
+    img = api.Renderer(spp=spp, max_depth=5, seed=11).render(s, d.camera, W, H)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), W, H, spp, 5, seed=11)
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+
+
+def test_wavefront_refill_is_deterministic(gpu, box):
+    d, s = box
+    a = api.Renderer(spp=8, max_depth=5, seed=5).render(s, d.camera, 48, 40)
+    b = api.Renderer(spp=8, max_depth=5, seed=5, wavefront_size=777, block_size=64).render(s, d.camera, 48, 40)
+    assert rel_mse(a, b) < 1e-10
+    c = api.Renderer(spp=8, max_depth=5, seed=6).render(s, d.camera, 48, 40)
+    assert rel_mse(a, c) > 1e-4  # another seed is another estimate
+
+
+def test_li_batch_matches_restatement(gpu, oracle_mod, box):
+    d, s = box
+    cam = oracle_camera(oracle_mod, d.camera)
+    rays = oracle_mod.camera_rays(cam, 32, 32, 4, seed=2)
+    integ = api.PathIntegrator(max_depth=5, seed=9)
+    integ.setup(s)
+    L = integ.Li(rays)
+    Lo, st = oracle_mod.Scene.from_desc(d).li(rays, 5, seed=9)
+    assert rel_mse(L, Lo) < 1e-5
+    close = np.all(np.abs(L - Lo) <= 1e-3 * np.maximum(1.0, np.abs(Lo)), axis=1)
+    assert close.mean() > 0.995
+
+
+def test_device_memory_render_matches_host(gpu, box):
+    torch = pytest.importorskip("torch")
+    d, s = box
+    W, H = 40, 30
+    r = api.Renderer(spp=4, max_depth=5, seed=1)
+    host = r.render(s, d.camera, W, H)
+    rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    rgb64 = torch.empty((H, W, 3), dtype=torch.float64, device="cuda")
+    r.render(s, d.camera, W, H, device_out=(rgb, rgb64))
+    assert rel_mse(rgb.cpu().numpy(), host) < 1e-10
+    assert rel_mse(rgb64.cpu().numpy(), host) < 1e-8
+
+
+def test_mixture_and_delta_materials(gpu, oracle_mod):
+    """The shipped cbox shaders (diffuse, rough = 0.5 diffuse + 0.1 Beckmann
+    microfacet, mirror, dielectric, emitter) lowered and rendered."""
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    rough = api.material([api.diffuse((0.35, 0.35, 0.35)), api.microfacet("beckmann", 0.28, eta=1.5,
+                                                                         weight=(0.07, 0.07, 0.07))])
+    d.materials[2] = rough                                          # white walls -> rough
+    d.materials[3] = api.material([api.dielectric(1.5046, 1.000277)])  # metal box -> glass
+    d.materials.append(api.material([api.mirror((0.9, 0.9, 0.9))]))
+    v, i = scenes.box((0.1, 0.0, 0.1), (0.25, 0.15, 0.25))
+    d.add(v, i, len(d.materials) - 1)
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=6, seed=4).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=4)
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+
+
+def test_terrain_scene_small(gpu, oracle_mod):
+    d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
+    s = d.build()
+    img = api.Renderer(spp=2, max_depth=8, seed=1).render(s, d.camera, 64, 36)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 64, 36, 2, 8, seed=1)
+    assert np.isfinite(img).all()
+    assert rel_mse(img, ref) <= REL_MSE_TOL

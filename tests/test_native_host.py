@@ -1,0 +1,119 @@
+"""CPU-side tests of the C-ABI library: it builds for sm_103a, loads, exports
+every entry point the header declares, and validates host input before any
+device work. No compute calls are made without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from kazen_proto_gb300 import _native as N
+from kazen_proto_gb300 import api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "kazen_gb300.h")
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(kz_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_header_declares_the_boundary():
+    fns = header_functions()
+    for f in ["kz_scene_create", "kz_scene_add_mesh", "kz_scene_build", "kz_intersect_closest", "kz_intersect_any",
+              "kz_li_batch", "kz_render", "kz_closure_eval_batch", "kz_closure_sample_batch", "kz_last_error_string"]:
+        assert f in fns
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    for f in header_functions():
+        assert hasattr(native_lib, f), f
+    assert set(header_functions()) == set(N.SIGNATURES), "ctypes signature table out of sync with the header"
+
+
+def test_library_is_built_for_sm_103a():
+    from kazen_proto_gb300 import build as kb
+    assert "arch=compute_103a,code=sm_103a" in " ".join(kb.ARCH)
+    assert "--fmad=false" in kb.common_flags()
+
+
+def test_struct_layouts_match_header():
+    assert C.sizeof(N.KzRay) == 32
+    assert C.sizeof(N.KzLobe) == 64
+    assert C.sizeof(N.KzMaterial) == 16 + 8 * 64
+    assert N.RAY_DTYPE.itemsize == 32
+
+
+def test_abi_version_and_device_query(native_lib):
+    assert native_lib.kz_abi_version() == 1
+    assert native_lib.kz_device_count() >= 0
+
+
+def test_scene_handle_validates_on_host(native_lib):
+    s = api.Scene()
+    with pytest.raises(N.KazenError) as e:
+        s.add_mesh(np.array([[0, 0, 0], [1, 0, 0], [0, np.nan, 0]], np.float32), [[0, 1, 2]])
+    assert e.value.code == N.KZ_ERR_INVALID_ARG
+    with pytest.raises(N.KazenError) as e:
+        s.add_mesh(np.zeros((3, 3), np.float32), [[0, 1, 3]])
+    assert e.value.code == N.KZ_ERR_INVALID_ARG and "out of range" in str(e.value)
+    with pytest.raises(N.KazenError):
+        s.add_mesh(np.zeros((3, 3), np.float32), [[0, 1, 2]], xform=[1, 0, 0, 0, 0, np.inf, 0, 0, 0, 0, 1, 0])
+    assert s.add_mesh(np.eye(3, dtype=np.float32), [[0, 1, 2]], material_id=0) == 0
+    # materials: bad closure id, emission as a lobe, zero roughness, negative Le
+    with pytest.raises(N.KazenError):
+        s.set_materials([api.material([api.lobe(99)])])
+    with pytest.raises(N.KazenError):
+        s.set_materials([api.material([api.lobe(N.KZ_CLOSURE_KP_EMITTER)])])
+    with pytest.raises(N.KazenError):
+        s.set_materials([api.material([api.conductor_ggx(alpha=0.0)])])
+    with pytest.raises(N.KazenError):
+        s.set_materials([api.material([], Le=(-1, 0, 0))])
+    # a mesh that names a material that does not exist is rejected at build
+    s.set_materials([])
+    with pytest.raises(N.KazenError) as e:
+        s.build_bvh()
+    assert e.value.code == N.KZ_ERR_INVALID_ARG
+    s.close()
+
+
+def test_calls_before_build_report_state(native_lib):
+    s = api.Scene()
+    r = api.make_rays([[0, 0, 0]], [[0, 0, 1]])
+    with pytest.raises(N.KazenError) as e:
+        s.intersect(r)
+    assert e.value.code == N.KZ_ERR_STATE
+    s.close()
+
+
+def test_no_gpu_fails_loudly(native_lib):
+    if native_lib.kz_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    s = api.Scene()
+    s.add_mesh(np.eye(3, dtype=np.float32), [[0, 1, 2]])
+    s.set_materials([api.material([api.diffuse()])])
+    with pytest.raises(N.KazenError) as e:
+        s.build_bvh()
+    assert e.value.code == N.KZ_ERR_NO_DEVICE
+    with pytest.raises(N.KazenError) as e:
+        api.closure_eval([api.diffuse()], [[0, 1, 0]], [[0, 1, 0]])
+    assert e.value.code == N.KZ_ERR_NO_DEVICE
+
+
+def test_material_lowering_of_shipped_shaders():
+    # resource/scene/cbox/{diffuse,mirror,dielectric,rough,area}.osl as lowered records
+    diffuse = api.material([api.diffuse((0.5, 0.5, 0.5))])
+    mirror = api.material([api.mirror()])
+    diel = api.material([api.dielectric(1.5046, 1.000277)])
+    rough = api.material([api.diffuse((0.35, 0.35, 0.35)), api.microfacet("beckmann", 0.28, eta=1.5,
+                                                                         weight=(0.07, 0.07, 0.07))])
+    area = api.material([], Le=(1.0, 1.0, 1.0))
+    assert diffuse["lobes"][0]["closure_id"] == N.KZ_CLOSURE_DIFFUSE
+    assert mirror["lobes"][0]["closure_id"] == N.KZ_CLOSURE_KP_MIRROR
+    assert np.allclose(diel["lobes"][0]["params"][:2], [1.5046, 1.000277])
+    assert rough["n_lobes"] == 2 and rough["lobes"][1]["closure_id"] == N.KZ_CLOSURE_KP_GLOSS
+    assert rough["lobes"][1]["params"][0] == N.KZ_DIST_BECKMANN
+    assert area["n_lobes"] == 0 and area["Le"][0] == 1.0

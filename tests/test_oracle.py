@@ -1,0 +1,164 @@
+"""CPU tests of the restatement (oracle) against the reference's known answers
+and analytic identities. No GPU needed."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from kazen_proto_gb300 import api, scenes
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
+
+
+def test_pcg32_matches_published_vector(oracle_mod):
+    k = GOLD["pcg32"]
+    out = oracle_mod.pcg32(k["initstate"], k["initseq"], len(k["outputs"]))
+    assert [int(x) for x in out] == k["outputs"]
+
+
+@pytest.mark.parametrize("case", GOLD["furnace"], ids=lambda c: c["name"])
+def test_reference_furnace_tests(oracle_mod, case):
+    # tests/render_tests/microfacet_tests.cpp:8-21
+    if case["name"] == "fixed_beckmann":
+        v = oracle_mod.furnace_fixed_beckmann(case["alpha"], math.pi / 4)
+    elif case["name"] == "weak_beckmann":
+        v = oracle_mod.furnace_weak(1, case["theta_deg"], case["alpha"])
+    else:
+        v = oracle_mod.furnace_weak(0, case["theta_deg"], case["alpha"])
+    assert abs(v - case["expected"]) <= case["rel_tol"] * case["expected"]
+
+
+def test_embree_single_triangle(oracle_mod):
+    k = GOLD["embree_single_triangle"]
+    tv = np.array(k["verts"], np.float32).reshape(1, 9)
+    r = api.make_rays(k["ray_o"], k["ray_d"], tmin=k["tnear"], tmax=np.finfo(np.float32).max)
+    b = oracle_mod.Bvh(tv).closest(r)
+    assert b["prim"][0] == k["expect_prim"]
+    assert b["t"][0] == np.float32(1.0)
+    bf = oracle_mod.closest_brute(tv, r)
+    assert bf["prim"][0] == 0
+
+
+def _random_rays(rng, n, lo=-0.5, hi=1.5):
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    return api.make_rays(o, d)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_bvh_matches_brute_force(oracle_mod, seed):
+    rng = np.random.default_rng(seed)
+    tv = scenes.triangle_soup(3000, seed=seed + 10)
+    rays = _random_rays(rng, 4000)
+    a = oracle_mod.Bvh(tv).closest(rays, nthreads=4)
+    b = oracle_mod.closest_brute(tv, rays)
+    assert np.array_equal(a["prim"], b["prim"])
+    assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+    occ = oracle_mod.Bvh(tv).any(rays)
+    assert np.array_equal(occ, b["prim"] != 0xFFFFFFFF)
+
+
+def test_watertight_closed_mesh(oracle_mod):
+    # rays aimed exactly at shared vertices / edges of a closed icosphere must never miss
+    v, f = scenes.icosphere(2)
+    tv = v[f].reshape(-1, 9)
+    targets = np.concatenate([v, 0.5 * (v[f[:, 0]] + v[f[:, 1]])]).astype(np.float32)
+    o = np.zeros_like(targets)
+    rays = api.make_rays(o, targets)
+    b = oracle_mod.Bvh(tv).closest(rays)
+    assert (b["prim"] != 0xFFFFFFFF).all()
+
+
+def test_duplicate_triangles_tie_to_smaller_id(oracle_mod):
+    tri = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
+    tv = np.stack([tri, tri + np.float32(0), tri]).astype(np.float32)
+    tv[1] += np.array([0, 0, 5, 0, 0, 5, 0, 0, 5], np.float32)  # farther copy
+    rays = api.make_rays([[0.2, 0.2, -1.0]], [[0, 0, 1]])
+    b = oracle_mod.Bvh(tv).closest(rays)
+    assert b["prim"][0] == 0
+
+
+def _grid_dirs(rng, n, upper=True):
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    if upper:
+        d[:, 1] = np.abs(d[:, 1])
+    return d.astype(np.float32)
+
+
+@pytest.mark.parametrize("lobe_fn", [
+    lambda: api.diffuse((1, 1, 1)),
+    lambda: api.conductor_ggx((1, 1, 1), 0.3),
+    lambda: api.microfacet("ggx", 0.4, eta=1.0 / 1.5),
+    lambda: api.microfacet("beckmann", 0.4, eta=1.0 / 1.5),
+], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"])
+def test_sampling_matches_pdf(oracle_mod, lobe_fn):
+    """E[f*cos/pdf] by sampling equals the quadrature of f*cos (importance
+    sampling is consistent with the pdf the integrator divides by)."""
+    rng = np.random.default_rng(5)
+    wi = np.array([[math.sin(0.6), math.cos(0.6), 0.0]], np.float32)
+    n = 200000
+    lb = np.repeat(lobe_fn()[None], n)
+    u = rng.random((n, 3), dtype=np.float32)
+    wo, w, pdf, fl = oracle_mod.closure_sample(lb, np.repeat(wi, n, 0), u)
+    est = np.where((fl & 1)[:, None] > 0, w, 0).mean(0)
+    # quadrature of f*cos over the hemisphere (uniform directions / (1/2pi))
+    m = 400000
+    d = _grid_dirs(rng, m)
+    f, _ = oracle_mod.closure_eval(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), d, 1)
+    quad = f.mean(0) * 2 * math.pi
+    assert np.allclose(est, quad, rtol=0.03, atol=2e-3), (est, quad)
+
+
+@pytest.mark.parametrize("lobe_fn", [
+    lambda: api.diffuse((1, 1, 1)),
+    lambda: api.conductor_ggx((1, 1, 1), 0.3),
+    lambda: api.microfacet("ggx", 0.25, eta=1.0 / 1.5),
+    lambda: api.microfacet("beckmann", 0.25, eta=1.0 / 1.5),
+], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"])
+def test_integrator_pdf_normalised(oracle_mod, lobe_fn):
+    """The solid-angle pdf integrates, over the directions the sampler can
+    return, to the fraction of samples that are valid (microfacet samples that
+    reflect below the horizon are rejected; a diffuse lobe never rejects)."""
+    rng = np.random.default_rng(6)
+    wi = np.array([[math.sin(0.9), math.cos(0.9), 0.0]], np.float32)
+    m = 600000
+    d = _grid_dirs(rng, m)
+    _, pdf = oracle_mod.closure_eval(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), d, 1)
+    integral = pdf.mean() * 2 * math.pi
+    u = rng.random((m, 3), dtype=np.float32)
+    _, _, _, fl = oracle_mod.closure_sample(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), u)
+    valid = (fl & 1).mean()
+    assert abs(integral - valid) < 0.02, (integral, valid)
+    assert valid > 0.85
+
+
+def test_dielectric_energy_and_reciprocal_fresnel(oracle_mod):
+    rng = np.random.default_rng(7)
+    n = 1000
+    wi = _grid_dirs(rng, n)
+    lb = np.repeat(api.dielectric(1.5, 1.0)[None], n)
+    u = rng.random((n, 3), dtype=np.float32)
+    wo, w, pdf, fl = oracle_mod.closure_sample(lb, wi, u)
+    assert ((fl & 3) == 3).all()
+    assert np.allclose(np.linalg.norm(wo, axis=1), 1.0, atol=1e-5)
+    # refracted directions obey Snell's law: sin_t = sin_i / 1.5
+    refr = wo[:, 1] < 0
+    si = np.sqrt(np.maximum(0, 1 - wi[refr, 1] ** 2))
+    st = np.sqrt(np.maximum(0, 1 - wo[refr, 1] ** 2))
+    assert np.allclose(st, si / 1.5, atol=1e-5)
+
+
+def test_oracle_renders_box_scene(oracle_mod):
+    d = scenes.box_scene(32, 32, spp=4, max_depth=5)
+    sc = oracle_mod.Scene.from_desc(d)
+    c = d.camera
+    cam = oracle_mod.make_camera(c.eye, c.lookat, c.up, c.fov)
+    img, st = sc.render(cam, 32, 32, 4, 5, seed=1)
+    assert np.isfinite(img).all() and (img >= 0).all()
+    assert img.mean() > 0.05
+    assert st["path_bounces"] >= 32 * 32 * 4
+    # the light is visible from the camera: some pixel carries its radiance
+    assert img.max() > 3.0
