@@ -44,14 +44,18 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--small", action="store_true", help="reduced workload (quick checks only)")
+    p.add_argument("--profile", action="store_true",
+                   help="full-size scene, 640x360 frame at 4 spp, for ncu captures of single launches")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-traversal", action="store_true")
     return p.parse_args()
 
 
-def workload(small: bool):
-    if small:
+def workload(args):
+    if args.small:
         return dict(width=320, height=180, spp=8, max_depth=8, cells=256, n_spheres=64, wavefront=1 << 18)
+    if getattr(args, "profile", False):
+        return dict(width=640, height=360, spp=4, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
     return dict(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
 
 
@@ -190,7 +194,7 @@ def traversal_bench(steps, warmup):
     tv = scenes.triangle_soup(1 << 20, seed=1)
     rays = scenes.soup_rays(1 << 24, seed=2)
     s = scenes.soup_desc(tv).build()
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: handle 0 would mean "the library's own stream"
     s.set_stream(stream)
     dr = torch.from_numpy(rays.view(np.float32).reshape(-1, 8)).cuda()
     n = dr.shape[0]
@@ -231,12 +235,13 @@ def traversal_bench(steps, warmup):
 
 
 def load_traffic():
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per ray of k_trace_paths from the committed ncu summary."""
+    import re
+    path = os.path.join(ROOT, "profiles", "k_trace_paths_terrain_profile.md")
     if os.path.exists(path):
-        try:
-            return json.load(open(path))
-        except Exception:
-            return None
+        m = re.search(r"^dram_bytes_per_ray:\s*([0-9.]+)", open(path).read(), re.M)
+        if m:
+            return {"kernel": "k_trace_paths", "dram_bytes_per_ray": float(m.group(1))}
     return None
 
 
@@ -250,10 +255,10 @@ def run_ours(args):
     kbuild.build()
     dev_index = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev_index)
-    w = workload(args.small)
+    w = workload(args)
     desc = scenes.terrain_scene(w["width"], w["height"], w["spp"], w["max_depth"], w["cells"], w["n_spheres"])
     s = desc.build()
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: handle 0 would mean "the library's own stream"
     s.set_stream(stream)
     W, H = w["width"], w["height"]
     seed = 1000 * rank
@@ -261,14 +266,6 @@ def run_ours(args):
                      flags=N.KZ_RENDER_FLAG_TIMING)
     rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    # fetch counts for the roofline: one counted frame at reduced spp (untimed)
-    cnt = api.Renderer(spp=max(1, w["spp"] // 16), max_depth=w["max_depth"], seed=seed,
-                       wavefront_size=w["wavefront"], flags=N.KZ_RENDER_FLAG_COUNT)
-    cnt.render(s, desc.camera, W, H, device_out=(rgb, None))
-    cs = cnt.last_stats
-    nodes_per_ray = cs["closest_node_fetches"] / max(1, cs["path_bounces"])
-    tris_per_ray = cs["closest_tri_fetches"] / max(1, cs["path_bounces"])
 
     for _ in range(args.warmup):
         r.render(s, desc.camera, W, H, device_out=(rgb, None))
@@ -313,12 +310,21 @@ def run_ours(args):
         e2e_bounces += r.last_stats["path_bounces"]
     e_units, e_secs = aggregate(e2e_bounces, e2e_s, dist)
 
+    # fetch counts for the roofline: one counted frame at reduced spp (untimed,
+    # after the timed region so profiler launch indices are unaffected)
+    cnt = api.Renderer(spp=max(1, w["spp"] // 16), max_depth=w["max_depth"], seed=seed,
+                       wavefront_size=w["wavefront"], flags=N.KZ_RENDER_FLAG_COUNT)
+    cnt.render(s, desc.camera, W, H, device_out=(rgb, None))
+    cs = cnt.last_stats
+    nodes_per_ray = cs["closest_node_fetches"] / max(1, cs["path_bounces"])
+    tris_per_ray = cs["closest_tri_fetches"] / max(1, cs["path_bounces"])
+
     trav = None
-    if rank == 0 and not args.no_traversal and not args.small:
+    if rank == 0 and not args.no_traversal and not args.small and not args.profile:
         trav = traversal_bench(max(3, args.steps), max(3, args.warmup))
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
 
     if rank != 0:
@@ -373,7 +379,7 @@ def run_reference(args):
         return
     from kazen_proto_gb300 import scenes
     from oracle import oracle as O
-    w = workload(args.small)
+    w = workload(args)
     desc = scenes.terrain_scene(w["width"], w["height"], w["spp"], w["max_depth"], w["cells"], w["n_spheres"])
     sc = O.Scene.from_desc(desc)
     c = desc.camera

@@ -206,7 +206,8 @@ class Scene:
         return {k: getattr(inf, k) for k, _ in N.KzSceneInfo._fields_}
 
     def set_stream(self, stream) -> None:
-        """Run on an external CUDA stream (torch.cuda.Stream or raw handle); None = own stream."""
+        """Run on an external CUDA stream (torch.cuda.Stream or raw handle). None, or a
+        handle of 0 (torch's legacy default stream), selects the library's own stream."""
         raw = None
         if stream is not None:
             raw = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
