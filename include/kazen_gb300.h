@@ -256,6 +256,34 @@ kz_status kz_render(kz_scene* scene, const kz_camera* camera,
                     float* out_rgb, double* out_rgb64, int32_t mem,
                     kz_render_stats* out_stats);
 
+/* ---- Li batch that allocates nothing -------------------------------------
+ * No counterpart in the reference: kazen_proto has no device path of its own.
+ * Same result as kz_li_batch with KZ_MEM_DEVICE, for callers that cannot call
+ * cudaMalloc while they render: a host application or framework that owns
+ * the GPU's memory budget through its own allocator, or a latency-critical
+ * loop that cannot afford cudaMalloc's implicit device synchronisation. The
+ * wavefront scratch (path state and shadow-ray queue) lives in one static
+ * device array of the library, about 3 MiB, that every GPU which loads the
+ * library holds until the process exits; the call itself makes no
+ * cudaMalloc, cudaFree or other allocating call.
+ *   - rays and out_rgb are device pointers on the scene's device; the scene
+ *     must be built (kz_scene_build allocates the scene, as before).
+ *   - cfg->wavefront_size = 0 selects KZ_LI_NOALLOC_MAX_WAVEFRONT paths in
+ *     flight; a larger value fails with KZ_ERR_INVALID_ARG. n itself may be
+ *     up to 2^32-1: paths stream through the fixed wavefront.
+ *   - The first call on a device looks up the array's device address (once
+ *     per device, with that device current); make that first call before any
+ *     stream capture.
+ *   - All calls share the one array and its previous contents (the counters
+ *     are cleared on every call): calls that overlap on the GPU — from two
+ *     threads, or on two scenes' streams — race and corrupt each other.
+ *   - KZ_RENDER_FLAG_TIMING is ignored (stage times stay 0); the call
+ *     returns after the work has finished on the scene stream. */
+#define KZ_LI_NOALLOC_MAX_WAVEFRONT 16384u
+kz_status kz_li_batch_noalloc(kz_scene* scene, const kz_ray* rays, uint64_t n,
+                              const kz_render_config* cfg, float* out_rgb,
+                              kz_render_stats* out_stats);
+
 #ifdef __cplusplus
 }
 #endif

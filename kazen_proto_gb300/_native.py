@@ -126,7 +126,10 @@ SIGNATURES = {
                                 C.POINTER(KzRenderStats)]),
     "kz_render": (C.c_int32, [_P, C.POINTER(KzCamera), C.POINTER(KzFilmDesc), C.POINTER(KzRenderConfig), _P, _P,
                               C.c_int32, C.POINTER(KzRenderStats)]),
+    "kz_li_batch_noalloc": (C.c_int32, [_P, _P, C.c_uint64, C.POINTER(KzRenderConfig), _P,
+                                        C.POINTER(KzRenderStats)]),
 }
+KZ_LI_NOALLOC_MAX_WAVEFRONT = 16384
 
 
 class KazenError(RuntimeError):

@@ -860,3 +860,133 @@ kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// kz_li_batch_noalloc: the wavefront Li batch with its scratch in a static
+// device array instead of cudaMalloc'd buffers. Layout of the array for a
+// capacity of C paths: ping-pong path state A and B (four float4 arrays and
+// one 64-bit RNG array each), the shadow queue (three float4 arrays), then the
+// device counters. Every region starts on a 256-byte boundary.
+namespace {
+
+constexpr size_t kNoAllocCap = KZ_LI_NOALLOC_MAX_WAVEFRONT;
+constexpr size_t kNoAllocPathBytes = kNoAllocCap * (4 * sizeof(float4) + sizeof(unsigned long long));
+constexpr size_t kNoAllocShadowBytes = kNoAllocCap * 3 * sizeof(float4);
+constexpr size_t kNoAllocCounterOffset = 2 * kNoAllocPathBytes + kNoAllocShadowBytes;
+constexpr size_t kNoAllocBytes = kNoAllocCounterOffset + ((sizeof(kz::DevCounters) + 255) / 256) * 256;
+static_assert(kNoAllocCap % 64 == 0, "regions must stay 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device` (which must be current):
+// looked up on the first call per device and cached. In host code the symbol
+// is only a host-side stand-in, never a device address.
+kz_status noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return fail(KZ_ERR_INVALID_ARG, "device %d is beyond the %d devices the scratch table covers", device,
+                    kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(KZ_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        g_noalloc_addr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+    return KZ_OK;
+}
+
+kz::PathSoA carve_paths(unsigned char* base) {
+    kz::PathSoA p;
+    p.o4 = reinterpret_cast<float4*>(base);
+    p.d4 = p.o4 + kNoAllocCap;
+    p.b4 = p.d4 + kNoAllocCap;
+    p.hit = p.b4 + kNoAllocCap;
+    p.rng = reinterpret_cast<unsigned long long*>(p.hit + kNoAllocCap);
+    return p;
+}
+
+}  // namespace
+
+extern "C" kz_status kz_li_batch_noalloc(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_render_config* cfg,
+                                         float* out_rgb, kz_render_stats* out_stats) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_scene(s));
+    KZ_TRY(check_cfg(cfg));
+    if (cfg->wavefront_size > KZ_LI_NOALLOC_MAX_WAVEFRONT)
+        return fail(KZ_ERR_INVALID_ARG, "wavefront_size %u exceeds the no-allocation maximum of %u paths",
+                    cfg->wavefront_size, KZ_LI_NOALLOC_MAX_WAVEFRONT);
+    if (cfg->block_size && (cfg->block_size % 32 != 0 || cfg->block_size > 1024))
+        return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
+    if (n > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "at most 2^32-1 rays per call");
+    if (out_stats) *out_stats = kz_render_stats{};
+    if (n == 0) return KZ_OK;
+    if (!rays || !out_rgb) return fail(KZ_ERR_INVALID_ARG, "rays and out_rgb are required");
+
+    unsigned char* base = nullptr;
+    KZ_TRY(noalloc_scratch(s->device, &base));
+    kz::PathSoA A = carve_paths(base);
+    kz::PathSoA B = carve_paths(base + kNoAllocPathBytes);
+    float4* sh = reinterpret_cast<float4*>(base + 2 * kNoAllocPathBytes);
+    kz::ShadowSoA sq{sh, sh + kNoAllocCap, sh + 2 * kNoAllocCap};
+    kz::DevCounters* ctr = reinterpret_cast<kz::DevCounters*>(base + kNoAllocCounterOffset);
+
+    kz::PathParams pp;
+    pp.spp = 1;
+    pp.max_depth = cfg->max_depth;
+    pp.rr_min = cfg->rr_min_depth;
+    pp.seed = cfg->seed;
+    pp.camera = 0;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(cfg->wavefront_size ? cfg->wavefront_size : kNoAllocCap, n);
+    const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
+    const bool count = (cfg->flags & KZ_RENDER_FLAG_COUNT) != 0;
+    cudaStream_t strm = s->stream;
+
+    // the array keeps the previous call's contents: clear the counters and
+    // the output this call accumulates into
+    KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), strm));
+    KZ_CUDA(cudaMemsetAsync(out_rgb, 0, n * 3 * sizeof(float), strm));
+    kz_render_stats st{};
+    st.paths = n;
+    kz::DevCounters hc;
+    uint64_t next = 0;
+    uint32_t nA = 0;
+    for (;;) {
+        const uint32_t n_new = (uint32_t)std::min<uint64_t>(cap - nA, n - next);
+        if (n_new) {
+            kz::launch_generate_rays(rays, pp, A, nA, next, n_new, block, strm);
+            st.kernel_launches += 1;
+            nA += n_new;
+            next += n_new;
+        }
+        if (nA == 0) break;
+        kz::launch_trace_paths(s->dev, A, nA, ctr, count, block, strm);
+        KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
+        kz::launch_shade(s->dev, pp, A, nA, B, sq, ctr, out_rgb, nullptr, block, strm);
+        kz::launch_trace_shadow(s->dev, sq, nA, ctr, count, out_rgb, nullptr, block, strm);
+        st.kernel_launches += 3;
+        KZ_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, strm));
+        KZ_CUDA(cudaStreamSynchronize(strm));
+        KZ_CUDA(cudaGetLastError());
+        st.path_bounces += nA;
+        st.shadow_rays += hc.n_shadow;
+        st.iterations += 1;
+        if (hc.status) return fail((kz_status)hc.status, "device status %u during Li batch", hc.status);
+        nA = hc.n_next;
+        std::swap(A, B);
+    }
+    if (count) {
+        st.closest_node_fetches = hc.fetch[0];
+        st.closest_tri_fetches = hc.fetch[1];
+        st.shadow_node_fetches = hc.fetch[2];
+        st.shadow_tri_fetches = hc.fetch[3];
+    }
+    if (out_stats) *out_stats = st;
+    return KZ_OK;
+}
