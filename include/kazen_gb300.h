@@ -256,6 +256,59 @@ kz_status kz_render(kz_scene* scene, const kz_camera* camera,
                     float* out_rgb, double* out_rgb64, int32_t mem,
                     kz_render_stats* out_stats);
 
+/* ---- learned path guiding -------------------------------------------------
+ * Not in the reference (kazen_proto has no guiding). A small network trained
+ * online on the radiance samples the tracer produces maps a shading point
+ * (position in the scene box, 8-band sin/cos encoding, plus the geometric
+ * normal: 51 inputs) through 3 hidden layers of 64 ReLU units to an 8-lobe
+ * von Mises-Fisher mixture over incident directions (mean 3, concentration
+ * 1, weight 1 per lobe: 40 outputs). BF16 weights, FP32 accumulation, Adam.
+ * The renderer samples it with probability alpha and the BSDF otherwise and
+ * weighs with the one-sample MIS pdf, so every image is unbiased whatever
+ * the network has learned. */
+typedef struct kz_guide kz_guide;
+
+typedef struct kz_guide_config {
+    float    alpha;             /* probability of sampling the network (0 = 0.5) */
+    float    learning_rate;     /* Adam step size (0 = 1e-3)                     */
+    uint32_t spp_per_pass;      /* spp rendered between training steps (0 = 1)   */
+    uint32_t train;             /* 1: train after every pass, 0: frozen network  */
+    uint32_t max_train_samples; /* samples per Adam step (0 = 2^18)               */
+    uint32_t steps_per_pass;    /* Adam steps after each pass (0 = 1)            */
+    double   time_budget_ms;    /* > 0: stop after the pass that reaches it       */
+} kz_guide_config;
+
+typedef struct kz_guide_stats {
+    uint64_t passes;
+    uint64_t spp_done;          /* the image is the average of this many spp     */
+    uint64_t train_steps;
+    uint64_t train_samples;     /* radiance samples collected                    */
+    double   last_loss;         /* weighted -log q of the last step              */
+    double   wall_ms;           /* whole call                                    */
+    double   train_ms;          /* collection + training (host wall clock)       */
+} kz_guide_stats;
+
+#define KZ_GUIDE_PARAMS 15080   /* FP32 parameters: W1..W4 [out][64], b1..b4 */
+
+kz_status kz_guide_create(kz_guide** out_guide, uint64_t seed);
+kz_status kz_guide_destroy(kz_guide* guide);
+kz_status kz_guide_get_params(kz_guide* guide, float* out_params /* KZ_GUIDE_PARAMS, host */);
+kz_status kz_guide_set_params(kz_guide* guide, const float* params /* KZ_GUIDE_PARAMS, host */);
+/* points: n * 8 floats (p01.xyz, -, n.xyz, -); out_raw: n * 40 network outputs. */
+kz_status kz_guide_forward(kz_guide* guide, const float* points, uint64_t n, float* out_raw, int32_t mem);
+/* samples: n * 12 floats ((p01.xyz, weight), (n.xyz, -), (dir.xyz, -)).
+ * Loss = mean over samples of weight * -log q(dir). Writes the loss, the
+ * gradient (optional, KZ_GUIDE_PARAMS floats, host) and, when apply != 0,
+ * takes one Adam step. n <= 2^20. */
+kz_status kz_guide_train_step(kz_guide* guide, const float* samples, uint64_t n, float learning_rate,
+                              int32_t apply, float* out_loss, float* out_grad, int32_t mem);
+/* Guided render (same film contract as kz_render). cfg->spp is the target;
+ * gcfg->time_budget_ms may stop it earlier (gstats->spp_done says where). */
+kz_status kz_render_guided(kz_scene* scene, kz_guide* guide, const kz_camera* camera,
+                           const kz_film_desc* film, const kz_render_config* cfg,
+                           const kz_guide_config* gcfg, float* out_rgb, double* out_rgb64,
+                           int32_t mem, kz_render_stats* out_stats, kz_guide_stats* out_gstats);
+
 /* ---- Li batch that allocates nothing -------------------------------------
  * No counterpart in the reference: kazen_proto has no device path of its own.
  * Same result as kz_li_batch with KZ_MEM_DEVICE, for callers that cannot call

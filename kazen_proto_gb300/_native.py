@@ -87,6 +87,21 @@ class KzRenderStats(C.Structure):
                 ("shadow_ms", C.c_double)]
 
 
+class KzGuideConfig(C.Structure):
+    _fields_ = [("alpha", C.c_float), ("learning_rate", C.c_float), ("spp_per_pass", C.c_uint32),
+                ("train", C.c_uint32), ("max_train_samples", C.c_uint32), ("steps_per_pass", C.c_uint32),
+                ("time_budget_ms", C.c_double)]
+
+
+class KzGuideStats(C.Structure):
+    _fields_ = [("passes", C.c_uint64), ("spp_done", C.c_uint64), ("train_steps", C.c_uint64),
+                ("train_samples", C.c_uint64), ("last_loss", C.c_double), ("wall_ms", C.c_double),
+                ("train_ms", C.c_double)]
+
+
+KZ_GUIDE_PARAMS = 15080
+
+
 class KzSceneInfo(C.Structure):
     _fields_ = [("n_meshes", C.c_uint64), ("n_triangles", C.c_uint64), ("n_lights", C.c_uint64),
                 ("n_bvh_nodes", C.c_uint64), ("bvh_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64),
@@ -128,6 +143,16 @@ SIGNATURES = {
                               C.c_int32, C.POINTER(KzRenderStats)]),
     "kz_li_batch_noalloc": (C.c_int32, [_P, _P, C.c_uint64, C.POINTER(KzRenderConfig), _P,
                                         C.POINTER(KzRenderStats)]),
+    "kz_guide_create": (C.c_int32, [C.POINTER(C.c_void_p), C.c_uint64]),
+    "kz_guide_destroy": (C.c_int32, [_P]),
+    "kz_guide_get_params": (C.c_int32, [_P, _P]),
+    "kz_guide_set_params": (C.c_int32, [_P, _P]),
+    "kz_guide_forward": (C.c_int32, [_P, _P, C.c_uint64, _P, C.c_int32]),
+    "kz_guide_train_step": (C.c_int32, [_P, _P, C.c_uint64, C.c_float, C.c_int32, C.POINTER(C.c_float), _P,
+                                        C.c_int32]),
+    "kz_render_guided": (C.c_int32, [_P, _P, C.POINTER(KzCamera), C.POINTER(KzFilmDesc), C.POINTER(KzRenderConfig),
+                                     C.POINTER(KzGuideConfig), _P, _P, C.c_int32, C.POINTER(KzRenderStats),
+                                     C.POINTER(KzGuideStats)]),
 }
 KZ_LI_NOALLOC_MAX_WAVEFRONT = 16384
 

@@ -353,3 +353,93 @@ def closure_sample(lobes, wi, u):
     check(lib().kz_closure_sample_batch(_ptr(lb), _ptr(a), _ptr(uu), n, _ptr(wo), _ptr(w), _ptr(pdf), _ptr(fl),
                                         N.KZ_MEM_HOST))
     return wo, w, pdf, fl
+
+
+# ---------------------------------------------------------------- learned path guiding
+class Guide:
+    """The guiding network (51 -> 64 -> 64 -> 64 -> 40, 8 vMF lobes) on the GPU."""
+
+    n_params = N.KZ_GUIDE_PARAMS
+
+    def __init__(self, seed=1):
+        h = C.c_void_p()
+        check(lib().kz_guide_create(C.byref(h), seed))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().kz_guide_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.empty(N.KZ_GUIDE_PARAMS, np.float32)
+        check(lib().kz_guide_get_params(self._h, _ptr(out)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == N.KZ_GUIDE_PARAMS
+        check(lib().kz_guide_set_params(self._h, _ptr(p)))
+
+    def forward(self, p01, nrm) -> np.ndarray:
+        """Raw network outputs (n, 40) for points in the unit scene box with normals."""
+        p01 = np.asarray(p01, np.float32).reshape(-1, 3)
+        nrm = np.asarray(nrm, np.float32).reshape(-1, 3)
+        pts = np.zeros((len(p01), 8), np.float32)
+        pts[:, 0:3] = p01
+        pts[:, 4:7] = nrm
+        out = np.empty((len(p01), 40), np.float32)
+        check(lib().kz_guide_forward(self._h, _ptr(pts), len(p01), _ptr(out), N.KZ_MEM_HOST))
+        return out
+
+    def train_step(self, p01, nrm, dirs, weights, lr=1e-3, apply=True, want_grad=False):
+        n = len(p01)
+        smp = np.zeros((n, 12), np.float32)
+        smp[:, 0:3] = p01
+        smp[:, 3] = weights
+        smp[:, 4:7] = nrm
+        smp[:, 8:11] = dirs
+        loss = C.c_float()
+        grad = np.empty(N.KZ_GUIDE_PARAMS, np.float32) if want_grad else None
+        check(lib().kz_guide_train_step(self._h, _ptr(smp), n, lr, 1 if apply else 0, C.byref(loss), _ptr(grad),
+                                        N.KZ_MEM_HOST))
+        return (loss.value, grad) if want_grad else loss.value
+
+
+def guide_config(alpha=0.5, learning_rate=1e-3, spp_per_pass=1, train=True, max_train_samples=1 << 18,
+                 steps_per_pass=1, time_budget_ms=0.0) -> N.KzGuideConfig:
+    c = N.KzGuideConfig()
+    c.alpha = alpha
+    c.learning_rate = learning_rate
+    c.spp_per_pass = spp_per_pass
+    c.train = 1 if train else 0
+    c.max_train_samples = max_train_samples
+    c.steps_per_pass = steps_per_pass
+    c.time_budget_ms = time_budget_ms
+    return c
+
+
+def render_guided(scene: Scene, guide: Guide, camera: Camera, width: int, height: int, spp: int, max_depth: int,
+                  seed=0, gcfg=None, fp64=False, wavefront_size=0):
+    """Guided render; returns (image, fp64 image or None, render stats, guide stats)."""
+    cfg = render_config(spp, max_depth, seed, wavefront_size)
+    gcfg = gcfg or guide_config()
+    film = N.KzFilmDesc(width, height)
+    cam = camera.to_c()
+    st, gst = N.KzRenderStats(), N.KzGuideStats()
+    img = np.empty((height, width, 3), np.float32)
+    img64 = np.empty((height, width, 3), np.float64) if fp64 else None
+    check(lib().kz_render_guided(scene.handle, guide.handle, C.byref(cam), C.byref(film), C.byref(cfg), C.byref(gcfg),
+                                 _ptr(img), _ptr(img64), N.KZ_MEM_HOST, C.byref(st), C.byref(gst)))
+    return (img, img64, {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_},
+            {k: getattr(gst, k) for k, _ in N.KzGuideStats._fields_})

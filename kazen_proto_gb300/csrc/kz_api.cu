@@ -1,6 +1,7 @@
 // kz_api.cu — the C ABI of include/kazen_gb300.h: scene management, host
 // validation, device memory, and the wavefront render loop driver.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -545,6 +546,21 @@ kz_status kz_scene_build(kz_scene* s) {
     KZ_CUDA(cudaStreamSynchronize(st));
 
     kz::DevScene& d = s->dev;
+    {
+        float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {1.f, 1.f, 1.f};
+        if (total) {
+            for (int a = 0; a < 3; ++a) lo[a] = hi[a] = tv[a];
+            for (size_t k = 0; k < tv.size(); k += 3)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], tv[k + a]);
+                    hi[a] = std::max(hi[a], tv[k + a]);
+                }
+        }
+        float inv[3];
+        for (int a = 0; a < 3; ++a) inv[a] = hi[a] > lo[a] ? 1.f / (hi[a] - lo[a]) : 1.f;
+        d.box_lo = make_float3(lo[0], lo[1], lo[2]);
+        d.box_inv = make_float3(inv[0], inv[1], inv[2]);
+    }
     d.nodes = s->nodes.as<float4>();
     d.tris = s->tris.as<float4>();
     d.n_nodes = out.n_nodes;
@@ -856,6 +872,382 @@ kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd
         if (out_rgb64) KZ_CUDA(cudaMemcpyAsync(out_rgb64, film64, npix * 24, cudaMemcpyDeviceToHost, st));
     }
     KZ_CUDA(cudaStreamSynchronize(st));
+    return KZ_OK;
+}
+
+}  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// Learned path guiding: the network object and the guided render loop.
+struct kz_guide {
+    std::mutex mu;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf w, m, v, grad, wbf, loss;  // parameters (FP32, BF16), Adam moments, gradient
+    DevBuf train_rec, samples, raw, recs, pts, ctr;
+    int step = 0;
+    ~kz_guide() {
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        DevBuf* all[] = {&w, &m, &v, &grad, &wbf, &loss, &train_rec, &samples, &raw, &recs, &pts, &ctr};
+        for (DevBuf* b : all) b->release();
+        if (stream) cudaStreamDestroy(stream);
+    }
+    kz::GuideDev dev(const kz::DevScene* sc) const {
+        kz::GuideDev g;
+        g.wbf = static_cast<const __nv_bfloat16*>(wbf.ptr);
+        g.wf = w.as<float>();
+        if (sc) {
+            g.box_lo = sc->box_lo;
+            g.box_inv = sc->box_inv;
+        }
+        return g;
+    }
+};
+
+namespace {
+
+// He-uniform initial weights from a PCG32 stream (host), biases 0; the
+// padded inputs of layer 1 stay zero.
+void guide_init_params(uint64_t seed, std::vector<float>& p) {
+    p.assign(KZ_GUIDE_PARAMS, 0.f);
+    uint64_t state = 0, inc = (seed << 1u) | 1u;
+    auto next = [&]() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u), rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    };
+    next();
+    state += 0x853c49e6748fea9bULL;
+    next();
+    const int offs[4] = {0, 64 * 64 + 64, 2 * (64 * 64 + 64), 3 * (64 * 64 + 64)};
+    const int rows[4] = {64, 64, 64, 40};
+    const int fan_in[4] = {51, 64, 64, 64};
+    for (int l = 0; l < 4; ++l) {
+        const float bound = (l < 3 ? std::sqrt(6.f / (float)fan_in[l]) : 0.5f * std::sqrt(3.f / (float)fan_in[l]));
+        for (int o = 0; o < rows[l]; ++o)
+            for (int i = 0; i < 64; ++i) {
+                const float u = (float)(next() >> 8) * (1.0f / 16777216.0f);
+                p[(size_t)offs[l] + o * 64 + i] = i < fan_in[l] ? (2.f * u - 1.f) * bound : 0.f;
+            }
+    }
+}
+
+kz_status guide_upload_params(kz_guide* g, const float* host) {
+    KZ_CUDA(cudaMemcpyAsync(g->w.ptr, host, KZ_GUIDE_PARAMS * 4, cudaMemcpyHostToDevice, g->stream));
+    kz::launch_guide_to_bf16(g->w.as<float>(), static_cast<__nv_bfloat16*>(g->wbf.ptr), g->stream);
+    KZ_CUDA(cudaGetLastError());
+    KZ_CUDA(cudaMemsetAsync(g->m.ptr, 0, KZ_GUIDE_PARAMS * 4, g->stream));
+    KZ_CUDA(cudaMemsetAsync(g->v.ptr, 0, KZ_GUIDE_PARAMS * 4, g->stream));
+    g->step = 0;
+    KZ_CUDA(cudaStreamSynchronize(g->stream));
+    return KZ_OK;
+}
+
+// One training batch on device samples: gradient into g->grad (zeroed
+// first), loss into g->loss; Adam when apply.
+kz_status guide_train_device(kz_guide* g, const float4* samples, uint32_t count, uint32_t rows, uint32_t stride,
+                             uint32_t offset, float wscale, float lr, bool apply, const kz::DevScene* sc,
+                             cudaStream_t st) {
+    KZ_TRY(g->train_rec.ensure((size_t)rows * 496 * 2));
+    KZ_CUDA(cudaMemsetAsync(g->grad.ptr, 0, KZ_GUIDE_PARAMS * 4, st));
+    KZ_CUDA(cudaMemsetAsync(g->loss.ptr, 0, 4, st));
+    kz::launch_guide_train(samples, count, rows, stride, offset, wscale, g->dev(sc),
+                           static_cast<__nv_bfloat16*>(g->train_rec.ptr), g->grad.as<float>(), g->loss.as<float>(), st);
+    KZ_CUDA(cudaGetLastError());
+    if (apply) {
+        g->step += 1;
+        kz::launch_guide_adam(g->w.as<float>(), g->m.as<float>(), g->v.as<float>(), g->grad.as<float>(),
+                              static_cast<__nv_bfloat16*>(g->wbf.ptr), lr, g->step, st);
+        KZ_CUDA(cudaGetLastError());
+    }
+    return KZ_OK;
+}
+
+uint64_t gcd64(uint64_t a, uint64_t b) {
+    while (b) {
+        uint64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+kz_status kz_guide_create(kz_guide** out, uint64_t seed) {
+    if (!out) return fail(KZ_ERR_INVALID_ARG, "out_guide is NULL");
+    *out = nullptr;
+    if (kz_device_count() == 0) return fail(KZ_ERR_NO_DEVICE, "no CUDA device is visible");
+    kz_guide* g = new kz_guide();
+    auto bail = [&](kz_status st) {
+        delete g;
+        return st;
+    };
+    if (cudaGetDevice(&g->device) != cudaSuccess) return bail(fail(KZ_ERR_CUDA, "cudaGetDevice failed"));
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(KZ_ERR_CUDA, "cudaStreamCreate failed"));
+    cudaError_t e = kz::guide_kernel_setup();
+    if (e != cudaSuccess) return bail(fail(KZ_ERR_CUDA, "guide kernel setup: %s", cudaGetErrorString(e)));
+    kz_status st = KZ_OK;
+    for (DevBuf* b : {&g->w, &g->m, &g->v, &g->grad})
+        if (st == KZ_OK) st = b->ensure(KZ_GUIDE_PARAMS * 4);
+    if (st == KZ_OK) st = g->wbf.ensure(KZ_GUIDE_PARAMS * 2);
+    if (st == KZ_OK) st = g->loss.ensure(16);
+    if (st == KZ_OK) st = g->ctr.ensure(16);
+    if (st != KZ_OK) return bail(st);
+    std::vector<float> p;
+    guide_init_params(seed, p);
+    st = guide_upload_params(g, p.data());
+    if (st != KZ_OK) return bail(st);
+    *out = g;
+    return KZ_OK;
+}
+
+kz_status kz_guide_destroy(kz_guide* g) {
+    delete g;
+    return KZ_OK;
+}
+
+kz_status kz_guide_get_params(kz_guide* g, float* out) {
+    if (!g || !out) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    KZ_CUDA(cudaMemcpyAsync(out, g->w.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, g->stream));
+    KZ_CUDA(cudaStreamSynchronize(g->stream));
+    return KZ_OK;
+}
+
+kz_status kz_guide_set_params(kz_guide* g, const float* in) {
+    if (!g || !in) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    for (int i = 0; i < KZ_GUIDE_PARAMS; ++i)
+        if (!std::isfinite(in[i])) return fail(KZ_ERR_INVALID_ARG, "parameter %d is not finite", i);
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    return guide_upload_params(g, in);
+}
+
+kz_status kz_guide_forward(kz_guide* g, const float* points, uint64_t n, float* out_raw, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (!g) return fail(KZ_ERR_INVALID_ARG, "guide is NULL");
+    if (n == 0) return KZ_OK;
+    if (!points || !out_raw) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    if (n > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "too many points");
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    cudaStream_t st = g->stream;
+    const float4* dp = reinterpret_cast<const float4*>(points);
+    float* dr = out_raw;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(g->pts.ensure(n * 32));
+        KZ_TRY(g->raw.ensure(n * 160));
+        KZ_CUDA(cudaMemcpyAsync(g->pts.ptr, points, n * 32, cudaMemcpyHostToDevice, st));
+        dp = g->pts.as<float4>();
+        dr = g->raw.as<float>();
+    }
+    kz::launch_guide_infer_points(dp, (uint32_t)n, g->dev(nullptr), dr, st);
+    KZ_CUDA(cudaGetLastError());
+    if (mem == KZ_MEM_HOST) KZ_CUDA(cudaMemcpyAsync(out_raw, dr, n * 160, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    return KZ_OK;
+}
+
+kz_status kz_guide_train_step(kz_guide* g, const float* samples, uint64_t n, float lr, int32_t apply,
+                              float* out_loss, float* out_grad, int32_t mem) {
+    KZ_TRY(check_mem(mem));
+    if (!g) return fail(KZ_ERR_INVALID_ARG, "guide is NULL");
+    if (n == 0 || n > (1u << 20)) return fail(KZ_ERR_INVALID_ARG, "n must be in [1, 2^20]");
+    if (!samples) return fail(KZ_ERR_INVALID_ARG, "samples is NULL");
+    if (!(lr > 0.f) && apply) return fail(KZ_ERR_INVALID_ARG, "learning_rate must be > 0");
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    cudaStream_t st = g->stream;
+    const float4* ds = reinterpret_cast<const float4*>(samples);
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(g->samples.ensure(n * 48));
+        KZ_CUDA(cudaMemcpyAsync(g->samples.ptr, samples, n * 48, cudaMemcpyHostToDevice, st));
+        ds = g->samples.as<float4>();
+    }
+    KZ_TRY(guide_train_device(g, ds, (uint32_t)n, (uint32_t)n, 1, 0, 1.0f / (float)n, lr, apply != 0, nullptr, st));
+    float loss = 0.f;
+    KZ_CUDA(cudaMemcpyAsync(&loss, g->loss.ptr, 4, cudaMemcpyDeviceToHost, st));
+    if (out_grad) KZ_CUDA(cudaMemcpyAsync(out_grad, g->grad.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    if (out_loss) *out_loss = loss;
+    return KZ_OK;
+}
+
+kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, const kz_film_desc* fd,
+                           const kz_render_config* cfg, const kz_guide_config* gcfg_in, float* out_rgb,
+                           double* out_rgb64, int32_t mem, kz_render_stats* out_stats, kz_guide_stats* out_gstats) {
+    const auto t_start = std::chrono::steady_clock::now();
+    KZ_TRY(check_mem(mem));
+    if (!s || !g) return fail(KZ_ERR_INVALID_ARG, "scene and guide are required");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::lock_guard<std::mutex> lk2(g->mu);
+    KZ_TRY(check_scene(s));
+    KZ_TRY(check_cfg(cfg));
+    if (cfg->max_depth > 16) return fail(KZ_ERR_INVALID_ARG, "guided rendering supports max_depth <= 16");
+    if (g->device != s->device) return fail(KZ_ERR_INVALID_ARG, "guide and scene live on different devices");
+    if (!camera || !fd || !out_rgb) return fail(KZ_ERR_INVALID_ARG, "camera, film and out_rgb are required");
+    if (fd->width == 0 || fd->height == 0) return fail(KZ_ERR_INVALID_ARG, "film size must be > 0");
+    kz_guide_config gc = gcfg_in ? *gcfg_in : kz_guide_config{};
+    if (gc.alpha == 0.f) gc.alpha = 0.5f;
+    if (!(gc.alpha > 0.f && gc.alpha < 1.f)) return fail(KZ_ERR_INVALID_ARG, "alpha must be in (0, 1)");
+    if (gc.learning_rate == 0.f) gc.learning_rate = 1e-3f;
+    if (gc.spp_per_pass == 0) gc.spp_per_pass = 1;
+    if (gc.max_train_samples == 0) gc.max_train_samples = 1u << 18;
+    if (gc.steps_per_pass == 0) gc.steps_per_pass = 1;
+    const uint64_t npix = (uint64_t)fd->width * fd->height;
+    const uint64_t per_pass = npix * gc.spp_per_pass;
+    if (per_pass > (1ull << 28)) return fail(KZ_ERR_INVALID_ARG, "width*height*spp_per_pass must be <= 2^28");
+    kz::DevCamera cam;
+    KZ_TRY(make_camera(camera, fd->width, fd->height, cam));
+    cudaStream_t strm = s->stream;
+
+    // buffers
+    float* film = out_rgb;
+    double* film64 = out_rgb64;
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(s->film.ensure(npix * 12));
+        film = s->film.as<float>();
+        if (out_rgb64) {
+            KZ_TRY(s->film64.ensure(npix * 24));
+            film64 = s->film64.as<double>();
+        }
+    }
+    KZ_CUDA(cudaMemsetAsync(film, 0, npix * 12, strm));
+    if (film64) KZ_CUDA(cudaMemsetAsync(film64, 0, npix * 24, strm));
+    const uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
+    const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, per_pass));
+    const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
+    if (block % 32 != 0 || block > 1024) return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
+    kz::PathSoA A, B;
+    KZ_TRY(alloc_paths(s->pa, cap, A));
+    KZ_TRY(alloc_paths(s->pb, cap, B));
+    for (int k = 0; k < 3; ++k) KZ_TRY(s->sh[k].ensure((size_t)cap * sizeof(float4)));
+    kz::ShadowSoA sq{s->sh[0].as<float4>(), s->sh[1].as<float4>(), s->sh[2].as<float4>()};
+    KZ_TRY(s->ctr.ensure(sizeof(kz::DevCounters)));
+    kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
+    const uint64_t n_recs = per_pass * cfg->max_depth;
+    KZ_TRY(g->recs.ensure(n_recs * sizeof(kz::VRec)));
+    KZ_TRY(g->samples.ensure(n_recs * 48));
+    KZ_TRY(g->raw.ensure((size_t)cap * 160));
+    kz::VRec* recs = g->recs.as<kz::VRec>();
+    const kz::GuideDev gdev = g->dev(&s->dev);
+
+    kz_render_stats st{};
+    kz_guide_stats gs{};
+    double train_ms = 0.0;
+    uint64_t spp_done = 0;
+    uint32_t pass = 0;
+    while (spp_done < cfg->spp) {
+        const uint32_t spp_pass = (uint32_t)std::min<uint64_t>(gc.spp_per_pass, cfg->spp - spp_done);
+        const uint64_t total = npix * spp_pass;
+        kz::PathParams pp;
+        pp.spp = spp_pass;
+        pp.max_depth = cfg->max_depth;
+        pp.rr_min = cfg->rr_min_depth;
+        pp.seed = cfg->seed * 0x9E3779B97F4A7C15ull + pass + 1;  // a fresh PCG32 seed per pass
+        pp.camera = 1;
+        KZ_CUDA(cudaMemsetAsync(recs, 0, total * cfg->max_depth * sizeof(kz::VRec), strm));
+        KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), strm));
+        kz::GuideShade gsh;
+        gsh.raw = g->raw.as<float>();
+        gsh.recs = recs;
+        gsh.pass_first = 0;
+        gsh.alpha = gc.alpha;
+        uint64_t next = 0;
+        uint32_t nA = 0;
+        for (;;) {
+            const uint32_t n_new = (uint32_t)std::min<uint64_t>(cap - nA, total - next);
+            if (n_new) {
+                kz::launch_generate_camera(cam, pp, A, nA, next, n_new, block, strm);
+                st.kernel_launches += 1;
+                nA += n_new;
+                next += n_new;
+            }
+            if (nA == 0) break;
+            kz::launch_trace_paths(s->dev, A, nA, ctr, false, block, strm);
+            kz::launch_guide_infer_paths(s->dev, A, nA, gdev, g->raw.as<float>(), strm);
+            KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
+            kz::launch_shade_guided(s->dev, pp, A, nA, B, sq, ctr, film, film64, gsh, block, strm);
+            kz::launch_trace_shadow_guided(s->dev, sq, nA, ctr, film, film64, recs, cfg->max_depth, block, strm);
+            st.kernel_launches += 4;
+            KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
+            KZ_CUDA(cudaStreamSynchronize(strm));
+            KZ_CUDA(cudaGetLastError());
+            st.path_bounces += nA;
+            st.shadow_rays += s->ctr_host->n_shadow;
+            st.iterations += 1;
+            if (s->ctr_host->status)
+                return fail((kz_status)s->ctr_host->status, "device status %u during guided rendering",
+                            s->ctr_host->status);
+            nA = s->ctr_host->n_next;
+            std::swap(A, B);
+        }
+        st.paths += total;
+        spp_done += spp_pass;
+        pass += 1;
+        // training on this pass's radiance samples
+        if (gc.train) {
+            const auto t0 = std::chrono::steady_clock::now();
+            KZ_CUDA(cudaMemsetAsync(g->ctr.ptr, 0, 16, strm));
+            uint32_t* cnt = g->ctr.as<uint32_t>();
+            float* wsum = reinterpret_cast<float*>(cnt + 1);
+            kz::launch_guide_collect(recs, total * cfg->max_depth, g->samples.as<float4>(),
+                                     (uint32_t)std::min<uint64_t>(n_recs, 0xffffffffull), cnt, wsum, strm);
+            uint32_t hc[2] = {0, 0};
+            KZ_CUDA(cudaMemcpyAsync(hc, g->ctr.ptr, 8, cudaMemcpyDeviceToHost, strm));
+            KZ_CUDA(cudaStreamSynchronize(strm));
+            const uint32_t count = hc[0];
+            float wsum_h;
+            std::memcpy(&wsum_h, &hc[1], 4);
+            gs.train_samples += count;
+            if (count > 0 && wsum_h > 0.f && std::isfinite(wsum_h)) {
+                const uint32_t rows = std::min(count, gc.max_train_samples);
+                uint64_t stride = 2654435761ull % count;
+                if (stride == 0) stride = 1;
+                while (gcd64(stride, count) != 1) ++stride;
+                // weights normalised so each step sees mean weight 1 over its rows
+                const float wscale = (float)count / (wsum_h * (float)rows);
+                for (uint32_t k = 0; k < gc.steps_per_pass; ++k) {
+                    KZ_TRY(guide_train_device(g, g->samples.as<float4>(), count, rows, (uint32_t)stride,
+                                              (uint32_t)(((uint64_t)k * rows) % count), wscale, gc.learning_rate, true,
+                                              &s->dev, strm));
+                    gs.train_steps += 1;
+                }
+                float loss = 0.f;
+                KZ_CUDA(cudaMemcpyAsync(&loss, g->loss.ptr, 4, cudaMemcpyDeviceToHost, strm));
+                KZ_CUDA(cudaStreamSynchronize(strm));
+                gs.last_loss = loss;
+            }
+            train_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+        if (gc.time_budget_ms > 0.0) {
+            const double el =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+            if (el >= gc.time_budget_ms) break;
+        }
+    }
+    kz::launch_scale(film, nullptr, npix * 3, 1.0f / (float)spp_done, 0.0, strm);
+    if (film64) kz::launch_scale(nullptr, film64, npix * 3, 0.f, 1.0 / (double)spp_done, strm);
+    KZ_CUDA(cudaGetLastError());
+    if (mem == KZ_MEM_HOST) {
+        KZ_CUDA(cudaMemcpyAsync(out_rgb, film, npix * 12, cudaMemcpyDeviceToHost, strm));
+        if (out_rgb64) KZ_CUDA(cudaMemcpyAsync(out_rgb64, film64, npix * 24, cudaMemcpyDeviceToHost, strm));
+    }
+    KZ_CUDA(cudaStreamSynchronize(strm));
+    gs.passes = pass;
+    gs.spp_done = spp_done;
+    gs.train_ms = train_ms;
+    gs.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    if (out_stats) *out_stats = st;
+    if (out_gstats) *out_gstats = gs;
     return KZ_OK;
 }
 

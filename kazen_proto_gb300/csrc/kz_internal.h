@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/kazen_gb300.h"
@@ -32,6 +33,35 @@ struct DevScene {
     const float* light_cdf = nullptr;
     const float4* light_tris = nullptr;
     uint32_t n_lights = 0;
+    float3 box_lo = {0.f, 0.f, 0.f};   // scene bounds (guiding input encoding)
+    float3 box_inv = {1.f, 1.f, 1.f};  // 1 / extent per axis
+};
+
+// Guiding network parameters as the kernels read them.
+struct GuideDev {
+    const __nv_bfloat16* wbf = nullptr;  // BF16 weights, [out][in] per layer
+    const float* wf = nullptr;           // FP32 master copy (biases are read from it)
+    float3 box_lo = {0.f, 0.f, 0.f};
+    float3 box_inv = {1.f, 1.f, 1.f};
+};
+
+// One recorded path vertex of a guided pass (training data): position in the
+// scene box and the pdf the direction was sampled with, geometric normal and
+// a valid flag, sampled world direction, throughput after the vertex, and
+// the incident radiance gathered from the rest of the path.
+struct VRec {
+    float4 p;     // (p01.xyz, pdf)
+    float4 n;     // (n.xyz, valid ? 1 : 0)
+    float4 d;     // (dir.xyz, -)
+    float4 beta;  // (throughput after this vertex, -)
+    float4 L;     // (incident radiance estimate, -)
+};
+
+struct GuideShade {
+    const float* raw = nullptr;  // network outputs per path slot (40 floats)
+    VRec* recs = nullptr;        // [path - pass_first][vertex]
+    uint64_t pass_first = 0;
+    float alpha = 0.5f;          // probability of sampling the learned distribution
 };
 
 // Camera basis computed on the host (same float expressions the CPU
@@ -102,6 +132,29 @@ void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* c
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
                   ShadowSoA sq, DevCounters* ctr, float* film, double* film64, uint32_t block,
                   cudaStream_t st);
+void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
+                         ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
+                         uint32_t block, cudaStream_t st);
+void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
+                                double* film64, VRec* recs, uint32_t max_depth, uint32_t block, cudaStream_t st);
+// Training samples from a pass's vertex records: 3 float4 per sample
+// ((p01, weight), (n, -), (dir, -)); counters[0] = count, weight sum in *wsum.
+void launch_guide_collect(const VRec* recs, uint64_t n_recs, float4* samples, uint32_t cap, uint32_t* count,
+                          float* wsum, cudaStream_t st);
+
+// ---- guiding network (kz_mlp.cu) -------------------------------------------
+cudaError_t guide_kernel_setup();
+void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const GuideDev& gd, float* raw,
+                              cudaStream_t st);
+void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd, float* raw, cudaStream_t st);
+// One training batch of `rows` samples; row r reads sample ((r + offset) * stride) % count.
+// Adds the weighted loss to *loss and the gradient (weights scaled by wscale) to grad.
+void launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, uint32_t stride, uint32_t offset,
+                        float wscale, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
+                        cudaStream_t st);
+void launch_guide_adam(float* w, float* m, float* v, const float* grad, __nv_bfloat16* wbf, float lr, int step,
+                       cudaStream_t st);
+void launch_guide_to_bf16(const float* w, __nv_bfloat16* wbf, cudaStream_t st);
 void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
                          float* film, double* film64, uint32_t block, cudaStream_t st);
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st);

@@ -10,6 +10,7 @@
 // vertex in a fixed order whatever branches run:
 //   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
 //   [5] lobe pick   [6,7,8] lobe sample
+#include "kz_guide.cuh"
 #include "kz_internal.h"
 #include "kz_traverse.cuh"
 
@@ -245,8 +246,30 @@ __device__ __forceinline__ uint32_t cdf_sample(const float* cdf, uint32_t n, flo
 //    (integrator.cpp:452-462 reuses the previous light sample's pdf);
 //  * max_depth counts shaded vertices (the reference steps depth twice per
 //    loop, integrator.cpp:420,555).
+// Guided mode (learned path guiding, not in the reference) additionally:
+//  * on materials without delta lobes, samples the direction from the
+//    network's vMF mixture with probability alpha and from the BSDF mixture
+//    otherwise, with the one-sample MIS pdf alpha*q + (1-alpha)*p_bsdf in the
+//    path weight, the NEE MIS weight and the next emission hit's MIS weight;
+//  * records every such vertex (position, normal, direction, pdf,
+//    throughput after it) and adds each later contribution, divided by that
+//    throughput, to the vertex's incident-radiance estimate: the training
+//    data of the network.
+__device__ __forceinline__ void propagate(VRec* recs, uint64_t rbase, uint32_t depth, f3 c) {
+    for (uint32_t k = 0; k < depth; ++k) {
+        VRec& r = recs[rbase + k];
+        if (r.n.w == 0.f) continue;
+        const float4 b = r.beta;
+        r.L.x += b.x > 0.f ? c.x / b.x : 0.f;
+        r.L.y += b.y > 0.f ? c.y / b.y : 0.f;
+        r.L.z += b.z > 0.f ? c.z / b.z : 0.f;
+    }
+}
+
+template <bool kGuided>
 __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
-                                               ShadowSoA sq, DevCounters* ctr, float* film, double* film64) {
+                                               ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
+                                               GuideShade gs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool cont = false, shadow = false;
     float4 o_next, d_next, b_next, s_o, s_d, s_c;
@@ -282,6 +305,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
             f3 beta = xyz(b4);
             f3 Lsum = mk(0.f, 0.f, 0.f);
             const uint32_t nl = s.n_lights;
+            const uint64_t rbase = kGuided ? ((uint64_t)pid - gs.pass_first) * pp.max_depth : 0;
 
             // 1. emission (front face only: single_emissive_surface)
             const f3 Le = ld3(mat.Le);
@@ -296,6 +320,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                     }
                 }
                 Lsum = Lsum + hmul(beta, Le) * w;
+                if (kGuided) propagate(gs.recs, rbase, depth, Lsum);
             }
 
             // lobe selection probabilities (CompositeClosure::compute_pdfs)
@@ -303,15 +328,21 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
             float lp[KZ_MAX_LOBES];
             const float winv = 1.f / (beta.x + beta.y + beta.z);
             float wsum = 0.f;
-            bool any_smooth = false;
+            bool any_smooth = false, any_delta = false;
             for (uint32_t k = 0; k < nlobes; ++k) {
                 const kz_lobe& lb = mat.lobes[k];
                 lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
                 wsum += lp[k];
-                any_smooth |= !lobe_is_delta(lb.closure_id);
+                const bool dl = lobe_is_delta(lb.closure_id);
+                any_smooth |= !dl;
+                any_delta |= dl;
             }
             if (wsum > 0.f)
                 for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
+            const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
+            VmfMixture mix;
+            if (kGuided && guided) mixture_from_raw(gs.raw + (size_t)i * kGuideOut, mix);
+            const float alpha = gs.alpha;
 
             // 2. next-event estimation
             if (nl > 0 && any_smooth && wsum > 0.f) {
@@ -343,13 +374,16 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                         f = f + hmul(ld3(lb.weight), e.f);
                         bpdf += lp[k] * e.pdf;
                     }
+                    if (kGuided && guided) bpdf = alpha * mixture_pdf(mix, ldir) + (1.f - alpha) * bpdf;
                     if (!is_zero(f)) {
                         const float w = power_heuristic(lpdf, bpdf);
                         const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
                         shadow = true;
                         s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
                         s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
-                        s_c = make_float4(c.x, c.y, c.z, 0.f);
+                        const uint32_t tag =
+                            kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u)) : 0u;
+                        s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
                     }
                 }
             }
@@ -361,8 +395,64 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                 if (prob < u[4]) alive = false;
                 else beta = beta * (1.f / prob);
             }
-            // 4. BSDF sample (one-sample mixture over the non-delta lobes)
-            if (alive && wsum > 0.f) {
+            // 4. direction sampling
+            if (kGuided && guided && alive) {
+                // one-sample MIS of the learned vMF mixture and the BSDF mixture
+                f3 wo, wdir;
+                bool ok = true;
+                if (u[5] < alpha) {
+                    wdir = mixture_sample(mix, u[5] / alpha, u[6], u[7]);
+                    wo = fr.to_local(wdir);
+                } else {
+                    const float us = (u[5] - alpha) / (1.f - alpha);
+                    uint32_t sel = nlobes - 1;
+                    float acc = 0.f;
+                    for (uint32_t k = 0; k < nlobes; ++k) {
+                        acc += lp[k];
+                        if (us < acc) {
+                            sel = k;
+                            break;
+                        }
+                    }
+                    while (sel > 0 && lp[sel] == 0.f) --sel;
+                    const LobeSample smp = lobe_sample(mat.lobes[sel], wi, u[6], u[7], u[8]);
+                    ok = smp.valid;
+                    wo = smp.wo;
+                    wdir = normalize(fr.to_world(wo));
+                }
+                f3 f = mk(0.f, 0.f, 0.f);
+                float pdf = 0.f;
+                if (ok) {
+                    for (uint32_t k = 0; k < nlobes; ++k) {
+                        const kz_lobe& lb = mat.lobes[k];
+                        const LobeEval e = lobe_eval(lb, wi, wo);
+                        f = f + hmul(ld3(lb.weight), e.f);
+                        pdf += lp[k] * e.pdf;
+                    }
+                    pdf = alpha * mixture_pdf(mix, wdir) + (1.f - alpha) * pdf;
+                }
+                alive = ok && pdf > 0.f && !is_zero(f);
+                if (alive) {
+                    beta = hmul(beta, f * (1.f / pdf));
+                    alive = !is_zero(beta);
+                }
+                if (alive) {
+                    cont = true;
+                    o_next = make_float4(P.x, P.y, P.z, pdf);
+                    d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float(depth + 1));
+                    b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
+                    rng_next = rng.state;
+                    VRec& r = gs.recs[rbase + depth];
+                    const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
+                                        mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
+                    r.p = make_float4(p01.x, p01.y, p01.z, pdf);
+                    r.n = make_float4(Ng.x, Ng.y, Ng.z, 1.f);
+                    r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.f);
+                    r.beta = make_float4(beta.x, beta.y, beta.z, 0.f);
+                    r.L = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            } else if (alive && wsum > 0.f) {
+                // BSDF sample (one-sample mixture over the non-delta lobes)
                 uint32_t sel = nlobes - 1;
                 float acc = 0.f;
                 for (uint32_t k = 0; k < nlobes; ++k) {
@@ -428,9 +518,9 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
     }
 }
 
-template <bool kCount>
+template <bool kCount, bool kGuided>
 __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, DevCounters* ctr, float* film,
-                                                      double* film64) {
+                                                      double* film64, VRec* recs, uint32_t max_depth) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t dn = 0, dt = 0;
     if (i < ctr->n_shadow) {
@@ -442,9 +532,40 @@ __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, 
         if (!occluded && !overflow) {
             const float4 c = sq.c4[i];
             film_add(film, film64, __float_as_uint(d.w), xyz(c));
+            if (kGuided) {
+                const uint32_t tag = __float_as_uint(c.w);
+                propagate(recs, (uint64_t)(tag >> 4) * max_depth, tag & 15u, xyz(c));
+            }
         }
     }
     if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
+}
+
+// Training samples from the records of a guided pass: every valid vertex
+// whose incident-radiance estimate is positive, weighted by luminance / pdf.
+__global__ void k_guide_collect(const VRec* __restrict__ recs, uint64_t n, float4* __restrict__ samples, uint32_t cap,
+                                uint32_t* count, float* wsum) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = false;
+    float4 a, b, c;
+    if (i < n) {
+        const VRec r = recs[i];
+        const float lum = 0.2126f * r.L.x + 0.7152f * r.L.y + 0.0722f * r.L.z;
+        if (r.n.w != 0.f && lum > 0.f && r.p.w > 0.f && isfinite(lum)) {
+            const float w = lum / r.p.w;
+            take = isfinite(w);
+            a = make_float4(r.p.x, r.p.y, r.p.z, w);
+            b = make_float4(r.n.x, r.n.y, r.n.z, 0.f);
+            c = make_float4(r.d.x, r.d.y, r.d.z, 0.f);
+        }
+    }
+    const uint32_t slot = warp_append(take, count);
+    if (take && slot < cap) {
+        samples[3 * (size_t)slot] = a;
+        samples[3 * (size_t)slot + 1] = b;
+        samples[3 * (size_t)slot + 2] = c;
+        atomicAdd(wsum, a.w);
+    }
 }
 
 __global__ void k_scale(float* film, double* film64, uint64_t n, float sf, double sd) {
@@ -502,13 +623,30 @@ void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* c
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
                   DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
     if (!n_in) return;
-    k_shade<<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64);
+    k_shade<false><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
+                                                            GuideShade{});
+}
+void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
+                         ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
+                         uint32_t block, cudaStream_t st) {
+    if (!n_in) return;
+    k_shade<true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64, gs);
+}
+void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
+                                double* film64, VRec* recs, uint32_t max_depth, uint32_t block, cudaStream_t st) {
+    if (!n_max) return;
+    k_trace_shadow<false, true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, recs, max_depth);
+}
+void launch_guide_collect(const VRec* recs, uint64_t n_recs, float4* samples, uint32_t cap, uint32_t* count,
+                          float* wsum, cudaStream_t st) {
+    if (!n_recs) return;
+    k_guide_collect<<<grid_for(n_recs, 256), 256, 0, st>>>(recs, n_recs, samples, cap, count, wsum);
 }
 void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count, float* film,
                          double* film64, uint32_t block, cudaStream_t st) {
     if (!n_max) return;
-    if (count) k_trace_shadow<true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64);
-    else k_trace_shadow<false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64);
+    if (count) k_trace_shadow<true, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr, 0);
+    else k_trace_shadow<false, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr, 0);
 }
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
     if (!n) return;

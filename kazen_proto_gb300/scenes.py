@@ -255,3 +255,45 @@ def terrain_scene(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_sp
         d.add(v, q, L, is_light=True)
     d.camera = api.Camera(eye=(0.5, 0.9, -0.6), lookat=(0.5, 0.05, 0.55), up=(0, 1, 0), fov=60.0)
     return d
+
+
+def slit_room_scene(width=1024, height=1024, spp=16, max_depth=10, n_spheres=32, seed=11) -> SceneDesc:
+    """Narrow-aperture guiding scene: a closed unit room of 24 inward Lambert
+    quads (five walls split 2 x 2, and the +x wall made of the 4 quads that
+    frame a 0.05 x 0.5 slit), an exterior 0.6 x 0.6 quad light of radiance
+    200 facing the slit, and 32 GGX-conductor icospheres (alpha U[0.1, 0.5])."""
+    rng = np.random.default_rng(seed)
+    d = SceneDesc(width=width, height=height, spp=spp, max_depth=max_depth)
+    d.materials = [api.material([api.diffuse((0.7, 0.7, 0.7))])]
+    WALL = 0
+
+    def split(p0, e1, e2):
+        p0, e1, e2 = (np.asarray(x, np.float32) for x in (p0, e1, e2))
+        for a in range(2):
+            for b in range(2):
+                v, i = quad(p0 + e1 * (0.5 * a) + e2 * (0.5 * b), e1 * 0.5, e2 * 0.5)
+                d.add(v, i, WALL)
+
+    split((0, 0, 0), (0, 0, 1), (1, 0, 0))   # floor, +y
+    split((0, 1, 0), (1, 0, 0), (0, 0, 1))   # ceiling, -y
+    split((0, 0, 1), (0, 1, 0), (1, 0, 0))   # back, -z
+    split((0, 0, 0), (1, 0, 0), (0, 1, 0))   # front, +z
+    split((0, 0, 0), (0, 1, 0), (0, 0, 1))   # left, +x
+    # right wall (x = 1, facing -x) with a vertical slit: z in [0.475, 0.525], y in [0.25, 0.75]
+    z0, z1, y0, y1 = 0.475, 0.525, 0.25, 0.75
+    for (za, zb, ya, yb) in [(0, 1, 0, y0), (0, 1, y1, 1), (0, z0, y0, y1), (z1, 1, y0, y1)]:
+        v, i = quad((1, ya, za), (0, 0, zb - za), (0, yb - ya, 0))
+        d.add(v, i, WALL)
+    light = api.material([], Le=(200.0, 200.0, 200.0))
+    d.materials.append(light)
+    v, i = quad((1.3, 0.2, 0.2), (0, 0, 0.6), (0, 0.6, 0))  # faces -x, toward the slit
+    d.add(v, i, len(d.materials) - 1, is_light=True)
+    sv, sf = icosphere(2)
+    for _ in range(n_spheres):
+        r = rng.uniform(0.03, 0.07)
+        pos = np.array([rng.uniform(0.1, 0.9), rng.uniform(0.05, 0.6), rng.uniform(0.1, 0.9)], np.float32)
+        d.materials.append(api.material([api.conductor_ggx(tuple(rng.uniform(0.6, 0.95, 3)),
+                                                            float(rng.uniform(0.1, 0.5)))]))
+        d.add((sv * np.float32(r) + pos).astype(np.float32), sf, len(d.materials) - 1)
+    d.camera = api.Camera(eye=(0.08, 0.55, 0.08), lookat=(0.75, 0.35, 0.8), up=(0, 1, 0), fov=75.0)
+    return d
