@@ -311,7 +311,7 @@ __device__ __forceinline__ Mdf lobe_mdf(const kz_lobe& l, f3 wi, float& eta) {
 
 // Value and pdf of one lobe exactly as the reference eval functions return
 // them; a configuration the reference rejects gives (0, 0).
-__device__ LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
+__device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
     LobeEval r{mk(0.f, 0.f, 0.f), 0.f};
     switch (l.closure_id) {
     case KZ_CLOSURE_DIFFUSE: {
@@ -407,7 +407,7 @@ __device__ LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
 }
 
 // f*|cos(wo)| and the solid-angle pdf of wo under the lobe's own sampler.
-__device__ LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
+__device__ inline LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
     LobeEval r = lobe_eval_reference(l, wi, wo);
     switch (l.closure_id) {
     case KZ_CLOSURE_DIFFUSE:
@@ -446,7 +446,7 @@ __device__ LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
     }
 }
 
-__device__ LobeSample lobe_sample(const kz_lobe& l, f3 wi, float u0, float u1, float u2) {
+__device__ inline LobeSample lobe_sample(const kz_lobe& l, f3 wi, float u0, float u1, float u2) {
     LobeSample s{mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f), 0.f, false, false};
     switch (l.closure_id) {
     case KZ_CLOSURE_DIFFUSE: {
