@@ -48,6 +48,7 @@ def parse():
                    help="full-size scene, 640x360 frame at 4 spp, for ncu captures of single launches")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-traversal", action="store_true")
+    p.add_argument("--no-guiding", action="store_true")
     return p.parse_args()
 
 
@@ -234,6 +235,54 @@ def traversal_bench(steps, warmup):
     return res
 
 
+# ---------------------------------------------------------------- learned guiding, equal time
+def guiding_bench(R=256, plain_spp=2048, ref_spp=32768, max_depth=10):
+    """Narrow-aperture slit room at R x R: relMSE against a plain FP64
+    reference of ref_spp, plain path tracing for plain_spp vs guided path
+    tracing (network trained online from scratch, inside the same wall-clock
+    budget), plus the equal-spp error of the trained network."""
+    from kazen_proto_gb300 import api, scenes
+
+    def rel_mse(img, ref, eps=1e-2):
+        return float(np.mean((np.asarray(img, np.float64) - ref) ** 2 / (ref ** 2 + eps)))
+
+    d = scenes.slit_room_scene(R, R, max_depth=max_depth)
+    s = d.build()
+    t0 = time.perf_counter()
+    ref = api.Renderer(spp=ref_spp, max_depth=max_depth, seed=99).render(s, d.camera, R, R, fp64=True)[1]
+    ref_s = time.perf_counter() - t0
+    r = api.Renderer(spp=plain_spp, max_depth=max_depth, seed=1)
+    r.render(s, d.camera, R, R)  # warm-up
+    t0 = time.perf_counter()
+    img_p = r.render(s, d.camera, R, R)
+    T = time.perf_counter() - t0
+    e_plain = rel_mse(img_p, ref)
+    g = api.Guide(seed=3)
+    api.render_guided(s, g, d.camera, R, R, spp=4, max_depth=max_depth, seed=2,
+                      gcfg=api.guide_config(train=False, spp_per_pass=4))  # warm-up (kernels, buffers)
+    g.close()
+    g = api.Guide(seed=3)
+    t0 = time.perf_counter()
+    img_g, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=1 << 20, max_depth=max_depth, seed=7,
+                                          gcfg=api.guide_config(spp_per_pass=4, learning_rate=1e-2,
+                                                                max_train_steps=512, time_budget_ms=T * 1e3))
+    Tg = time.perf_counter() - t0
+    e_guided = rel_mse(img_g, ref)
+    img_f, _, _, _ = api.render_guided(s, g, d.camera, R, R, spp=plain_spp, max_depth=max_depth, seed=11,
+                                       gcfg=api.guide_config(train=False, spp_per_pass=64))
+    e_frozen = rel_mse(img_f, ref)
+    return {"scene": "slit room %dx%d, max depth %d, 24 Lambert quads + 32 GGX spheres, 4x4 exterior light "
+                     "(radiance 200) behind a 0.05x0.5 slit" % (R, R, max_depth),
+            "reference": "plain, %d spp, FP64 accumulation (%.1f s)" % (ref_spp, ref_s),
+            "plain": {"spp": plain_spp, "seconds": round(T, 4), "relmse": e_plain},
+            "guided_equal_time": {"seconds": round(Tg, 4), "spp": gst["spp_done"], "train_steps": gst["train_steps"],
+                                  "train_ms": round(gst["train_ms"], 1), "train_samples": gst["train_samples"],
+                                  "relmse": e_guided},
+            "relmse_ratio_plain_over_guided_equal_time": round(e_plain / e_guided, 3),
+            "guided_trained_equal_spp": {"spp": plain_spp, "relmse": e_frozen},
+            "relmse_ratio_plain_over_guided_equal_spp": round(e_plain / e_frozen, 3)}
+
+
 def load_traffic():
     """DRAM bytes per ray of k_trace_paths from the committed ncu summary."""
     import re
@@ -323,6 +372,10 @@ def run_ours(args):
     if rank == 0 and not args.no_traversal and not args.small and not args.profile:
         trav = traversal_bench(max(3, args.steps), max(3, args.warmup))
 
+    guide = None
+    if rank == 0 and not args.no_guiding and not args.small and not args.profile:
+        guide = guiding_bench()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
@@ -366,6 +419,7 @@ def run_ours(args):
         "clocks": clk,
         "cpu_baseline": cpu,
         "traversal": trav,
+        "guiding": guide,
     }
     if img is not None:
         line["image_mean"] = float(np.mean(img))

@@ -270,11 +270,12 @@ typedef struct kz_guide kz_guide;
 
 typedef struct kz_guide_config {
     float    alpha;             /* probability of sampling the network (0 = 0.5) */
-    float    learning_rate;     /* Adam step size (0 = 1e-3)                     */
+    float    learning_rate;     /* Adam step size (0 = 1e-2)                     */
     uint32_t spp_per_pass;      /* spp rendered between training steps (0 = 1)   */
     uint32_t train;             /* 1: train after every pass, 0: frozen network  */
     uint32_t max_train_samples; /* samples per Adam step (0 = 2^18)               */
     uint32_t steps_per_pass;    /* Adam steps after each pass (0 = 1)            */
+    uint32_t max_train_steps;   /* > 0: freeze the network after this many steps */
     double   time_budget_ms;    /* > 0: stop after the pass that reaches it       */
 } kz_guide_config;
 

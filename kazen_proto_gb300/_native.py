@@ -90,7 +90,7 @@ class KzRenderStats(C.Structure):
 class KzGuideConfig(C.Structure):
     _fields_ = [("alpha", C.c_float), ("learning_rate", C.c_float), ("spp_per_pass", C.c_uint32),
                 ("train", C.c_uint32), ("max_train_samples", C.c_uint32), ("steps_per_pass", C.c_uint32),
-                ("time_budget_ms", C.c_double)]
+                ("max_train_steps", C.c_uint32), ("time_budget_ms", C.c_double)]
 
 
 class KzGuideStats(C.Structure):

@@ -416,8 +416,8 @@ class Guide:
         return (loss.value, grad) if want_grad else loss.value
 
 
-def guide_config(alpha=0.5, learning_rate=1e-3, spp_per_pass=1, train=True, max_train_samples=1 << 18,
-                 steps_per_pass=1, time_budget_ms=0.0) -> N.KzGuideConfig:
+def guide_config(alpha=0.5, learning_rate=1e-2, spp_per_pass=1, train=True, max_train_samples=1 << 18,
+                 steps_per_pass=1, time_budget_ms=0.0, max_train_steps=0) -> N.KzGuideConfig:
     c = N.KzGuideConfig()
     c.alpha = alpha
     c.learning_rate = learning_rate
@@ -425,6 +425,7 @@ def guide_config(alpha=0.5, learning_rate=1e-3, spp_per_pass=1, train=True, max_
     c.train = 1 if train else 0
     c.max_train_samples = max_train_samples
     c.steps_per_pass = steps_per_pass
+    c.max_train_steps = max_train_steps
     c.time_budget_ms = time_budget_ms
     return c
 

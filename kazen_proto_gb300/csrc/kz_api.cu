@@ -883,14 +883,16 @@ kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd
 struct kz_guide {
     std::mutex mu;
     int device = 0;
+    float band_scale = 1.f;
+    float weight_cap = 20.f;
     cudaStream_t stream = nullptr;
     DevBuf w, m, v, grad, wbf, loss;  // parameters (FP32, BF16), Adam moments, gradient
-    DevBuf train_rec, samples, raw, recs, pts, ctr;
+    DevBuf train_rec, samples, raw, recs, nee, pts, ctr;
     int step = 0;
     ~kz_guide() {
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
-        DevBuf* all[] = {&w, &m, &v, &grad, &wbf, &loss, &train_rec, &samples, &raw, &recs, &pts, &ctr};
+        DevBuf* all[] = {&w, &m, &v, &grad, &wbf, &loss, &train_rec, &samples, &raw, &recs, &nee, &pts, &ctr};
         for (DevBuf* b : all) b->release();
         if (stream) cudaStreamDestroy(stream);
     }
@@ -898,6 +900,7 @@ struct kz_guide {
         kz::GuideDev g;
         g.wbf = static_cast<const __nv_bfloat16*>(wbf.ptr);
         g.wf = w.as<float>();
+        g.band_scale = band_scale;
         if (sc) {
             g.box_lo = sc->box_lo;
             g.box_inv = sc->box_inv;
@@ -949,12 +952,12 @@ kz_status guide_upload_params(kz_guide* g, const float* host) {
 // One training batch on device samples: gradient into g->grad (zeroed
 // first), loss into g->loss; Adam when apply.
 kz_status guide_train_device(kz_guide* g, const float4* samples, uint32_t count, uint32_t rows, uint32_t stride,
-                             uint32_t offset, float wscale, float lr, bool apply, const kz::DevScene* sc,
+                             uint32_t offset, float wscale, float wcap, float lr, bool apply, const kz::DevScene* sc,
                              cudaStream_t st) {
     KZ_TRY(g->train_rec.ensure((size_t)rows * 496 * 2));
     KZ_CUDA(cudaMemsetAsync(g->grad.ptr, 0, KZ_GUIDE_PARAMS * 4, st));
     KZ_CUDA(cudaMemsetAsync(g->loss.ptr, 0, 4, st));
-    kz::launch_guide_train(samples, count, rows, stride, offset, wscale, g->dev(sc),
+    kz::launch_guide_train(samples, count, rows, stride, offset, wscale, wcap, g->dev(sc),
                            static_cast<__nv_bfloat16*>(g->train_rec.ptr), g->grad.as<float>(), g->loss.as<float>(), st);
     KZ_CUDA(cudaGetLastError());
     if (apply) {
@@ -1072,7 +1075,8 @@ kz_status kz_guide_train_step(kz_guide* g, const float* samples, uint64_t n, flo
         KZ_CUDA(cudaMemcpyAsync(g->samples.ptr, samples, n * 48, cudaMemcpyHostToDevice, st));
         ds = g->samples.as<float4>();
     }
-    KZ_TRY(guide_train_device(g, ds, (uint32_t)n, (uint32_t)n, 1, 0, 1.0f / (float)n, lr, apply != 0, nullptr, st));
+    KZ_TRY(guide_train_device(g, ds, (uint32_t)n, (uint32_t)n, 1, 0, 1.0f / (float)n, 3.0e38f, lr, apply != 0,
+                              nullptr, st));
     float loss = 0.f;
     KZ_CUDA(cudaMemcpyAsync(&loss, g->loss.ptr, 4, cudaMemcpyDeviceToHost, st));
     if (out_grad) KZ_CUDA(cudaMemcpyAsync(out_grad, g->grad.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, st));
@@ -1098,7 +1102,7 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     kz_guide_config gc = gcfg_in ? *gcfg_in : kz_guide_config{};
     if (gc.alpha == 0.f) gc.alpha = 0.5f;
     if (!(gc.alpha > 0.f && gc.alpha < 1.f)) return fail(KZ_ERR_INVALID_ARG, "alpha must be in (0, 1)");
-    if (gc.learning_rate == 0.f) gc.learning_rate = 1e-3f;
+    if (gc.learning_rate == 0.f) gc.learning_rate = 1e-2f;
     if (gc.spp_per_pass == 0) gc.spp_per_pass = 1;
     if (gc.max_train_samples == 0) gc.max_train_samples = 1u << 18;
     if (gc.steps_per_pass == 0) gc.steps_per_pass = 1;
@@ -1135,9 +1139,11 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
     const uint64_t n_recs = per_pass * cfg->max_depth;
     KZ_TRY(g->recs.ensure(n_recs * sizeof(kz::VRec)));
-    KZ_TRY(g->samples.ensure(n_recs * 48));
+    KZ_TRY(g->nee.ensure(n_recs * sizeof(kz::NRec)));
+    KZ_TRY(g->samples.ensure(2 * n_recs * 48));
     KZ_TRY(g->raw.ensure((size_t)cap * 160));
     kz::VRec* recs = g->recs.as<kz::VRec>();
+    kz::NRec* nee = g->nee.as<kz::NRec>();
     const kz::GuideDev gdev = g->dev(&s->dev);
 
     kz_render_stats st{};
@@ -1148,17 +1154,22 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     while (spp_done < cfg->spp) {
         const uint32_t spp_pass = (uint32_t)std::min<uint64_t>(gc.spp_per_pass, cfg->spp - spp_done);
         const uint64_t total = npix * spp_pass;
+        const bool train = gc.train && (gc.max_train_steps == 0 || gs.train_steps < gc.max_train_steps);
         kz::PathParams pp;
         pp.spp = spp_pass;
         pp.max_depth = cfg->max_depth;
         pp.rr_min = cfg->rr_min_depth;
         pp.seed = cfg->seed * 0x9E3779B97F4A7C15ull + pass + 1;  // a fresh PCG32 seed per pass
         pp.camera = 1;
-        KZ_CUDA(cudaMemsetAsync(recs, 0, total * cfg->max_depth * sizeof(kz::VRec), strm));
+        if (train) {
+            KZ_CUDA(cudaMemsetAsync(recs, 0, total * cfg->max_depth * sizeof(kz::VRec), strm));
+            KZ_CUDA(cudaMemsetAsync(nee, 0, total * cfg->max_depth * sizeof(kz::NRec), strm));
+        }
         KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), strm));
         kz::GuideShade gsh;
         gsh.raw = g->raw.as<float>();
-        gsh.recs = recs;
+        gsh.recs = train ? recs : nullptr;
+        gsh.nee = train ? nee : nullptr;
         gsh.pass_first = 0;
         gsh.alpha = gc.alpha;
         uint64_t next = 0;
@@ -1176,7 +1187,8 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
             kz::launch_guide_infer_paths(s->dev, A, nA, gdev, g->raw.as<float>(), strm);
             KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
             kz::launch_shade_guided(s->dev, pp, A, nA, B, sq, ctr, film, film64, gsh, block, strm);
-            kz::launch_trace_shadow_guided(s->dev, sq, nA, ctr, film, film64, recs, cfg->max_depth, block, strm);
+            kz::launch_trace_shadow_guided(s->dev, sq, nA, ctr, film, film64, gsh.recs, gsh.nee, cfg->max_depth,
+                                           block, strm);
             st.kernel_launches += 4;
             KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
             KZ_CUDA(cudaStreamSynchronize(strm));
@@ -1194,13 +1206,13 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
         spp_done += spp_pass;
         pass += 1;
         // training on this pass's radiance samples
-        if (gc.train) {
+        if (train) {
             const auto t0 = std::chrono::steady_clock::now();
             KZ_CUDA(cudaMemsetAsync(g->ctr.ptr, 0, 16, strm));
             uint32_t* cnt = g->ctr.as<uint32_t>();
             float* wsum = reinterpret_cast<float*>(cnt + 1);
-            kz::launch_guide_collect(recs, total * cfg->max_depth, g->samples.as<float4>(),
-                                     (uint32_t)std::min<uint64_t>(n_recs, 0xffffffffull), cnt, wsum, strm);
+            kz::launch_guide_collect(recs, nee, total * cfg->max_depth, g->samples.as<float4>(),
+                                     (uint32_t)std::min<uint64_t>(2 * n_recs, 0xffffffffull), cnt, wsum, strm);
             uint32_t hc[2] = {0, 0};
             KZ_CUDA(cudaMemcpyAsync(hc, g->ctr.ptr, 8, cudaMemcpyDeviceToHost, strm));
             KZ_CUDA(cudaStreamSynchronize(strm));
@@ -1216,9 +1228,11 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
                 // weights normalised so each step sees mean weight 1 over its rows
                 const float wscale = (float)count / (wsum_h * (float)rows);
                 for (uint32_t k = 0; k < gc.steps_per_pass; ++k) {
+                    // outliers (rare paths through a narrow opening) would
+                    // dominate a step: cap a sample at 20x the mean weight
                     KZ_TRY(guide_train_device(g, g->samples.as<float4>(), count, rows, (uint32_t)stride,
-                                              (uint32_t)(((uint64_t)k * rows) % count), wscale, gc.learning_rate, true,
-                                              &s->dev, strm));
+                                              (uint32_t)(((uint64_t)k * rows) % count), wscale, g->weight_cap / (float)rows,
+                                              gc.learning_rate, true, &s->dev, strm));
                     gs.train_steps += 1;
                 }
                 float loss = 0.f;

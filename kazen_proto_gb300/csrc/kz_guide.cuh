@@ -42,11 +42,11 @@ constexpr int kGuideParams = kOffB4 + 40;  // 15,080 (14,016 live weights, layer
 // Input features of a shading point: position p01 in [0,1]^3 of the scene
 // box, normal n. Feature j: for j < 48, axis a = j / 16, band b = (j % 16) / 2,
 // sin for even j, cos for odd j, of 2^b * pi * p01[a]; 48..50 the normal.
-__device__ __forceinline__ float guide_feature(int j, f3 p01, f3 n) {
+__device__ __forceinline__ float guide_feature(int j, f3 p01, f3 n, float band_scale) {
     if (j < 48) {
         const int a = j >> 4;
         const int b = (j & 15) >> 1;
-        const float x = comp(p01, a) * (float)(1 << b) * kPi;
+        const float x = comp(p01, a) * (float)(1 << b) * (kPi * band_scale);
         return (j & 1) ? cosf(x) : sinf(x);
     }
     if (j < 51) return comp(n, j - 48);

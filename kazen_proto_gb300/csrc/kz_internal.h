@@ -43,6 +43,7 @@ struct GuideDev {
     const float* wf = nullptr;           // FP32 master copy (biases are read from it)
     float3 box_lo = {0.f, 0.f, 0.f};
     float3 box_inv = {1.f, 1.f, 1.f};
+    float band_scale = 1.f;  // frequency of band b: 2^b * pi * band_scale
 };
 
 // One recorded path vertex of a guided pass (training data): position in the
@@ -57,9 +58,18 @@ struct VRec {
     float4 L;     // (incident radiance estimate, -)
 };
 
+// A next-event sample as training data: (p01.xyz, weight), (n.xyz, 1 once
+// the shadow ray found the light visible), (light direction, -).
+struct NRec {
+    float4 p;
+    float4 n;
+    float4 d;
+};
+
 struct GuideShade {
     const float* raw = nullptr;  // network outputs per path slot (40 floats)
     VRec* recs = nullptr;        // [path - pass_first][vertex]
+    NRec* nee = nullptr;         // [path - pass_first][vertex]
     uint64_t pass_first = 0;
     float alpha = 0.5f;          // probability of sampling the learned distribution
 };
@@ -136,11 +146,12 @@ void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, ui
                          ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
                          uint32_t block, cudaStream_t st);
 void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
-                                double* film64, VRec* recs, uint32_t max_depth, uint32_t block, cudaStream_t st);
-// Training samples from a pass's vertex records: 3 float4 per sample
-// ((p01, weight), (n, -), (dir, -)); counters[0] = count, weight sum in *wsum.
-void launch_guide_collect(const VRec* recs, uint64_t n_recs, float4* samples, uint32_t cap, uint32_t* count,
-                          float* wsum, cudaStream_t st);
+                                double* film64, VRec* recs, NRec* nee, uint32_t max_depth, uint32_t block,
+                                cudaStream_t st);
+// Training samples from a pass's vertex and next-event records: 3 float4 per
+// sample ((p01, weight), (n, -), (dir, -)); *count and the weight sum *wsum.
+void launch_guide_collect(const VRec* recs, const NRec* nee, uint64_t n_recs, float4* samples, uint32_t cap,
+                          uint32_t* count, float* wsum, cudaStream_t st);
 
 // ---- guiding network (kz_mlp.cu) -------------------------------------------
 cudaError_t guide_kernel_setup();
@@ -148,9 +159,10 @@ void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const Gu
                               cudaStream_t st);
 void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd, float* raw, cudaStream_t st);
 // One training batch of `rows` samples; row r reads sample ((r + offset) * stride) % count.
-// Adds the weighted loss to *loss and the gradient (weights scaled by wscale) to grad.
+// Adds the weighted loss to *loss and the gradient to grad; a sample's weight
+// is min(weight * wscale, wcap).
 void launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, uint32_t stride, uint32_t offset,
-                        float wscale, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
+                        float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
                         cudaStream_t st);
 void launch_guide_adam(float* w, float* m, float* v, const float* grad, __nv_bfloat16* wbf, float lr, int step,
                        cudaStream_t st);

@@ -320,7 +320,8 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                     }
                 }
                 Lsum = Lsum + hmul(beta, Le) * w;
-                if (kGuided) propagate(gs.recs, rbase, depth, Lsum);
+                // MIS-weighted, like the next-event samples it pairs with
+                if (kGuided && gs.recs) propagate(gs.recs, rbase, depth, Lsum);
             }
 
             // lobe selection probabilities (CompositeClosure::compute_pdfs)
@@ -384,6 +385,18 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                         const uint32_t tag =
                             kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u)) : 0u;
                         s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
+                        if (kGuided && gs.nee && guided) {
+                            // training sample: the light direction with its
+                            // MIS-weighted share of L*f*cos over the light pdf
+                            const f3 fl = hmul(f, ld3(lt.Le));
+                            const float wt = (0.2126f * fl.x + 0.7152f * fl.y + 0.0722f * fl.z) * (w / lpdf);
+                            const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
+                                                mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
+                            NRec& nr = gs.nee[rbase + depth];
+                            nr.p = make_float4(p01.x, p01.y, p01.z, wt);
+                            nr.n = make_float4(Ng.x, Ng.y, Ng.z, 0.f);
+                            nr.d = make_float4(ldir.x, ldir.y, ldir.z, 0.f);
+                        }
                     }
                 }
             }
@@ -442,12 +455,16 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
                     d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float(depth + 1));
                     b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
                     rng_next = rng.state;
+                }
+                if (alive && gs.recs) {
                     VRec& r = gs.recs[rbase + depth];
                     const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
                                         mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
                     r.p = make_float4(p01.x, p01.y, p01.z, pdf);
                     r.n = make_float4(Ng.x, Ng.y, Ng.z, 1.f);
-                    r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.f);
+                    // d.w: luminance of f*|cos| along the sampled direction,
+                    // so the network learns the whole integrand L*f*cos
+                    r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.2126f * f.x + 0.7152f * f.y + 0.0722f * f.z);
                     r.beta = make_float4(beta.x, beta.y, beta.z, 0.f);
                     r.L = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
@@ -520,7 +537,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSo
 
 template <bool kCount, bool kGuided>
 __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, DevCounters* ctr, float* film,
-                                                      double* film64, VRec* recs, uint32_t max_depth) {
+                                                      double* film64, VRec* recs, NRec* nee, uint32_t max_depth) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t dn = 0, dt = 0;
     if (i < ctr->n_shadow) {
@@ -532,9 +549,11 @@ __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, 
         if (!occluded && !overflow) {
             const float4 c = sq.c4[i];
             film_add(film, film64, __float_as_uint(d.w), xyz(c));
-            if (kGuided) {
+            if (kGuided && recs) {
                 const uint32_t tag = __float_as_uint(c.w);
-                propagate(recs, (uint64_t)(tag >> 4) * max_depth, tag & 15u, xyz(c));
+                const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
+                propagate(recs, rb, tag & 15u, xyz(c));
+                if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
             }
         }
     }
@@ -542,21 +561,30 @@ __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, 
 }
 
 // Training samples from the records of a guided pass: every valid vertex
-// whose incident-radiance estimate is positive, weighted by luminance / pdf.
-__global__ void k_guide_collect(const VRec* __restrict__ recs, uint64_t n, float4* __restrict__ samples, uint32_t cap,
-                                uint32_t* count, float* wsum) {
+// whose integrand estimate L*f*cos is positive, weighted by its luminance
+// over the pdf the direction was sampled with.
+__global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __restrict__ nee, uint64_t n,
+                                float4* __restrict__ samples, uint32_t cap, uint32_t* count, float* wsum) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool take = false;
     float4 a, b, c;
     if (i < n) {
         const VRec r = recs[i];
-        const float lum = 0.2126f * r.L.x + 0.7152f * r.L.y + 0.0722f * r.L.z;
+        const float lum = (0.2126f * r.L.x + 0.7152f * r.L.y + 0.0722f * r.L.z) * r.d.w;
         if (r.n.w != 0.f && lum > 0.f && r.p.w > 0.f && isfinite(lum)) {
             const float w = lum / r.p.w;
             take = isfinite(w);
             a = make_float4(r.p.x, r.p.y, r.p.z, w);
             b = make_float4(r.n.x, r.n.y, r.n.z, 0.f);
             c = make_float4(r.d.x, r.d.y, r.d.z, 0.f);
+        }
+    } else if (i < 2 * n && nee) {
+        const NRec r = nee[i - n];
+        if (r.n.w != 0.f && r.p.w > 0.f && isfinite(r.p.w)) {
+            take = true;
+            a = r.p;
+            b = make_float4(r.n.x, r.n.y, r.n.z, 0.f);
+            c = r.d;
         }
     }
     const uint32_t slot = warp_append(take, count);
@@ -633,20 +661,26 @@ void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, ui
     k_shade<true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64, gs);
 }
 void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
-                                double* film64, VRec* recs, uint32_t max_depth, uint32_t block, cudaStream_t st) {
+                                double* film64, VRec* recs, NRec* nee, uint32_t max_depth, uint32_t block,
+                                cudaStream_t st) {
     if (!n_max) return;
-    k_trace_shadow<false, true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, recs, max_depth);
+    k_trace_shadow<false, true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, recs, nee,
+                                                                         max_depth);
 }
-void launch_guide_collect(const VRec* recs, uint64_t n_recs, float4* samples, uint32_t cap, uint32_t* count,
-                          float* wsum, cudaStream_t st) {
+void launch_guide_collect(const VRec* recs, const NRec* nee, uint64_t n_recs, float4* samples, uint32_t cap,
+                          uint32_t* count, float* wsum, cudaStream_t st) {
     if (!n_recs) return;
-    k_guide_collect<<<grid_for(n_recs, 256), 256, 0, st>>>(recs, n_recs, samples, cap, count, wsum);
+    k_guide_collect<<<grid_for(2 * n_recs, 256), 256, 0, st>>>(recs, nee, n_recs, samples, cap, count, wsum);
 }
 void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count, float* film,
                          double* film64, uint32_t block, cudaStream_t st) {
     if (!n_max) return;
-    if (count) k_trace_shadow<true, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr, 0);
-    else k_trace_shadow<false, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr, 0);
+    if (count)
+        k_trace_shadow<true, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr,
+                                                                              nullptr, 0);
+    else
+        k_trace_shadow<false, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr,
+                                                                               nullptr, 0);
 }
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
     if (!n) return;

@@ -79,15 +79,15 @@ __device__ __forceinline__ void to_afrag(const float (&c)[NT][4], uint32_t (&a)[
 }
 
 // Input features of rows g and g+8 straight into A fragments (4 k-tiles).
-__device__ __forceinline__ void feature_afrag(uint32_t (&a)[4][4], f3 p0, f3 n0, f3 p1, f3 n1, int lane) {
+__device__ __forceinline__ void feature_afrag(uint32_t (&a)[4][4], f3 p0, f3 n0, f3 p1, f3 n1, float bs, int lane) {
     const int t = lane & 3;
 #pragma unroll
     for (int kt = 0; kt < 4; ++kt) {
         const int c = 16 * kt + 2 * t;
-        a[kt][0] = pack2(guide_feature(c, p0, n0), guide_feature(c + 1, p0, n0));
-        a[kt][1] = pack2(guide_feature(c, p1, n1), guide_feature(c + 1, p1, n1));
-        a[kt][2] = pack2(guide_feature(c + 8, p0, n0), guide_feature(c + 9, p0, n0));
-        a[kt][3] = pack2(guide_feature(c + 8, p1, n1), guide_feature(c + 9, p1, n1));
+        a[kt][0] = pack2(guide_feature(c, p0, n0, bs), guide_feature(c + 1, p0, n0, bs));
+        a[kt][1] = pack2(guide_feature(c, p1, n1, bs), guide_feature(c + 1, p1, n1, bs));
+        a[kt][2] = pack2(guide_feature(c + 8, p0, n0, bs), guide_feature(c + 9, p0, n0, bs));
+        a[kt][3] = pack2(guide_feature(c + 8, p1, n1, bs), guide_feature(c + 9, p1, n1, bs));
     }
 }
 
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene sc, PathSoA ps, co
         }
         uint32_t x[4][4], a1[4][4], a2[4][4], a3[4][4];
         float h1[8][4], h2[8][4], h3[8][4], o[5][4];
-        feature_afrag(x, p[0], nn[0], p[1], nn[1], lane);
+        feature_afrag(x, p[0], nn[0], p[1], nn[1], gd.band_scale, lane);
         forward_tile(s, gd.wf, x, h1, h2, h3, o, a1, a2, a3, lane);
         for (int h = 0; h < 2; ++h) {
             const uint32_t r = tile * 16 + g + 8 * h;
@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene sc, PathSoA ps, co
 __global__ void __launch_bounds__(kTrainWarps * 32) k_guide_train_fb(const float4* __restrict__ samples,
                                                                      uint32_t count, uint32_t n, uint32_t stride,
                                                                      uint32_t offset, GuideDev gd, float inv_n,
+                                                                     float wcap,
                                                                      __nv_bfloat16* __restrict__ rec,
                                                                      float* __restrict__ loss) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_guide_train_fb(const float
         }
         uint32_t x[4][4], a1[4][4], a2[4][4], a3[4][4];
         float h1[8][4], h2[8][4], h3[8][4], o[5][4];
-        feature_afrag(x, p[0], nn[0], p[1], nn[1], lane);
+        feature_afrag(x, p[0], nn[0], p[1], nn[1], gd.band_scale, lane);
         forward_tile(s, gd.wf, x, h1, h2, h3, o, a1, a2, a3, lane);
         // raw outputs -> shared rows; one lane per row computes d(loss)/d(raw)
 #pragma unroll
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_guide_train_fb(const float
                 const float4 a = samples[3 * si], c = samples[3 * si + 2];
                 float raw[kGuideOut];
                 for (int k = 0; k < kGuideOut; ++k) raw[k] = so[lane * 41 + k];
-                const float w = a.w * inv_n;
+                const float w = fminf(a.w * inv_n, wcap);
                 loss_acc += w * mixture_nll_grad(raw, mk(c.x, c.y, c.z), w, gr);
             } else {
                 for (int k = 0; k < kGuideOut; ++k) gr[k] = 0.f;
@@ -480,13 +481,13 @@ void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd
 }
 
 void launch_guide_train(const float4* samples, uint32_t count, uint32_t n, uint32_t stride, uint32_t offset,
-                        float wscale, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
+                        float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
                         cudaStream_t st) {
     if (!n || !count) return;
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = min((tiles + kTrainWarps - 1) / kTrainWarps, (uint32_t)sm_count() * 2);
-    k_guide_train_fb<<<grid, kTrainWarps * 32, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, rec,
-                                                                  loss);
+    k_guide_train_fb<<<grid, kTrainWarps * 32, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, wcap,
+                                                                  rec, loss);
     const uint32_t ctas = min((n + kChunk - 1) / kChunk, (uint32_t)sm_count() * 2);
     uint32_t rows = (n + ctas - 1) / ctas;
     rows = (rows + kChunk - 1) / kChunk * kChunk;

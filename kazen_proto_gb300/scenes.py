@@ -257,11 +257,14 @@ def terrain_scene(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_sp
     return d
 
 
-def slit_room_scene(width=1024, height=1024, spp=16, max_depth=10, n_spheres=32, seed=11) -> SceneDesc:
+def slit_room_scene(width=1024, height=1024, spp=16, max_depth=10, n_spheres=32, seed=11, light_size=4.0,
+                    light_dist=2.0) -> SceneDesc:
     """Narrow-aperture guiding scene: a closed unit room of 24 inward Lambert
     quads (five walls split 2 x 2, and the +x wall made of the 4 quads that
-    frame a 0.05 x 0.5 slit), an exterior 0.6 x 0.6 quad light of radiance
-    200 facing the slit, and 32 GGX-conductor icospheres (alpha U[0.1, 0.5])."""
+    frame a 0.05 x 0.5 slit), an exterior quad light of radiance 200 facing
+    the slit (4 x 4, 2 units outside the wall: only a sliver of it is visible
+    through the slit from inside), and 32 GGX-conductor icospheres (alpha
+    U[0.1, 0.5])."""
     rng = np.random.default_rng(seed)
     d = SceneDesc(width=width, height=height, spp=spp, max_depth=max_depth)
     d.materials = [api.material([api.diffuse((0.7, 0.7, 0.7))])]
@@ -286,7 +289,8 @@ def slit_room_scene(width=1024, height=1024, spp=16, max_depth=10, n_spheres=32,
         d.add(v, i, WALL)
     light = api.material([], Le=(200.0, 200.0, 200.0))
     d.materials.append(light)
-    v, i = quad((1.3, 0.2, 0.2), (0, 0, 0.6), (0, 0.6, 0))  # faces -x, toward the slit
+    h = 0.5 * light_size  # centred on the slit, light_dist outside the wall, facing -x
+    v, i = quad((1.0 + light_dist, 0.5 - h, 0.5 - h), (0, 0, light_size), (0, light_size, 0))
     d.add(v, i, len(d.materials) - 1, is_light=True)
     sv, sf = icosphere(2)
     for _ in range(n_spheres):

@@ -80,25 +80,28 @@ def rel_mse(img, ref, eps=1e-2):
     return float(np.mean((np.asarray(img, np.float64) - ref) ** 2 / (ref ** 2 + eps)))
 
 
+R = 64
+
+
 @pytest.fixture(scope="module")
 def slit():
-    d = scenes.slit_room_scene(48, 48, spp=16, max_depth=10, n_spheres=32)
+    d = scenes.slit_room_scene(R, R, spp=16, max_depth=10, n_spheres=32)
     s = d.build()
-    ref = api.Renderer(spp=16384, max_depth=10, seed=99).render(s, d.camera, 48, 48, fp64=True)[1]
+    ref = api.Renderer(spp=16384, max_depth=10, seed=99).render(s, d.camera, R, R, fp64=True)[1]
     return d, s, ref
 
 
 def test_guided_render_is_unbiased(gpu, slit):
     d, s, ref = slit
     g = api.Guide(seed=4)
-    img, _, st, gst = api.render_guided(s, g, d.camera, 48, 48, spp=512, max_depth=10, seed=5,
+    img, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=512, max_depth=10, seed=5,
                                         gcfg=api.guide_config(spp_per_pass=8))
     assert gst["spp_done"] == 512 and gst["train_steps"] > 0 and np.isfinite(img).all()
     # image mean within 3 % of the 16,384-spp plain reference
     assert abs(img.mean() / ref.mean() - 1) < 0.03, (img.mean(), ref.mean())
     # a frozen, untrained network also stays unbiased
     g2 = api.Guide(seed=6)
-    img2, _, _, gst2 = api.render_guided(s, g2, d.camera, 48, 48, spp=512, max_depth=10, seed=8,
+    img2, _, _, gst2 = api.render_guided(s, g2, d.camera, R, R, spp=512, max_depth=10, seed=8,
                                          gcfg=api.guide_config(train=False))
     assert gst2["train_steps"] == 0
     assert abs(img2.mean() / ref.mean() - 1) < 0.03, (img2.mean(), ref.mean())
@@ -109,13 +112,14 @@ def test_trained_guide_reduces_error(gpu, slit):
     rendering of the narrow-aperture scene has lower relMSE than plain."""
     d, s, ref = slit
     g = api.Guide(seed=9)
-    api.render_guided(s, g, d.camera, 48, 48, spp=512, max_depth=10, seed=1,
-                      gcfg=api.guide_config(spp_per_pass=8, learning_rate=2e-3))
+    _, _, _, gst = api.render_guided(s, g, d.camera, R, R, spp=4096, max_depth=10, seed=1,
+                                     gcfg=api.guide_config(spp_per_pass=4, learning_rate=1e-2))
+    assert gst["train_steps"] == 1024
     errs_g, errs_p = [], []
     for k in range(4):
-        gi, _, _, _ = api.render_guided(s, g, d.camera, 48, 48, spp=64, max_depth=10, seed=100 + k,
-                                        gcfg=api.guide_config(train=False))
-        pi = api.Renderer(spp=64, max_depth=10, seed=200 + k).render(s, d.camera, 48, 48)
+        gi, _, _, _ = api.render_guided(s, g, d.camera, R, R, spp=64, max_depth=10, seed=100 + k,
+                                        gcfg=api.guide_config(train=False, spp_per_pass=64))
+        pi = api.Renderer(spp=64, max_depth=10, seed=200 + k).render(s, d.camera, R, R)
         errs_g.append(rel_mse(gi, ref))
         errs_p.append(rel_mse(pi, ref))
-    assert np.mean(errs_g) < 0.8 * np.mean(errs_p), (errs_g, errs_p)
+    assert np.mean(errs_g) < 0.75 * np.mean(errs_p), (errs_g, errs_p)
