@@ -236,7 +236,7 @@ def traversal_bench(steps, warmup):
 
 
 # ---------------------------------------------------------------- learned guiding, equal time
-def guiding_bench(R=256, plain_spp=2048, ref_spp=32768, max_depth=10):
+def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
     """Narrow-aperture slit room at R x R: relMSE against a plain FP64
     reference of ref_spp, plain path tracing for plain_spp vs guided path
     tracing (network trained online from scratch, inside the same wall-clock
@@ -265,7 +265,7 @@ def guiding_bench(R=256, plain_spp=2048, ref_spp=32768, max_depth=10):
     t0 = time.perf_counter()
     img_g, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=1 << 20, max_depth=max_depth, seed=7,
                                           gcfg=api.guide_config(spp_per_pass=4, learning_rate=1e-2,
-                                                                max_train_steps=512, time_budget_ms=T * 1e3))
+                                                                max_train_steps=256, time_budget_ms=T * 1e3))
     Tg = time.perf_counter() - t0
     e_guided = rel_mse(img_g, ref)
     img_f, _, _, _ = api.render_guided(s, g, d.camera, R, R, spp=plain_spp, max_depth=max_depth, seed=11,

@@ -250,14 +250,27 @@ kz_status alloc_paths(DevBuf* b, uint32_t cap, kz::PathSoA& p) {
 
 // Wavefront path tracing of `total` paths; contributions are summed into
 // film (and film64) on the device.
+// Guiding hooks of the wavefront loop (null for plain rendering).
+struct GuideHooks {
+    const kz::GuideShade* gs = nullptr;
+    kz::GuideDev gd;
+    float* raw = nullptr;
+};
+
+// Wavefront path tracing of `total` paths, driven by device-side counters:
+// the host enqueues batches of iterations (plan, generate, trace, [infer],
+// shade, shadow, finish) and synchronises once per batch. Contributions are
+// summed into film (and film64) on the device.
 kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* rays_dev, uint64_t total,
-                        const kz_render_config* cfg, float* film, double* film64, kz_render_stats* stats) {
+                        const kz_render_config* cfg, float* film, double* film64, kz_render_stats* stats,
+                        const kz::PathParams* pp_override = nullptr, const GuideHooks* gh = nullptr) {
     kz::PathParams pp;
     pp.spp = cam ? cfg->spp : 1u;
     pp.max_depth = cfg->max_depth;
     pp.rr_min = cfg->rr_min_depth;
     pp.seed = cfg->seed;
     pp.camera = cam ? 1u : 0u;
+    if (pp_override) pp = *pp_override;
     uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
     const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(want, total), 1u << 30));
     const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
@@ -269,74 +282,84 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
     kz::ShadowSoA sq{s->sh[0].as<float4>(), s->sh[1].as<float4>(), s->sh[2].as<float4>()};
     KZ_TRY(s->ctr.ensure(sizeof(kz::DevCounters)));
     kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
-    KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), s->stream));
-    kz_render_stats st{};
-    st.paths = total;
-    uint64_t next = 0;
-    uint32_t nA = 0;
     cudaStream_t strm = s->stream;
+    {
+        kz::DevCounters init{};
+        init.total = total;
+        *s->ctr_host = init;
+        KZ_CUDA(cudaMemcpyAsync(ctr, s->ctr_host, sizeof(kz::DevCounters), cudaMemcpyHostToDevice, strm));
+    }
     const bool timing = (cfg->flags & KZ_RENDER_FLAG_TIMING) != 0;
     const bool count = (cfg->flags & KZ_RENDER_FLAG_COUNT) != 0;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    if (timing)
-        for (auto& e : ev) KZ_CUDA(cudaEventCreate(&e));
+    // one batch covers the life of one wave of paths
+    const uint32_t batch = std::max<uint32_t>(4, cfg->max_depth + 1);
+    std::vector<cudaEvent_t> ev;
+    if (timing) {
+        ev.assign(5 * (size_t)batch, nullptr);
+        for (auto& e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                for (auto& f : ev)
+                    if (f) cudaEventDestroy(f);
+                return fail(KZ_ERR_CUDA, "cudaEventCreate failed");
+            }
+    }
     struct EvGuard {
-        cudaEvent_t* e;
+        std::vector<cudaEvent_t>& e;
         ~EvGuard() {
-            for (int k = 0; k < 5; ++k)
-                if (e[k]) cudaEventDestroy(e[k]);
+            for (auto& x : e)
+                if (x) cudaEventDestroy(x);
         }
     } guard{ev};
-    auto mark = [&](int k) -> kz_status {
-        if (timing) KZ_CUDA(cudaEventRecord(ev[k], strm));
-        return KZ_OK;
-    };
+    kz_render_stats st{};
+    st.paths = total;
     for (;;) {
-        const uint32_t n_new = (uint32_t)std::min<uint64_t>(cap - nA, total - next);
-        KZ_TRY(mark(0));
-        if (n_new) {
-            if (cam) kz::launch_generate_camera(*cam, pp, A, nA, next, n_new, block, strm);
-            else kz::launch_generate_rays(rays_dev, pp, A, nA, next, n_new, block, strm);
-            st.kernel_launches += 1;
-            nA += n_new;
-            next += n_new;
+        for (uint32_t it = 0; it < batch; ++it) {
+            cudaEvent_t* e = timing ? &ev[5 * (size_t)it] : nullptr;
+            if (e) KZ_CUDA(cudaEventRecord(e[0], strm));
+            kz::launch_plan(ctr, cap, strm);
+            if (cam) kz::launch_generate_camera_dev(*cam, pp, A, ctr, cap, block, strm);
+            else kz::launch_generate_rays_dev(rays_dev, pp, A, ctr, cap, block, strm);
+            if (e) KZ_CUDA(cudaEventRecord(e[1], strm));
+            kz::launch_trace_paths_dev(s->dev, A, cap, ctr, count, block, strm);
+            if (gh) kz::launch_guide_infer_paths_dev(s->dev, A, cap, ctr, gh->gd, gh->raw, strm);
+            if (e) KZ_CUDA(cudaEventRecord(e[2], strm));
+            kz::launch_shade_dev(s->dev, pp, A, cap, B, sq, ctr, film, film64, gh ? gh->gs : nullptr, block, strm);
+            if (e) KZ_CUDA(cudaEventRecord(e[3], strm));
+            if (gh)
+                kz::launch_trace_shadow_guided(s->dev, sq, cap, ctr, film, film64, gh->gs->recs, gh->gs->nee,
+                                               pp.max_depth, block, strm);
+            else
+                kz::launch_trace_shadow(s->dev, sq, cap, ctr, count, film, film64, block, strm);
+            kz::launch_finish(ctr, strm);
+            if (e) KZ_CUDA(cudaEventRecord(e[4], strm));
+            st.kernel_launches += gh ? 7 : 6;
+            std::swap(A, B);
         }
-        if (nA == 0) break;
-        KZ_TRY(mark(1));
-        kz::launch_trace_paths(s->dev, A, nA, ctr, count, block, strm);
-        KZ_TRY(mark(2));
-        KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
-        kz::launch_shade(s->dev, pp, A, nA, B, sq, ctr, film, film64, block, strm);
-        KZ_TRY(mark(3));
-        kz::launch_trace_shadow(s->dev, sq, nA, ctr, count, film, film64, block, strm);
-        KZ_TRY(mark(4));
-        st.kernel_launches += 3;
+        KZ_CUDA(cudaGetLastError());
         KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
         KZ_CUDA(cudaStreamSynchronize(strm));
-        KZ_CUDA(cudaGetLastError());
-        if (timing) {
-            float ms[4];
-            for (int k = 0; k < 4; ++k) KZ_CUDA(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
-            st.generate_ms += ms[0];
-            st.trace_ms += ms[1];
-            st.shade_ms += ms[2];
-            st.shadow_ms += ms[3];
-        }
-        st.path_bounces += nA;
-        st.shadow_rays += s->ctr_host->n_shadow;
-        st.iterations += 1;
-        if (s->ctr_host->status) {
-            uint32_t code = s->ctr_host->status;
-            return fail((kz_status)code, "device status %u during rendering", code);
-        }
-        nA = s->ctr_host->n_next;
-        std::swap(A, B);
+        if (timing)
+            for (uint32_t it = 0; it < batch; ++it) {
+                float ms[4];
+                for (int k = 0; k < 4; ++k) KZ_CUDA(cudaEventElapsedTime(&ms[k], ev[5 * it + k], ev[5 * it + k + 1]));
+                st.generate_ms += ms[0];
+                st.trace_ms += ms[1];
+                st.shade_ms += ms[2];
+                st.shadow_ms += ms[3];
+            }
+        const kz::DevCounters& hc = *s->ctr_host;
+        if (hc.status) return fail((kz_status)hc.status, "device status %u during rendering", hc.status);
+        if (hc.n_active == 0 && hc.next_path >= hc.total) break;
     }
+    const kz::DevCounters& hc = *s->ctr_host;
+    st.path_bounces = hc.path_bounces;
+    st.shadow_rays = hc.shadow_rays;
+    st.iterations = hc.iterations;
     if (count) {
-        st.closest_node_fetches = s->ctr_host->fetch[0];
-        st.closest_tri_fetches = s->ctr_host->fetch[1];
-        st.shadow_node_fetches = s->ctr_host->fetch[2];
-        st.shadow_tri_fetches = s->ctr_host->fetch[3];
+        st.closest_node_fetches = hc.fetch[0];
+        st.closest_tri_fetches = hc.fetch[1];
+        st.shadow_node_fetches = hc.fetch[2];
+        st.shadow_tri_fetches = hc.fetch[3];
     }
     if (stats) *stats = st;
     return KZ_OK;
@@ -1109,6 +1132,7 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     const uint64_t npix = (uint64_t)fd->width * fd->height;
     const uint64_t per_pass = npix * gc.spp_per_pass;
     if (per_pass > (1ull << 28)) return fail(KZ_ERR_INVALID_ARG, "width*height*spp_per_pass must be <= 2^28");
+    const uint64_t max_pass_paths = std::max<uint64_t>(per_pass, 1ull << 24);
     kz::DevCamera cam;
     KZ_TRY(make_camera(camera, fd->width, fd->height, cam));
     cudaStream_t strm = s->stream;
@@ -1130,13 +1154,6 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, per_pass));
     const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
     if (block % 32 != 0 || block > 1024) return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
-    kz::PathSoA A, B;
-    KZ_TRY(alloc_paths(s->pa, cap, A));
-    KZ_TRY(alloc_paths(s->pb, cap, B));
-    for (int k = 0; k < 3; ++k) KZ_TRY(s->sh[k].ensure((size_t)cap * sizeof(float4)));
-    kz::ShadowSoA sq{s->sh[0].as<float4>(), s->sh[1].as<float4>(), s->sh[2].as<float4>()};
-    KZ_TRY(s->ctr.ensure(sizeof(kz::DevCounters)));
-    kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
     const uint64_t n_recs = per_pass * cfg->max_depth;
     KZ_TRY(g->recs.ensure(n_recs * sizeof(kz::VRec)));
     KZ_TRY(g->nee.ensure(n_recs * sizeof(kz::NRec)));
@@ -1152,9 +1169,13 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     uint64_t spp_done = 0;
     uint32_t pass = 0;
     while (spp_done < cfg->spp) {
-        const uint32_t spp_pass = (uint32_t)std::min<uint64_t>(gc.spp_per_pass, cfg->spp - spp_done);
-        const uint64_t total = npix * spp_pass;
         const bool train = gc.train && (gc.max_train_steps == 0 || gs.train_steps < gc.max_train_steps);
+        // once the network is frozen, passes only bound the time budget's
+        // granularity: render them larger (up to 64 spp, within the buffers)
+        uint64_t want_spp = gc.spp_per_pass;
+        if (!train) want_spp = std::max<uint64_t>(want_spp, std::min<uint64_t>(64, max_pass_paths / npix));
+        const uint32_t spp_pass = (uint32_t)std::min<uint64_t>(want_spp, cfg->spp - spp_done);
+        const uint64_t total = npix * spp_pass;
         kz::PathParams pp;
         pp.spp = spp_pass;
         pp.max_depth = cfg->max_depth;
@@ -1165,43 +1186,25 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
             KZ_CUDA(cudaMemsetAsync(recs, 0, total * cfg->max_depth * sizeof(kz::VRec), strm));
             KZ_CUDA(cudaMemsetAsync(nee, 0, total * cfg->max_depth * sizeof(kz::NRec), strm));
         }
-        KZ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(kz::DevCounters), strm));
         kz::GuideShade gsh;
         gsh.raw = g->raw.as<float>();
         gsh.recs = train ? recs : nullptr;
         gsh.nee = train ? nee : nullptr;
         gsh.pass_first = 0;
         gsh.alpha = gc.alpha;
-        uint64_t next = 0;
-        uint32_t nA = 0;
-        for (;;) {
-            const uint32_t n_new = (uint32_t)std::min<uint64_t>(cap - nA, total - next);
-            if (n_new) {
-                kz::launch_generate_camera(cam, pp, A, nA, next, n_new, block, strm);
-                st.kernel_launches += 1;
-                nA += n_new;
-                next += n_new;
-            }
-            if (nA == 0) break;
-            kz::launch_trace_paths(s->dev, A, nA, ctr, false, block, strm);
-            kz::launch_guide_infer_paths(s->dev, A, nA, gdev, g->raw.as<float>(), strm);
-            KZ_CUDA(cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), strm));
-            kz::launch_shade_guided(s->dev, pp, A, nA, B, sq, ctr, film, film64, gsh, block, strm);
-            kz::launch_trace_shadow_guided(s->dev, sq, nA, ctr, film, film64, gsh.recs, gsh.nee, cfg->max_depth,
-                                           block, strm);
-            st.kernel_launches += 4;
-            KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
-            KZ_CUDA(cudaStreamSynchronize(strm));
-            KZ_CUDA(cudaGetLastError());
-            st.path_bounces += nA;
-            st.shadow_rays += s->ctr_host->n_shadow;
-            st.iterations += 1;
-            if (s->ctr_host->status)
-                return fail((kz_status)s->ctr_host->status, "device status %u during guided rendering",
-                            s->ctr_host->status);
-            nA = s->ctr_host->n_next;
-            std::swap(A, B);
-        }
+        GuideHooks hooks;
+        hooks.gs = &gsh;
+        hooks.gd = gdev;
+        hooks.raw = g->raw.as<float>();
+        kz_render_config pcfg = *cfg;
+        pcfg.spp = spp_pass;
+        pcfg.wavefront_size = cap;
+        kz_render_stats pst{};
+        KZ_TRY(run_wavefront(s, &cam, nullptr, total, &pcfg, film, film64, &pst, &pp, &hooks));
+        st.path_bounces += pst.path_bounces;
+        st.shadow_rays += pst.shadow_rays;
+        st.iterations += pst.iterations;
+        st.kernel_launches += pst.kernel_launches;
         st.paths += total;
         spp_done += spp_pass;
         pass += 1;

@@ -117,8 +117,13 @@ struct DevCounters {
     uint32_t n_next;     // continuing paths written by shade
     uint32_t n_shadow;   // shadow rays queued by shade
     uint32_t status;     // device-side error (KZ_ERR_STACK ...)
-    uint32_t pad;
+    uint32_t n_active;   // paths in the current buffer (device-driven loop)
     unsigned long long fetch[4];  // closest nodes, closest tris, shadow nodes, shadow tris
+    // device-driven loop: path ids [0, total) are generated in order
+    unsigned long long next_path, total;
+    unsigned long long path_bounces, shadow_rays, iterations;
+    unsigned long long gen_first;  // first path id generated this iteration
+    uint32_t gen_count, gen_slot;  // how many, and where in the buffer
 };
 
 // ---- launchers (kz_kernels.cu) -------------------------------------------
@@ -170,5 +175,23 @@ void launch_guide_to_bf16(const float* w, __nv_bfloat16* wbf, cudaStream_t st);
 void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
                          float* film, double* film64, uint32_t block, cudaStream_t st);
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st);
+
+// Device-driven wavefront: one iteration = plan, generate, trace, [infer],
+// shade, shadow, finish; every count lives in DevCounters, so the host can
+// enqueue many iterations between synchronisations. Grids are sized for the
+// capacity `cap`; threads beyond the device-side count exit.
+void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st);
+void launch_finish(DevCounters* ctr, cudaStream_t st);
+void launch_generate_camera_dev(const DevCamera& cam, const PathParams& pp, PathSoA dst, DevCounters* ctr,
+                                uint32_t cap, uint32_t block, cudaStream_t st);
+void launch_generate_rays_dev(const kz_ray* rays, const PathParams& pp, PathSoA dst, DevCounters* ctr, uint32_t cap,
+                              uint32_t block, cudaStream_t st);
+void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t block,
+                            cudaStream_t st);
+void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq,
+                      DevCounters* ctr, float* film, double* film64, const GuideShade* gs, uint32_t block,
+                      cudaStream_t st);
+void launch_guide_infer_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, const DevCounters* ctr,
+                                  const GuideDev& gd, float* raw, cudaStream_t st);
 
 }  // namespace kz

@@ -136,11 +136,8 @@ __global__ void k_closure_sample(const kz_lobe* __restrict__ lobes, const float*
 }
 
 // ------------------------------------------------------------------ wavefront stages
-__global__ void k_generate_camera(DevCamera cam, PathParams pp, PathSoA dst, uint32_t dst_offset,
-                                  uint64_t first_path, uint32_t n_new) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_new) return;
-    const uint64_t pid = first_path + j;
+__device__ __forceinline__ void generate_camera_path(const DevCamera& cam, const PathParams& pp, PathSoA dst,
+                                                     uint32_t k, uint64_t pid) {
     const uint64_t pix = pid / pp.spp;
     const uint32_t px = (uint32_t)(pix % cam.W), py = (uint32_t)(pix / cam.W);
     Pcg rng;
@@ -155,26 +152,35 @@ __global__ void k_generate_camera(DevCamera cam, PathParams pp, PathSoA dst, uin
     const float cx = nx * cam.tan_half;
     const float cy = ny * cam.tan_half;
     const f3 d = normalize(ld3(cam.x) * cx + ld3(cam.y) * cy + ld3(cam.z) * (-1.0f));
-    const uint32_t k = dst_offset + j;
     dst.o4[k] = make_float4(cam.eye[0], cam.eye[1], cam.eye[2], 0.f);
     dst.d4[k] = make_float4(d.x, d.y, d.z, __uint_as_float(kSpecularFlag));
     dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
     dst.rng[k] = rng.state;
 }
 
-__global__ void k_generate_rays(const kz_ray* __restrict__ rays, PathParams pp, PathSoA dst, uint32_t dst_offset,
-                                uint64_t first_path, uint32_t n_new) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_new) return;
-    const uint64_t pid = first_path + j;
+__device__ __forceinline__ void generate_ray_path(const kz_ray* __restrict__ rays, const PathParams& pp, PathSoA dst,
+                                                  uint32_t k, uint64_t pid) {
     Pcg rng;
     rng.seed(pp.seed, pid);
     const kz_ray r = rays[pid];
-    const uint32_t k = dst_offset + j;
     dst.o4[k] = make_float4(r.ox, r.oy, r.oz, 0.f);
     dst.d4[k] = make_float4(r.dx, r.dy, r.dz, __uint_as_float(kSpecularFlag));
     dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
     dst.rng[k] = rng.state;
+}
+
+__global__ void k_generate_camera(DevCamera cam, PathParams pp, PathSoA dst, uint32_t dst_offset,
+                                  uint64_t first_path, uint32_t n_new) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_new) return;
+    generate_camera_path(cam, pp, dst, dst_offset + j, first_path + j);
+}
+
+__global__ void k_generate_rays(const kz_ray* __restrict__ rays, PathParams pp, PathSoA dst, uint32_t dst_offset,
+                                uint64_t first_path, uint32_t n_new) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_new) return;
+    generate_ray_path(rays, pp, dst, dst_offset + j, first_path + j);
 }
 
 // Sums two per-thread counters over the warp; one 64-bit atomic each.
@@ -191,8 +197,10 @@ __device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint32_t n, DevCounters* ctr) {
+__global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint32_t n, DevCounters* ctr,
+                                                     const uint32_t* n_dev) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = *n_dev;
     uint32_t dn = 0, dt = 0;
     if (i < n) {
         const float4 o = p.o4[i], d = p.d4[i];
@@ -269,8 +277,9 @@ __device__ __forceinline__ void propagate(VRec* recs, uint64_t rbase, uint32_t d
 template <bool kGuided>
 __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
-                                               GuideShade gs) {
+                                               GuideShade gs, const uint32_t* n_dev) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n_in = *n_dev;
     bool cont = false, shadow = false;
     float4 o_next, d_next, b_next, s_o, s_d, s_c;
     unsigned long long rng_next = 0;
@@ -596,6 +605,42 @@ __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __res
     }
 }
 
+// ------------------------------------------------------------------ device-driven loop
+__global__ void k_plan(DevCounters* c, uint32_t cap) {
+    const uint64_t remaining = c->total - c->next_path;
+    const uint32_t room = cap - c->n_active;
+    const uint32_t n_new = (uint32_t)(remaining < room ? remaining : room);
+    c->gen_first = c->next_path;
+    c->gen_count = n_new;
+    c->gen_slot = c->n_active;
+    c->next_path += n_new;
+    c->n_active += n_new;
+    c->n_next = 0;
+    c->n_shadow = 0;
+    if (c->n_active) {
+        c->iterations += 1;
+        c->path_bounces += c->n_active;
+    }
+}
+
+__global__ void k_finish(DevCounters* c) {
+    c->shadow_rays += c->n_shadow;
+    c->n_active = c->n_next;
+}
+
+__global__ void k_generate_camera_dev(DevCamera cam, PathParams pp, PathSoA dst, const DevCounters* c) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= c->gen_count) return;
+    generate_camera_path(cam, pp, dst, c->gen_slot + j, c->gen_first + j);
+}
+
+__global__ void k_generate_rays_dev(const kz_ray* __restrict__ rays, PathParams pp, PathSoA dst,
+                                    const DevCounters* c) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= c->gen_count) return;
+    generate_ray_path(rays, pp, dst, c->gen_slot + j, c->gen_first + j);
+}
+
 __global__ void k_scale(float* film, double* film64, uint64_t n, float sf, double sd) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -645,20 +690,49 @@ void launch_generate_rays(const kz_ray* rays, const PathParams& pp, PathSoA dst,
 void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* ctr, bool count, uint32_t block,
                         cudaStream_t st) {
     if (!n) return;
-    if (count) k_trace_paths<true><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr);
-    else k_trace_paths<false><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr);
+    if (count) k_trace_paths<true><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
+    else k_trace_paths<false><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
+}
+void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t block,
+                            cudaStream_t st) {
+    if (!cap) return;
+    if (count) k_trace_paths<true><<<grid_for(cap, block), block, 0, st>>>(s, p, cap, ctr, &ctr->n_active);
+    else k_trace_paths<false><<<grid_for(cap, block), block, 0, st>>>(s, p, cap, ctr, &ctr->n_active);
+}
+void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st) { k_plan<<<1, 1, 0, st>>>(ctr, cap); }
+void launch_finish(DevCounters* ctr, cudaStream_t st) { k_finish<<<1, 1, 0, st>>>(ctr); }
+void launch_generate_camera_dev(const DevCamera& cam, const PathParams& pp, PathSoA dst, DevCounters* ctr,
+                                uint32_t cap, uint32_t block, cudaStream_t st) {
+    if (!cap) return;
+    k_generate_camera_dev<<<grid_for(cap, block), block, 0, st>>>(cam, pp, dst, ctr);
+}
+void launch_generate_rays_dev(const kz_ray* rays, const PathParams& pp, PathSoA dst, DevCounters* ctr, uint32_t cap,
+                              uint32_t block, cudaStream_t st) {
+    if (!cap) return;
+    k_generate_rays_dev<<<grid_for(cap, block), block, 0, st>>>(rays, pp, dst, ctr);
+}
+void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq,
+                      DevCounters* ctr, float* film, double* film64, const GuideShade* gs, uint32_t block,
+                      cudaStream_t st) {
+    if (!cap) return;
+    if (gs)
+        k_shade<true><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64, *gs,
+                                                              &ctr->n_active);
+    else
+        k_shade<false><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64,
+                                                               GuideShade{}, &ctr->n_active);
 }
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
                   DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
     if (!n_in) return;
     k_shade<false><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
-                                                            GuideShade{});
+                                                            GuideShade{}, nullptr);
 }
 void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
                          ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
                          uint32_t block, cudaStream_t st) {
     if (!n_in) return;
-    k_shade<true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64, gs);
+    k_shade<true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64, gs, nullptr);
 }
 void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
                                 double* film64, VRec* recs, NRec* nee, uint32_t max_depth, uint32_t block,

@@ -150,8 +150,11 @@ __device__ __forceinline__ void forward_tile(const SmemW& s, const float* __rest
 // record). raw[i*40 ..] = network outputs.
 template <bool kPaths>
 __global__ void __launch_bounds__(128) k_guide_infer(DevScene sc, PathSoA ps, const float4* __restrict__ pts,
-                                                     uint32_t n, GuideDev gd, float* __restrict__ raw) {
+                                                     uint32_t n, GuideDev gd, float* __restrict__ raw,
+                                                     const uint32_t* n_dev) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (n_dev) n = *n_dev;
+    if ((n + 15) / 16 <= blockIdx.x * (blockDim.x >> 5)) return;  // no tile for this CTA
     SmemW s;
     stage_weights(gd.wbf, reinterpret_cast<__nv_bfloat16*>(smem_raw), false, s);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -468,7 +471,15 @@ void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const Gu
     if (!n) return;
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
-    k_guide_infer<true><<<grid, 128, kSmemInfer, st>>>(s, p, nullptr, n, gd, raw);
+    k_guide_infer<true><<<grid, 128, kSmemInfer, st>>>(s, p, nullptr, n, gd, raw, nullptr);
+}
+
+void launch_guide_infer_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, const DevCounters* ctr,
+                                  const GuideDev& gd, float* raw, cudaStream_t st) {
+    if (!cap) return;
+    const uint32_t tiles = (cap + 15) / 16;
+    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
+    k_guide_infer<true><<<grid, 128, kSmemInfer, st>>>(s, p, nullptr, cap, gd, raw, &ctr->n_active);
 }
 
 void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd, float* raw, cudaStream_t st) {
@@ -477,7 +488,7 @@ void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd
     PathSoA np{};
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
-    k_guide_infer<false><<<grid, 128, kSmemInfer, st>>>(none, np, pts, n, gd, raw);
+    k_guide_infer<false><<<grid, 128, kSmemInfer, st>>>(none, np, pts, n, gd, raw, nullptr);
 }
 
 void launch_guide_train(const float4* samples, uint32_t count, uint32_t n, uint32_t stride, uint32_t offset,
