@@ -310,6 +310,44 @@ kz_status kz_render_guided(kz_scene* scene, kz_guide* guide, const kz_camera* ca
                            const kz_guide_config* gcfg, float* out_rgb, double* out_rgb64,
                            int32_t mem, kz_render_stats* out_stats, kz_guide_stats* out_gstats);
 
+/* ---- batched rendering ------------------------------------------------------
+ * Many independent jobs (each its own scene, camera, film, spp and depth) in
+ * one persistent kernel launch, optionally captured in a CUDA graph: lanes
+ * keep a path each and refill from a global path counter every
+ * refill_period vertices. Not in the reference (its renderer runs one scene
+ * at a time, src/core/renderer.cpp:18-90); every job's film equals what
+ * kz_render produces for it (same PCG32 streams). All scenes must be built
+ * on the same device; the call runs on the first job's scene stream. */
+typedef struct kz_batch_job {
+    kz_scene* scene;
+    kz_camera camera;
+    uint32_t  width, height;
+    uint32_t  spp, max_depth, rr_min_depth;
+    uint64_t  seed;
+    float*    out_rgb;          /* width*height*3 floats, spp average */
+} kz_batch_job;
+
+typedef struct kz_batch_config {
+    uint32_t block_size;        /* threads per block (0 = 128)               */
+    uint32_t ctas_per_sm;       /* resident blocks per SM (0 = 2)            */
+    uint32_t refill_period;     /* vertices between lane refills (0 = 1)     */
+    uint32_t use_graph;         /* 1: launch through a captured CUDA graph   */
+} kz_batch_config;
+
+typedef struct kz_batch_stats {
+    uint64_t paths;
+    uint64_t path_bounces;
+    uint64_t shadow_rays;
+    uint64_t threads;           /* persistent lanes (the wavefront in flight) */
+    double   device_ms;         /* CUDA-event time of the launch (graph)      */
+} kz_batch_stats;
+
+kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, const kz_batch_config* cfg,
+                          int32_t mem, kz_batch_stats* out_stats);
+/* Frees the scene's cached render scratch (wavefront buffers, staging);
+ * geometry, BVH and materials stay. */
+kz_status kz_scene_release_scratch(kz_scene* scene);
+
 /* ---- Li batch that allocates nothing -------------------------------------
  * No counterpart in the reference: kazen_proto has no device path of its own.
  * Same result as kz_li_batch with KZ_MEM_DEVICE, for callers that cannot call

@@ -102,6 +102,22 @@ class KzGuideStats(C.Structure):
 KZ_GUIDE_PARAMS = 15080
 
 
+class KzBatchJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", KzCamera), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("spp", C.c_uint32), ("max_depth", C.c_uint32), ("rr_min_depth", C.c_uint32), ("seed", C.c_uint64),
+                ("out_rgb", C.c_void_p)]
+
+
+class KzBatchConfig(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("refill_period", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+
+class KzBatchStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("path_bounces", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("threads", C.c_uint64), ("device_ms", C.c_double)]
+
+
 class KzSceneInfo(C.Structure):
     _fields_ = [("n_meshes", C.c_uint64), ("n_triangles", C.c_uint64), ("n_lights", C.c_uint64),
                 ("n_bvh_nodes", C.c_uint64), ("bvh_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64),
@@ -143,6 +159,9 @@ SIGNATURES = {
                               C.c_int32, C.POINTER(KzRenderStats)]),
     "kz_li_batch_noalloc": (C.c_int32, [_P, _P, C.c_uint64, C.POINTER(KzRenderConfig), _P,
                                         C.POINTER(KzRenderStats)]),
+    "kz_render_batch": (C.c_int32, [C.POINTER(KzBatchJob), C.c_uint32, C.POINTER(KzBatchConfig), C.c_int32,
+                                    C.POINTER(KzBatchStats)]),
+    "kz_scene_release_scratch": (C.c_int32, [_P]),
     "kz_guide_create": (C.c_int32, [C.POINTER(C.c_void_p), C.c_uint64]),
     "kz_guide_destroy": (C.c_int32, [_P]),
     "kz_guide_get_params": (C.c_int32, [_P, _P]),

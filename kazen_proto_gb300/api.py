@@ -216,6 +216,10 @@ class Scene:
     def synchronize(self) -> None:
         check(lib().kz_scene_synchronize(self._h))
 
+    def release_scratch(self) -> None:
+        """Free cached render scratch (wavefront buffers); the scene stays built."""
+        check(lib().kz_scene_release_scratch(self._h))
+
     # -- intersector ------------------------------------------------------
     def intersect(self, rays, want_uv=True, out=None):
         """Closest hits. numpy ray records -> numpy outputs; a CUDA float32
@@ -444,3 +448,34 @@ def render_guided(scene: Scene, guide: Guide, camera: Camera, width: int, height
                                  _ptr(img), _ptr(img64), N.KZ_MEM_HOST, C.byref(st), C.byref(gst)))
     return (img, img64, {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_},
             {k: getattr(gst, k) for k, _ in N.KzGuideStats._fields_})
+
+
+# ---------------------------------------------------------------- batched rendering
+def batch_config(block_size=0, ctas_per_sm=0, refill_period=0, use_graph=True) -> N.KzBatchConfig:
+    c = N.KzBatchConfig()
+    c.block_size = block_size
+    c.ctas_per_sm = ctas_per_sm
+    c.refill_period = refill_period
+    c.use_graph = 1 if use_graph else 0
+    return c
+
+
+def render_batch(jobs, cfg=None):
+    """jobs: list of dicts {scene, camera, width, height, spp, max_depth, seed[, rr_min_depth]}.
+    Returns (list of (H, W, 3) images, stats). One persistent launch for all jobs."""
+    arr = (N.KzBatchJob * len(jobs))()
+    outs = []
+    for k, j in enumerate(jobs):
+        img = np.empty((j["height"], j["width"], 3), np.float32)
+        outs.append(img)
+        a = arr[k]
+        a.scene = j["scene"].handle
+        a.camera = j["camera"].to_c()
+        a.width, a.height = j["width"], j["height"]
+        a.spp, a.max_depth = j["spp"], j["max_depth"]
+        a.rr_min_depth = j.get("rr_min_depth", 3)
+        a.seed = j.get("seed", 0)
+        a.out_rgb = img.ctypes.data
+    st = N.KzBatchStats()
+    check(lib().kz_render_batch(arr, len(jobs), C.byref(cfg or batch_config()), N.KZ_MEM_HOST, C.byref(st)))
+    return outs, {k: getattr(st, k) for k, _ in N.KzBatchStats._fields_}

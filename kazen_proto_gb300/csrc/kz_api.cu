@@ -1270,6 +1270,167 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
 
 }  // extern "C"
 
+
+// ---------------------------------------------------------------------------
+// Batched rendering: one persistent launch over many jobs.
+extern "C" kz_status kz_scene_release_scratch(kz_scene* s) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->cuda_ready) return KZ_OK;
+    KZ_CUDA(cudaSetDevice(s->device));
+    KZ_CUDA(cudaStreamSynchronize(s->stream));
+    DevBuf* all[] = {&s->s_rays, &s->s_t, &s->s_prim, &s->s_geom, &s->s_u, &s->s_v, &s->s_occ, &s->s_ctr,
+                     &s->film, &s->film64};
+    for (DevBuf* b : all) b->release();
+    for (auto& b : s->pa) b.release();
+    for (auto& b : s->pb) b.release();
+    for (auto& b : s->sh) b.release();
+    return KZ_OK;
+}
+
+extern "C" kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, const kz_batch_config* cfg_in,
+                                     int32_t mem, kz_batch_stats* out_stats) {
+    KZ_TRY(check_mem(mem));
+    if (n_jobs == 0) return KZ_OK;
+    if (!jobs) return fail(KZ_ERR_INVALID_ARG, "jobs is NULL");
+    kz_batch_config cfg = cfg_in ? *cfg_in : kz_batch_config{};
+    if (cfg.block_size == 0) cfg.block_size = 128;
+    if (cfg.ctas_per_sm == 0) cfg.ctas_per_sm = 2;
+    if (cfg.refill_period == 0) cfg.refill_period = 1;
+    if (cfg.block_size % 32 != 0 || cfg.block_size > 256)
+        return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32 and <= 256");
+    if (cfg.ctas_per_sm > 64) return fail(KZ_ERR_INVALID_ARG, "ctas_per_sm must be <= 64");
+    // lock every distinct scene once, in address order
+    std::vector<kz_scene*> scenes;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        if (!jobs[j].scene) return fail(KZ_ERR_INVALID_ARG, "job %u has no scene", j);
+        scenes.push_back(jobs[j].scene);
+    }
+    std::sort(scenes.begin(), scenes.end());
+    scenes.erase(std::unique(scenes.begin(), scenes.end()), scenes.end());
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (kz_scene* sc : scenes) locks.emplace_back(sc->mu);
+    for (kz_scene* sc : scenes) {
+        KZ_TRY(check_scene(sc));
+        if (sc->device != scenes[0]->device) return fail(KZ_ERR_INVALID_ARG, "scenes live on different devices");
+    }
+    kz_scene* s0 = jobs[0].scene;
+    KZ_CUDA(cudaSetDevice(s0->device));
+    cudaStream_t st = s0->stream;
+
+    std::vector<kz::DevJob> dj(n_jobs);
+    std::vector<uint64_t> npix(n_jobs);
+    uint64_t total = 0, film_floats = 0;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const kz_batch_job& J = jobs[j];
+        if (J.width == 0 || J.height == 0 || J.spp == 0) return fail(KZ_ERR_INVALID_ARG, "job %u: empty film or spp", j);
+        if (J.max_depth == 0 || J.max_depth > 255) return fail(KZ_ERR_INVALID_ARG, "job %u: max_depth in [1, 255]", j);
+        if (!J.out_rgb) return fail(KZ_ERR_INVALID_ARG, "job %u: out_rgb is NULL", j);
+        npix[j] = (uint64_t)J.width * J.height;
+        const uint64_t paths = npix[j] * J.spp;
+        if (paths > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "job %u: width*height*spp must be < 2^32", j);
+        kz::DevJob& d = dj[j];
+        d.scene = J.scene->dev;
+        KZ_TRY(make_camera(&J.camera, J.width, J.height, d.cam));
+        d.pp.spp = J.spp;
+        d.pp.max_depth = J.max_depth;
+        d.pp.rr_min = J.rr_min_depth;
+        d.pp.seed = J.seed;
+        d.pp.camera = 1;
+        d.path_begin = total;
+        total += paths;
+        film_floats += npix[j] * 3;
+    }
+    // device films (the caller's when they are device pointers)
+    DevBuf films, djobs, ctrs;
+    std::vector<float*> fptr(n_jobs);
+    if (mem == KZ_MEM_HOST) {
+        KZ_TRY(films.ensure(film_floats * 4));
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < n_jobs; ++j) {
+            fptr[j] = films.as<float>() + off;
+            off += npix[j] * 3;
+        }
+    } else {
+        for (uint32_t j = 0; j < n_jobs; ++j) fptr[j] = jobs[j].out_rgb;
+    }
+    for (uint32_t j = 0; j < n_jobs; ++j) dj[j].film = fptr[j];
+    KZ_TRY(djobs.ensure(n_jobs * sizeof(kz::DevJob)));
+    KZ_TRY(ctrs.ensure(sizeof(kz::BatchCounters)));
+    KZ_CUDA(cudaMemcpyAsync(djobs.ptr, dj.data(), n_jobs * sizeof(kz::DevJob), cudaMemcpyHostToDevice, st));
+    int sms = 0;
+    KZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s0->device));
+    const uint32_t ctas = (uint32_t)sms * cfg.ctas_per_sm;
+    kz::BatchCounters* bc = ctrs.as<kz::BatchCounters>();
+
+    auto enqueue = [&]() -> kz_status {
+        KZ_CUDA(cudaMemsetAsync(bc, 0, sizeof(kz::BatchCounters), st));
+        for (uint32_t j = 0; j < n_jobs; ++j) KZ_CUDA(cudaMemsetAsync(fptr[j], 0, npix[j] * 12, st));
+        kz::launch_render_batch(djobs.as<kz::DevJob>(), n_jobs, total, bc, cfg.refill_period, ctas, cfg.block_size,
+                                st);
+        for (uint32_t j = 0; j < n_jobs; ++j)
+            kz::launch_scale(fptr[j], nullptr, npix[j] * 3, 1.0f / (float)jobs[j].spp, 0.0, st);
+        return KZ_OK;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KZ_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(KZ_ERR_CUDA, "cudaEventCreate failed");
+    }
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } evg{e0, e1};
+    if (cfg.use_graph) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        KZ_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        kz_status est = enqueue();
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (est != KZ_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return est;
+        }
+        if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+        KZ_CUDA(cudaEventRecord(e0, st));
+        ce = cudaGraphLaunch(exec, st);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e1, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        cudaGraphExecDestroy(exec);
+        if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce));
+    } else {
+        KZ_CUDA(cudaEventRecord(e0, st));
+        KZ_TRY(enqueue());
+        KZ_CUDA(cudaEventRecord(e1, st));
+        KZ_CUDA(cudaStreamSynchronize(st));
+    }
+    KZ_CUDA(cudaGetLastError());
+    kz::BatchCounters hb;
+    KZ_CUDA(cudaMemcpyAsync(&hb, bc, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    if (mem == KZ_MEM_HOST)
+        for (uint32_t j = 0; j < n_jobs; ++j)
+            KZ_CUDA(cudaMemcpyAsync(jobs[j].out_rgb, fptr[j], npix[j] * 12, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    if (hb.status) return fail((kz_status)hb.status, "device status %u during batched rendering", hb.status);
+    float ms = 0.f;
+    KZ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (out_stats) {
+        out_stats->paths = total;
+        out_stats->path_bounces = hb.path_bounces;
+        out_stats->shadow_rays = hb.shadow_rays;
+        out_stats->threads = (uint64_t)ctas * cfg.block_size;
+        out_stats->device_ms = ms;
+    }
+    return KZ_OK;
+}
+
 // ---------------------------------------------------------------------------
 // kz_li_batch_noalloc: the wavefront Li batch with its scratch in a static
 // device array instead of cudaMalloc'd buffers. Layout of the array for a

@@ -126,6 +126,21 @@ struct DevCounters {
     uint32_t gen_count, gen_slot;  // how many, and where in the buffer
 };
 
+// One job of a batched render: its scene, camera and film.
+struct DevJob {
+    DevScene scene;
+    DevCamera cam;
+    PathParams pp;
+    float* film;                     // W*H*3 sums
+    unsigned long long path_begin;   // first global path id of this job
+};
+
+struct BatchCounters {
+    unsigned long long next_path;    // global path fetch counter
+    unsigned long long path_bounces, shadow_rays;
+    uint32_t status, pad;
+};
+
 // ---- launchers (kz_kernels.cu) -------------------------------------------
 void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
                               uint32_t* status, cudaStream_t st);
@@ -191,6 +206,11 @@ void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCount
 void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq,
                       DevCounters* ctr, float* film, double* film64, const GuideShade* gs, uint32_t block,
                       cudaStream_t st);
+// Persistent batch renderer: grid = ctas blocks of `block` threads; each lane
+// keeps one path in registers and refills from the global counter every
+// `period` vertices (warp-aggregated fetch).
+void launch_render_batch(const DevJob* jobs, uint32_t n_jobs, unsigned long long total, BatchCounters* bc,
+                         uint32_t period, uint32_t ctas, uint32_t block, cudaStream_t st);
 void launch_guide_infer_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, const DevCounters* ctr,
                                   const GuideDev& gd, float* raw, cudaStream_t st);
 

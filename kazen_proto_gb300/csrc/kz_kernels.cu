@@ -274,273 +274,292 @@ __device__ __forceinline__ void propagate(VRec* recs, uint64_t rbase, uint32_t d
     }
 }
 
+struct ShadeOut {
+    bool cont = false, shadow = false;
+    float4 o_next, d_next, b_next, s_o, s_d, s_c;
+    unsigned long long rng_next = 0;
+    f3 Lsum = {0.f, 0.f, 0.f};  // contribution to the film pixel film_idx
+    uint32_t film_idx = 0;
+};
+
+// One shaded path vertex: emission, next-event estimation (the shadow ray is
+// returned, not traced), roulette and direction sampling. `raw` holds the
+// guiding network's outputs for this path (guided mode only).
+template <bool kGuided>
+__device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams& pp, const float4 hit,
+                                             const float4 o4, const float4 d4, const float4 b4,
+                                             unsigned long long rng_state, const GuideShade& gs, const float* raw,
+                                             ShadeOut& out) {
+    const int rec = __float_as_int(hit.w);
+    if (rec >= 0) {
+        const uint32_t pid = __float_as_uint(b4.w);
+        const uint32_t film_idx = pid / pp.spp;
+        const uint32_t flags = __float_as_uint(d4.w);
+        const uint32_t depth = flags & 0xffu;
+        const bool prev_spec = (flags & kSpecularFlag) != 0;
+        const float prev_pdf = o4.w;
+        Pcg rng;
+        rng.state = rng_state;
+        rng.inc = ((uint64_t)pid << 1u) | 1u;
+        float u[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
+
+        const float4* tp = s.tris + (size_t)rec * 3;
+        const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+        const uint32_t geom = __float_as_uint(tb.w);
+        const kz_material& mat = s.materials[__float_as_uint(tc.w)];
+        const f3 v0 = xyz(ta), v1 = xyz(tb), v2 = xyz(tc);
+        const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
+        const f3 d = xyz(d4);
+        const f3 P = xyz(o4) + d * hit.x;
+        const Frame fr(Ng);
+        const f3 wi = -fr.to_local(d);
+        f3 beta = xyz(b4);
+        f3 Lsum = mk(0.f, 0.f, 0.f);
+        const uint32_t nl = s.n_lights;
+        const uint64_t rbase = kGuided ? ((uint64_t)pid - gs.pass_first) * pp.max_depth : 0;
+
+        // 1. emission (front face only: single_emissive_surface)
+        const f3 Le = ld3(mat.Le);
+        if (!is_zero(Le) && dot(d, Ng) < 0.f) {
+            float w = 1.f;
+            if (!prev_spec) {
+                const int li = __ldg(s.geom_light + geom);
+                if (li >= 0) {
+                    const float cos_l = -dot(d, Ng);
+                    const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
+                    w = power_heuristic(prev_pdf, lpdf);
+                }
+            }
+            Lsum = Lsum + hmul(beta, Le) * w;
+            // MIS-weighted, like the next-event samples it pairs with
+            if (kGuided && gs.recs) propagate(gs.recs, rbase, depth, Lsum);
+        }
+
+        // lobe selection probabilities (CompositeClosure::compute_pdfs)
+        const uint32_t nlobes = min(mat.n_lobes, (uint32_t)KZ_MAX_LOBES);
+        float lp[KZ_MAX_LOBES];
+        const float winv = 1.f / (beta.x + beta.y + beta.z);
+        float wsum = 0.f;
+        bool any_smooth = false, any_delta = false;
+        for (uint32_t k = 0; k < nlobes; ++k) {
+            const kz_lobe& lb = mat.lobes[k];
+            lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
+            wsum += lp[k];
+            const bool dl = lobe_is_delta(lb.closure_id);
+            any_smooth |= !dl;
+            any_delta |= dl;
+        }
+        if (wsum > 0.f)
+            for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
+        const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
+        VmfMixture mix;
+        if (kGuided && guided) mixture_from_raw(raw, mix);
+        const float alpha = gs.alpha;
+
+        // 2. next-event estimation
+        if (nl > 0 && any_smooth && wsum > 0.f) {
+            const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
+            const DevLight lt = s.lights[li];
+            const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
+            const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
+            const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
+            const float su0 = sqrtf(u[2]);
+            const float bu0 = 1.f - su0;
+            const float bv0 = u[3] * su0;
+            const f3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+            const f3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+            const f3 lv = p - P;
+            const float dist2 = dot(lv, lv);
+            const float dist = sqrtf(dist2);
+            const f3 ldir = mk(lv.x / dist, lv.y / dist, lv.z / dist);
+            const float cos_l = -dot(ldir, nlgt);
+            if (cos_l > 0.f) {
+                const float pdf_solid = dist2 / (cos_l * lt.area);
+                const float lpdf = pdf_solid * (1.0f / (float)nl);
+                const f3 wo = fr.to_local(ldir);
+                f3 f = mk(0.f, 0.f, 0.f);
+                float bpdf = 0.f;
+                for (uint32_t k = 0; k < nlobes; ++k) {
+                    const kz_lobe& lb = mat.lobes[k];
+                    if (lobe_is_delta(lb.closure_id)) continue;
+                    const LobeEval e = lobe_eval(lb, wi, wo);
+                    f = f + hmul(ld3(lb.weight), e.f);
+                    bpdf += lp[k] * e.pdf;
+                }
+                if (kGuided && guided) bpdf = alpha * mixture_pdf(mix, ldir) + (1.f - alpha) * bpdf;
+                if (!is_zero(f)) {
+                    const float w = power_heuristic(lpdf, bpdf);
+                    const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
+                    out.shadow = true;
+                    out.s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
+                    out.s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
+                    const uint32_t tag =
+                        kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u)) : 0u;
+                    out.s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
+                    if (kGuided && gs.nee && guided) {
+                        // training sample: the light direction with its
+                        // MIS-weighted share of L*f*cos over the light pdf
+                        const f3 fl = hmul(f, ld3(lt.Le));
+                        const float wt = (0.2126f * fl.x + 0.7152f * fl.y + 0.0722f * fl.z) * (w / lpdf);
+                        const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
+                                            mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
+                        NRec& nr = gs.nee[rbase + depth];
+                        nr.p = make_float4(p01.x, p01.y, p01.z, wt);
+                        nr.n = make_float4(Ng.x, Ng.y, Ng.z, 0.f);
+                        nr.d = make_float4(ldir.x, ldir.y, ldir.z, 0.f);
+                    }
+                }
+            }
+        }
+
+        bool alive = depth + 1 < pp.max_depth;
+        // 3. Russian roulette (integrator.cpp:491-498)
+        if (alive && depth >= pp.rr_min) {
+            const float prob = fminf(max_comp(beta) * 0.9025f, 0.99f);
+            if (prob < u[4]) alive = false;
+            else beta = beta * (1.f / prob);
+        }
+        // 4. direction sampling
+        if (kGuided && guided && alive) {
+            // one-sample MIS of the learned vMF mixture and the BSDF mixture
+            f3 wo, wdir;
+            bool ok = true;
+            if (u[5] < alpha) {
+                wdir = mixture_sample(mix, u[5] / alpha, u[6], u[7]);
+                wo = fr.to_local(wdir);
+            } else {
+                const float us = (u[5] - alpha) / (1.f - alpha);
+                uint32_t sel = nlobes - 1;
+                float acc = 0.f;
+                for (uint32_t k = 0; k < nlobes; ++k) {
+                    acc += lp[k];
+                    if (us < acc) {
+                        sel = k;
+                        break;
+                    }
+                }
+                while (sel > 0 && lp[sel] == 0.f) --sel;
+                const LobeSample smp = lobe_sample(mat.lobes[sel], wi, u[6], u[7], u[8]);
+                ok = smp.valid;
+                wo = smp.wo;
+                wdir = normalize(fr.to_world(wo));
+            }
+            f3 f = mk(0.f, 0.f, 0.f);
+            float pdf = 0.f;
+            if (ok) {
+                for (uint32_t k = 0; k < nlobes; ++k) {
+                    const kz_lobe& lb = mat.lobes[k];
+                    const LobeEval e = lobe_eval(lb, wi, wo);
+                    f = f + hmul(ld3(lb.weight), e.f);
+                    pdf += lp[k] * e.pdf;
+                }
+                pdf = alpha * mixture_pdf(mix, wdir) + (1.f - alpha) * pdf;
+            }
+            alive = ok && pdf > 0.f && !is_zero(f);
+            if (alive) {
+                beta = hmul(beta, f * (1.f / pdf));
+                alive = !is_zero(beta);
+            }
+            if (alive) {
+                out.cont = true;
+                out.o_next = make_float4(P.x, P.y, P.z, pdf);
+                out.d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float(depth + 1));
+                out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
+                out.rng_next = rng.state;
+            }
+            if (alive && gs.recs) {
+                VRec& r = gs.recs[rbase + depth];
+                const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
+                                    mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
+                r.p = make_float4(p01.x, p01.y, p01.z, pdf);
+                r.n = make_float4(Ng.x, Ng.y, Ng.z, 1.f);
+                // d.w: luminance of f*|cos| along the sampled direction,
+                // so the network learns the whole integrand L*f*cos
+                r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.2126f * f.x + 0.7152f * f.y + 0.0722f * f.z);
+                r.beta = make_float4(beta.x, beta.y, beta.z, 0.f);
+                r.L = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        } else if (alive && wsum > 0.f) {
+            // BSDF sample (one-sample mixture over the non-delta lobes)
+            uint32_t sel = nlobes - 1;
+            float acc = 0.f;
+            for (uint32_t k = 0; k < nlobes; ++k) {
+                acc += lp[k];
+                if (u[5] < acc) {
+                    sel = k;
+                    break;
+                }
+            }
+            while (sel > 0 && lp[sel] == 0.f) --sel;
+            const kz_lobe& ls = mat.lobes[sel];
+            const LobeSample smp = lobe_sample(ls, wi, u[6], u[7], u[8]);
+            alive = smp.valid;
+            f3 weight = mk(0.f, 0.f, 0.f);
+            float pdf_dir = 0.f;
+            if (alive) {
+                if (smp.delta) {
+                    weight = hmul(ld3(ls.weight), smp.weight) * (1.f / lp[sel]);
+                } else {
+                    f3 f = mk(0.f, 0.f, 0.f);
+                    float pdf = 0.f;
+                    for (uint32_t k = 0; k < nlobes; ++k) {
+                        const kz_lobe& lb = mat.lobes[k];
+                        if (lobe_is_delta(lb.closure_id)) continue;
+                        const LobeEval e = lobe_eval(lb, wi, smp.wo);
+                        f = f + hmul(ld3(lb.weight), e.f);
+                        pdf += lp[k] * e.pdf;
+                    }
+                    alive = pdf > 0.f;
+                    if (alive) weight = f * (1.f / pdf);
+                    pdf_dir = pdf;
+                }
+            }
+            if (alive) {
+                beta = hmul(beta, weight);
+                alive = !is_zero(beta);
+            }
+            if (alive) {
+                const f3 dn = normalize(fr.to_world(smp.wo));
+                out.cont = true;
+                out.o_next = make_float4(P.x, P.y, P.z, pdf_dir);
+                out.d_next = make_float4(dn.x, dn.y, dn.z,
+                                     __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u)));
+                out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
+                out.rng_next = rng.state;
+            }
+        }
+        out.Lsum = Lsum;
+            out.film_idx = film_idx;
+    }
+}
+
 template <bool kGuided>
 __global__ void __launch_bounds__(256) k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
                                                GuideShade gs, const uint32_t* n_dev) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n_in = *n_dev;
-    bool cont = false, shadow = false;
-    float4 o_next, d_next, b_next, s_o, s_d, s_c;
-    unsigned long long rng_next = 0;
+    ShadeOut so;
     if (i < n_in) {
-        const float4 hit = in.hit[i];
-        const int rec = __float_as_int(hit.w);
-        if (rec >= 0) {
-            const float4 o4 = in.o4[i], d4 = in.d4[i], b4 = in.b4[i];
-            const uint32_t pid = __float_as_uint(b4.w);
-            const uint32_t film_idx = pid / pp.spp;
-            const uint32_t flags = __float_as_uint(d4.w);
-            const uint32_t depth = flags & 0xffu;
-            const bool prev_spec = (flags & kSpecularFlag) != 0;
-            const float prev_pdf = o4.w;
-            Pcg rng;
-            rng.state = in.rng[i];
-            rng.inc = ((uint64_t)pid << 1u) | 1u;
-            float u[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
-
-            const float4* tp = s.tris + (size_t)rec * 3;
-            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
-            const uint32_t geom = __float_as_uint(tb.w);
-            const kz_material& mat = s.materials[__float_as_uint(tc.w)];
-            const f3 v0 = xyz(ta), v1 = xyz(tb), v2 = xyz(tc);
-            const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
-            const f3 d = xyz(d4);
-            const f3 P = xyz(o4) + d * hit.x;
-            const Frame fr(Ng);
-            const f3 wi = -fr.to_local(d);
-            f3 beta = xyz(b4);
-            f3 Lsum = mk(0.f, 0.f, 0.f);
-            const uint32_t nl = s.n_lights;
-            const uint64_t rbase = kGuided ? ((uint64_t)pid - gs.pass_first) * pp.max_depth : 0;
-
-            // 1. emission (front face only: single_emissive_surface)
-            const f3 Le = ld3(mat.Le);
-            if (!is_zero(Le) && dot(d, Ng) < 0.f) {
-                float w = 1.f;
-                if (!prev_spec) {
-                    const int li = __ldg(s.geom_light + geom);
-                    if (li >= 0) {
-                        const float cos_l = -dot(d, Ng);
-                        const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
-                        w = power_heuristic(prev_pdf, lpdf);
-                    }
-                }
-                Lsum = Lsum + hmul(beta, Le) * w;
-                // MIS-weighted, like the next-event samples it pairs with
-                if (kGuided && gs.recs) propagate(gs.recs, rbase, depth, Lsum);
-            }
-
-            // lobe selection probabilities (CompositeClosure::compute_pdfs)
-            const uint32_t nlobes = min(mat.n_lobes, (uint32_t)KZ_MAX_LOBES);
-            float lp[KZ_MAX_LOBES];
-            const float winv = 1.f / (beta.x + beta.y + beta.z);
-            float wsum = 0.f;
-            bool any_smooth = false, any_delta = false;
-            for (uint32_t k = 0; k < nlobes; ++k) {
-                const kz_lobe& lb = mat.lobes[k];
-                lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
-                wsum += lp[k];
-                const bool dl = lobe_is_delta(lb.closure_id);
-                any_smooth |= !dl;
-                any_delta |= dl;
-            }
-            if (wsum > 0.f)
-                for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
-            const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
-            VmfMixture mix;
-            if (kGuided && guided) mixture_from_raw(gs.raw + (size_t)i * kGuideOut, mix);
-            const float alpha = gs.alpha;
-
-            // 2. next-event estimation
-            if (nl > 0 && any_smooth && wsum > 0.f) {
-                const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
-                const DevLight lt = s.lights[li];
-                const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
-                const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
-                const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
-                const float su0 = sqrtf(u[2]);
-                const float bu0 = 1.f - su0;
-                const float bv0 = u[3] * su0;
-                const f3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
-                const f3 nlgt = normalize(cross(a1 - a0, a2 - a0));
-                const f3 lv = p - P;
-                const float dist2 = dot(lv, lv);
-                const float dist = sqrtf(dist2);
-                const f3 ldir = mk(lv.x / dist, lv.y / dist, lv.z / dist);
-                const float cos_l = -dot(ldir, nlgt);
-                if (cos_l > 0.f) {
-                    const float pdf_solid = dist2 / (cos_l * lt.area);
-                    const float lpdf = pdf_solid * (1.0f / (float)nl);
-                    const f3 wo = fr.to_local(ldir);
-                    f3 f = mk(0.f, 0.f, 0.f);
-                    float bpdf = 0.f;
-                    for (uint32_t k = 0; k < nlobes; ++k) {
-                        const kz_lobe& lb = mat.lobes[k];
-                        if (lobe_is_delta(lb.closure_id)) continue;
-                        const LobeEval e = lobe_eval(lb, wi, wo);
-                        f = f + hmul(ld3(lb.weight), e.f);
-                        bpdf += lp[k] * e.pdf;
-                    }
-                    if (kGuided && guided) bpdf = alpha * mixture_pdf(mix, ldir) + (1.f - alpha) * bpdf;
-                    if (!is_zero(f)) {
-                        const float w = power_heuristic(lpdf, bpdf);
-                        const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
-                        shadow = true;
-                        s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
-                        s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
-                        const uint32_t tag =
-                            kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u)) : 0u;
-                        s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
-                        if (kGuided && gs.nee && guided) {
-                            // training sample: the light direction with its
-                            // MIS-weighted share of L*f*cos over the light pdf
-                            const f3 fl = hmul(f, ld3(lt.Le));
-                            const float wt = (0.2126f * fl.x + 0.7152f * fl.y + 0.0722f * fl.z) * (w / lpdf);
-                            const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
-                                                mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
-                            NRec& nr = gs.nee[rbase + depth];
-                            nr.p = make_float4(p01.x, p01.y, p01.z, wt);
-                            nr.n = make_float4(Ng.x, Ng.y, Ng.z, 0.f);
-                            nr.d = make_float4(ldir.x, ldir.y, ldir.z, 0.f);
-                        }
-                    }
-                }
-            }
-
-            bool alive = depth + 1 < pp.max_depth;
-            // 3. Russian roulette (integrator.cpp:491-498)
-            if (alive && depth >= pp.rr_min) {
-                const float prob = fminf(max_comp(beta) * 0.9025f, 0.99f);
-                if (prob < u[4]) alive = false;
-                else beta = beta * (1.f / prob);
-            }
-            // 4. direction sampling
-            if (kGuided && guided && alive) {
-                // one-sample MIS of the learned vMF mixture and the BSDF mixture
-                f3 wo, wdir;
-                bool ok = true;
-                if (u[5] < alpha) {
-                    wdir = mixture_sample(mix, u[5] / alpha, u[6], u[7]);
-                    wo = fr.to_local(wdir);
-                } else {
-                    const float us = (u[5] - alpha) / (1.f - alpha);
-                    uint32_t sel = nlobes - 1;
-                    float acc = 0.f;
-                    for (uint32_t k = 0; k < nlobes; ++k) {
-                        acc += lp[k];
-                        if (us < acc) {
-                            sel = k;
-                            break;
-                        }
-                    }
-                    while (sel > 0 && lp[sel] == 0.f) --sel;
-                    const LobeSample smp = lobe_sample(mat.lobes[sel], wi, u[6], u[7], u[8]);
-                    ok = smp.valid;
-                    wo = smp.wo;
-                    wdir = normalize(fr.to_world(wo));
-                }
-                f3 f = mk(0.f, 0.f, 0.f);
-                float pdf = 0.f;
-                if (ok) {
-                    for (uint32_t k = 0; k < nlobes; ++k) {
-                        const kz_lobe& lb = mat.lobes[k];
-                        const LobeEval e = lobe_eval(lb, wi, wo);
-                        f = f + hmul(ld3(lb.weight), e.f);
-                        pdf += lp[k] * e.pdf;
-                    }
-                    pdf = alpha * mixture_pdf(mix, wdir) + (1.f - alpha) * pdf;
-                }
-                alive = ok && pdf > 0.f && !is_zero(f);
-                if (alive) {
-                    beta = hmul(beta, f * (1.f / pdf));
-                    alive = !is_zero(beta);
-                }
-                if (alive) {
-                    cont = true;
-                    o_next = make_float4(P.x, P.y, P.z, pdf);
-                    d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float(depth + 1));
-                    b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
-                    rng_next = rng.state;
-                }
-                if (alive && gs.recs) {
-                    VRec& r = gs.recs[rbase + depth];
-                    const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
-                                        mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
-                    r.p = make_float4(p01.x, p01.y, p01.z, pdf);
-                    r.n = make_float4(Ng.x, Ng.y, Ng.z, 1.f);
-                    // d.w: luminance of f*|cos| along the sampled direction,
-                    // so the network learns the whole integrand L*f*cos
-                    r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.2126f * f.x + 0.7152f * f.y + 0.0722f * f.z);
-                    r.beta = make_float4(beta.x, beta.y, beta.z, 0.f);
-                    r.L = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-            } else if (alive && wsum > 0.f) {
-                // BSDF sample (one-sample mixture over the non-delta lobes)
-                uint32_t sel = nlobes - 1;
-                float acc = 0.f;
-                for (uint32_t k = 0; k < nlobes; ++k) {
-                    acc += lp[k];
-                    if (u[5] < acc) {
-                        sel = k;
-                        break;
-                    }
-                }
-                while (sel > 0 && lp[sel] == 0.f) --sel;
-                const kz_lobe& ls = mat.lobes[sel];
-                const LobeSample smp = lobe_sample(ls, wi, u[6], u[7], u[8]);
-                alive = smp.valid;
-                f3 weight = mk(0.f, 0.f, 0.f);
-                float pdf_dir = 0.f;
-                if (alive) {
-                    if (smp.delta) {
-                        weight = hmul(ld3(ls.weight), smp.weight) * (1.f / lp[sel]);
-                    } else {
-                        f3 f = mk(0.f, 0.f, 0.f);
-                        float pdf = 0.f;
-                        for (uint32_t k = 0; k < nlobes; ++k) {
-                            const kz_lobe& lb = mat.lobes[k];
-                            if (lobe_is_delta(lb.closure_id)) continue;
-                            const LobeEval e = lobe_eval(lb, wi, smp.wo);
-                            f = f + hmul(ld3(lb.weight), e.f);
-                            pdf += lp[k] * e.pdf;
-                        }
-                        alive = pdf > 0.f;
-                        if (alive) weight = f * (1.f / pdf);
-                        pdf_dir = pdf;
-                    }
-                }
-                if (alive) {
-                    beta = hmul(beta, weight);
-                    alive = !is_zero(beta);
-                }
-                if (alive) {
-                    const f3 dn = normalize(fr.to_world(smp.wo));
-                    cont = true;
-                    o_next = make_float4(P.x, P.y, P.z, pdf_dir);
-                    d_next = make_float4(dn.x, dn.y, dn.z,
-                                         __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u)));
-                    b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
-                    rng_next = rng.state;
-                }
-            }
-            if (!is_zero(Lsum)) film_add(film, film64, film_idx, Lsum);
-        }
+        shade_vertex<kGuided>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
+                              kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
+        if (!is_zero(so.Lsum)) film_add(film, film64, so.film_idx, so.Lsum);
     }
+    const bool cont = so.cont, shadow = so.shadow;
     const uint32_t slot = warp_append(cont, &ctr->n_next);
     if (cont) {
-        out.o4[slot] = o_next;
-        out.d4[slot] = d_next;
-        out.b4[slot] = b_next;
-        out.rng[slot] = rng_next;
+        out.o4[slot] = so.o_next;
+        out.d4[slot] = so.d_next;
+        out.b4[slot] = so.b_next;
+        out.rng[slot] = so.rng_next;
     }
     const uint32_t sslot = warp_append(shadow, &ctr->n_shadow);
     if (shadow) {
-        sq.o4[sslot] = s_o;
-        sq.d4[sslot] = s_d;
-        sq.c4[sslot] = s_c;
+        sq.o4[sslot] = so.s_o;
+        sq.d4[sslot] = so.s_d;
+        sq.c4[sslot] = so.s_c;
     }
 }
 
@@ -602,6 +621,104 @@ __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __res
         samples[3 * (size_t)slot + 1] = b;
         samples[3 * (size_t)slot + 2] = c;
         atomicAdd(wsum, a.w);
+    }
+}
+
+// ------------------------------------------------------------------ persistent batch renderer
+// Many independent jobs (scenes, cameras, films) in one launch. Lanes hold a
+// path each; every `period` vertices (or when a warp has no live path) free
+// lanes take the next global path ids with one atomic per warp, find their
+// job by binary search over the jobs' first path ids, and start a camera
+// path. Each vertex is traced, shaded (shade_vertex) and its shadow ray
+// traced inline. Loop exit is warp-uniform: the fetch counter only grows and
+// ends the loop once it passes the total with no live lane left.
+__device__ __forceinline__ uint32_t find_job(const DevJob* __restrict__ jobs, uint32_t n_jobs, unsigned long long g) {
+    uint32_t lo = 0, hi = n_jobs;  // last job with path_begin <= g
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].path_begin <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_render_batch(const DevJob* __restrict__ jobs, uint32_t n_jobs,
+                                                      unsigned long long total, BatchCounters* bc, uint32_t period) {
+    const int lane = threadIdx.x & 31;
+    bool active = false, exhausted = false;
+    uint32_t job = 0;
+    float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4, b4 = o4;
+    unsigned long long rng = 0;
+    unsigned long long n_bounce = 0, n_shadow = 0;
+    for (uint32_t step = 0;; ++step) {
+        const bool any_live = __any_sync(0xffffffffu, active);
+        if (!exhausted && (step % period == 0 || !any_live)) {
+            const unsigned want = __ballot_sync(0xffffffffu, !active);
+            if (want) {
+                const int leader = __ffs(want) - 1;
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(&bc->next_path, (unsigned long long)__popc(want));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!active) {
+                    const unsigned long long g = base + (unsigned)__popc(want & ((1u << lane) - 1u));
+                    if (g < total) {
+                        job = find_job(jobs, n_jobs, g);
+                        const DevJob& J = jobs[job];
+                        PathSoA one;
+                        one.o4 = &o4;
+                        one.d4 = &d4;
+                        one.b4 = &b4;
+                        one.rng = &rng;
+                        generate_camera_path(J.cam, J.pp, one, 0, g - J.path_begin);
+                        active = true;
+                    }
+                }
+                if (base + (unsigned)__popc(want) >= total) exhausted = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active) {
+            const DevJob& J = jobs[job];
+            TRay r = make_tray(xyz(o4), xyz(d4), kRayEps);
+            HitRec h;
+            uint32_t dn = 0, dt = 0;
+            if (!trace_closest<false>(J.scene, r, __int_as_float(0x7f800000), h, dn, dt)) {
+                set_status(&bc->status, KZ_ERR_STACK);
+                h.rec = -1;
+            }
+            ++n_bounce;
+            ShadeOut so;
+            shade_vertex<false>(J.scene, J.pp, make_float4(h.t, h.u, h.v, __int_as_float(h.rec)), o4, d4, b4, rng,
+                                GuideShade{}, nullptr, so);
+            if (!is_zero(so.Lsum)) film_add(J.film, nullptr, so.film_idx, so.Lsum);
+            if (so.shadow) {
+                ++n_shadow;
+                TRay sr = make_tray(xyz(so.s_o), xyz(so.s_d), kRayEps);
+                bool overflow;
+                const bool occ = trace_any<false>(J.scene, sr, so.s_o.w, overflow, dn, dt);
+                if (overflow) set_status(&bc->status, KZ_ERR_STACK);
+                if (!occ && !overflow) film_add(J.film, nullptr, __float_as_uint(so.s_d.w), xyz(so.s_c));
+            }
+            if (so.cont) {
+                o4 = so.o_next;
+                d4 = so.d_next;
+                b4 = so.b_next;
+                rng = so.rng_next;
+            } else {
+                active = false;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_bounce += __shfl_down_sync(0xffffffffu, n_bounce, o);
+        n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&bc->path_bounces, n_bounce);
+        atomicAdd(&bc->shadow_rays, n_shadow);
     }
 }
 
@@ -755,6 +872,11 @@ void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCou
     else
         k_trace_shadow<false, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr,
                                                                                nullptr, 0);
+}
+void launch_render_batch(const DevJob* jobs, uint32_t n_jobs, unsigned long long total, BatchCounters* bc,
+                         uint32_t period, uint32_t ctas, uint32_t block, cudaStream_t st) {
+    if (!n_jobs || !total) return;
+    k_render_batch<<<ctas, block, 0, st>>>(jobs, n_jobs, total, bc, period ? period : 1u);
 }
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
     if (!n) return;

@@ -301,3 +301,45 @@ def slit_room_scene(width=1024, height=1024, spp=16, max_depth=10, n_spheres=32,
         d.add((sv * np.float32(r) + pos).astype(np.float32), sf, len(d.materials) - 1)
     d.camera = api.Camera(eye=(0.08, 0.55, 0.08), lookat=(0.75, 0.35, 0.8), up=(0, 1, 0), fov=75.0)
     return d
+
+
+def soup_render_scene(n_tris, seed, albedo=0.6) -> SceneDesc:
+    """A render job over the traversal workload's generator: an n_tris
+    triangle soup in the unit cube (Lambert), a 1 x 1 quad light above it."""
+    d = SceneDesc()
+    d.materials = [api.material([api.diffuse((albedo, albedo, albedo))]), api.material([], Le=(6.0, 6.0, 6.0))]
+    tv = triangle_soup(n_tris, seed)
+    d.add(tv.reshape(-1, 3), np.arange(3 * n_tris, dtype=np.uint32).reshape(n_tris, 3), 0)
+    v, i = quad((0.0, 1.6, 0.0), (1.0, 0, 0), (0, 0, 1.0))  # faces -y
+    d.add(v, i, 1, is_light=True)
+    d.camera = api.Camera(eye=(1.9, 1.3, -1.3), lookat=(0.5, 0.45, 0.5), up=(0, 1, 0), fov=45.0)
+    return d
+
+
+def batch_jobs(n_jobs=256, seed=5, tri_range=(50_000, 500_000), resolutions=(64, 128, 256, 512), spps=(4, 16, 64),
+               depths=(4, 8)):
+    """Uneven batch: seeded soup scenes with tri_range triangles, resolution,
+    spp and max depth drawn uniformly from the given sets."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(n_jobs):
+        n = int(rng.integers(tri_range[0], tri_range[1] + 1))
+        r = int(rng.choice(resolutions))
+        jobs.append({"desc_args": (n, int(rng.integers(1 << 30))), "width": r, "height": r,
+                     "spp": int(rng.choice(spps)), "max_depth": int(rng.choice(depths)), "seed": 1000 + k})
+    return jobs
+
+
+def build_batch_scenes(jobs, workers=8):
+    """Generate and build every job's scene (BVH builds run in parallel; the
+    C ABI releases the GIL). Adds 'scene' and 'camera' to each job."""
+    import concurrent.futures as cf
+
+    def one(j):
+        d = soup_render_scene(*j["desc_args"])
+        return d.build(), d.camera
+
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        for j, (sc, cam) in zip(jobs, ex.map(one, jobs)):
+            j["scene"], j["camera"] = sc, cam
+    return jobs

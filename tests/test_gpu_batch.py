@@ -1,0 +1,50 @@
+"""Batched rendering: many uneven jobs in one persistent launch (optionally a
+CUDA graph) must give each job the same film as rendering it alone."""
+import numpy as np
+import pytest
+
+from kazen_proto_gb300 import api, autotune, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def jobs():
+    js = scenes.batch_jobs(n_jobs=7, seed=3, tri_range=(2000, 20000), resolutions=(16, 32, 48), spps=(2, 4, 8),
+                           depths=(4, 8))
+    return scenes.build_batch_scenes(js, workers=4)
+
+
+def rel_mse(a, b, eps=1e-2):
+    return float(np.mean((np.asarray(a, np.float64) - b) ** 2 / (np.asarray(b, np.float64) ** 2 + eps)))
+
+
+def singles(jobs):
+    out = []
+    for j in jobs:
+        r = api.Renderer(spp=j["spp"], max_depth=j["max_depth"], seed=j["seed"])
+        out.append((r.render(j["scene"], j["camera"], j["width"], j["height"]), r.last_stats))
+    return out
+
+
+@pytest.mark.parametrize("cfg", [dict(block_size=128, ctas_per_sm=2, refill_period=1, use_graph=True),
+                                 dict(block_size=64, ctas_per_sm=1, refill_period=4, use_graph=False),
+                                 dict(block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True)])
+def test_batch_matches_single_renders(gpu, jobs, cfg):
+    imgs, st = api.render_batch(jobs, api.batch_config(**cfg))
+    ref = singles(jobs)
+    for img, (r, rs) in zip(imgs, ref):
+        assert rel_mse(img, r) < 1e-10
+    assert st["paths"] == sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+    assert st["path_bounces"] == sum(rs["path_bounces"] for _, rs in ref)
+    assert st["shadow_rays"] == sum(rs["shadow_rays"] for _, rs in ref)
+    assert st["device_ms"] > 0
+
+
+def test_autotuner_picks_a_candidate(gpu, jobs, tmp_path, monkeypatch):
+    monkeypatch.setattr(autotune, "PATH", str(tmp_path / "autotune.json"))
+    best, table = autotune.tune(jobs, reps=1)
+    assert len(table) == len(autotune.BLOCKS) * len(autotune.CTAS_PER_SM) * len(autotune.PERIODS)
+    assert best in [c for c, _ in table] and autotune.load() == best
+    imgs, _ = api.render_batch(jobs, autotune.tuned_config())
+    assert all(np.isfinite(i).all() for i in imgs)
