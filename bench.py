@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-traversal", action="store_true")
     p.add_argument("--no-guiding", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
     return p.parse_args()
 
 
@@ -249,7 +250,10 @@ def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
     d = scenes.slit_room_scene(R, R, max_depth=max_depth)
     s = d.build()
     t0 = time.perf_counter()
-    ref = api.Renderer(spp=ref_spp, max_depth=max_depth, seed=99).render(s, d.camera, R, R, fp64=True)[1]
+    chunk = min(ref_spp, (1 << 31) // (R * R))  # path ids of one render stay below 2^32
+    parts = [api.Renderer(spp=chunk, max_depth=max_depth, seed=99 + k).render(s, d.camera, R, R, fp64=True)[1]
+             for k in range(max(1, ref_spp // chunk))]
+    ref = np.mean(parts, axis=0)
     ref_s = time.perf_counter() - t0
     r = api.Renderer(spp=plain_spp, max_depth=max_depth, seed=1)
     r.render(s, d.camera, R, R)  # warm-up
@@ -281,6 +285,49 @@ def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
             "relmse_ratio_plain_over_guided_equal_time": round(e_plain / e_guided, 3),
             "guided_trained_equal_spp": {"spp": plain_spp, "relmse": e_frozen},
             "relmse_ratio_plain_over_guided_equal_spp": round(e_plain / e_frozen, 3)}
+
+
+# ---------------------------------------------------------------- batched uneven jobs
+def batch_bench(n_jobs=256):
+    """256 seeded soup jobs (50k-500k triangles; 64..512 squared; 4/16/64
+    spp; depth 4 or 8): one persistent launch (CUDA graph, autotuned) against
+    the same jobs rendered one kz_render call each."""
+    from kazen_proto_gb300 import api, autotune, scenes
+
+    t0 = time.perf_counter()
+    jobs = scenes.build_batch_scenes(scenes.batch_jobs(n_jobs=n_jobs, seed=5), workers=16)
+    build_s = time.perf_counter() - t0
+    # autotune on a sample of the jobs at reduced spp
+    sample = [dict(j, spp=min(j["spp"], 4)) for j in jobs[::8]]
+    best, table = autotune.tune(sample, reps=1)
+    cfg = autotune.tuned_config(use_graph=True)
+    api.render_batch(jobs[:4], cfg)  # warm-up
+    t0 = time.perf_counter()
+    imgs, st = api.render_batch(jobs, cfg)
+    wall_b = time.perf_counter() - t0
+    # one launch (one kz_render call) per job
+    singles_ms, singles_wall, bounces_single = 0.0, 0.0, 0
+    errs = []
+    for j, img in zip(jobs, imgs):
+        r = api.Renderer(spp=j["spp"], max_depth=j["max_depth"], seed=j["seed"], flags=0)
+        t0 = time.perf_counter()
+        ref = r.render(j["scene"], j["camera"], j["width"], j["height"])
+        singles_wall += time.perf_counter() - t0
+        bounces_single += r.last_stats["path_bounces"]
+        errs.append(float(np.abs(img - ref).max() / max(1e-6, float(np.abs(ref).max()))))
+        j["scene"].release_scratch()
+    for j in jobs:
+        j["scene"].close()
+    mb = st["path_bounces"] / (st["device_ms"] / 1e3) / 1e6
+    return {"jobs": n_jobs, "paths": st["paths"], "path_bounces": st["path_bounces"],
+            "triangles_total": int(sum(j["desc_args"][0] + 2 for j in jobs)), "scene_build_s": round(build_s, 1),
+            "autotuned": best, "autotune_candidates": len(table), "persistent_lanes": st["threads"],
+            "batched_graph": {"device_ms": round(st["device_ms"], 2), "wall_s": round(wall_b, 3),
+                              "mpaths_bounces_per_s": round(mb, 1)},
+            "one_launch_each": {"wall_s": round(singles_wall, 3),
+                                "mpaths_bounces_per_s": round(bounces_single / singles_wall / 1e6, 1)},
+            "speedup_wall": round(singles_wall / wall_b, 3),
+            "max_rel_film_difference": max(errs)}
 
 
 def load_traffic():
@@ -376,6 +423,10 @@ def run_ours(args):
     if rank == 0 and not args.no_guiding and not args.small and not args.profile:
         guide = guiding_bench()
 
+    batch = None
+    if rank == 0 and not args.no_batch and not args.small and not args.profile:
+        batch = batch_bench()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
@@ -420,6 +471,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "traversal": trav,
         "guiding": guide,
+        "batch": batch,
     }
     if img is not None:
         line["image_mean"] = float(np.mean(img))
