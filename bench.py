@@ -35,6 +35,7 @@ if ROOT not in sys.path:
 
 METRIC = "Mpaths*bounces/s (plain GPU wavefront PT)"
 UNIT = "Mpaths*bounces/s"
+NODE_BYTES = 80  # one 8-wide BVH node (kz_bvh.h)
 
 
 def parse():
@@ -225,7 +226,7 @@ def traversal_bench(steps, warmup):
         res[name + "_ms"] = ms / steps
     res["node_fetches_per_ray"] = nodes / n
     res["tri_fetches_per_ray"] = tris / n
-    bytes_per_ray = 32 + 8 + 64 * nodes / n + 48 * tris / n
+    bytes_per_ray = 32 + 8 + NODE_BYTES * nodes / n + 48 * tris / n
     res["closest_alg_bytes_per_ray"] = bytes_per_ray
     res["closest_alg_gbs"] = bytes_per_ray * n / (res["closest_ms"] / 1e3) / 1e9
     res["workload"] = "1,048,576-triangle soup, 16,777,216 incoherent rays, device-resident"
@@ -436,7 +437,7 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     trace_ms_frame = stage["trace_ms"] / args.steps
     rays_frame = bounces / args.steps
-    alg_bytes_ray = 32 + 16 + 64 * nodes_per_ray + 48 * tris_per_ray
+    alg_bytes_ray = 32 + 16 + NODE_BYTES * nodes_per_ray + 48 * tris_per_ray
     alg_bytes_frame = alg_bytes_ray * rays_frame
     achieved = alg_bytes_frame / (trace_ms_frame / 1e3) / 1e9
     iters_frame = iterations / args.steps
@@ -462,7 +463,7 @@ def run_ours(args):
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                      "alg_bytes_per_ray": round(alg_bytes_ray, 1),
                      "node_fetches_per_ray": round(nodes_per_ray, 2), "tri_fetches_per_ray": round(tris_per_ray, 2),
-                     "note": "algorithmic bytes = 32 B ray + 16 B hit + 64 B per node fetch + 48 B per triangle "
+                     "note": "algorithmic bytes = 32 B ray + 16 B hit + 80 B per 8-wide node fetch + 48 B per triangle "
                              "fetch; node/triangle fetches are served mostly from L1/L2"},
         "stages_ms_per_frame": {k: round(v / args.steps, 3) for k, v in stage.items()},
         "mrays_per_s": round((bounces + shadow) / (total_ms / 1e3) / 1e6, 2),

@@ -509,8 +509,14 @@ kz_status kz_scene_build(kz_scene* s) {
     }
     goff[s->meshes.size()] = (uint32_t)t;
     kz::BvhBuildInput in{tv.data(), (uint32_t)total, tgeom.data(), gmat.data()};
-    kz::BvhBuildOutput out;
-    kz::build_bvh(in, 4, out);
+    kz::WideBvhOutput out;
+    try {
+        kz::build_wide_bvh(in, out);
+    } catch (const std::bad_alloc&) {
+        return fail(KZ_ERR_OOM, "host allocation failed during the BVH build");
+    } catch (const std::exception& e) {
+        return fail(KZ_ERR_INVALID_ARG, "BVH build: %s", e.what());
+    }
 
     // lights: one per emissive mesh with triangles, area CDF in triangle order
     std::vector<kz::DevLight> lights;
@@ -584,7 +590,7 @@ kz_status kz_scene_build(kz_scene* s) {
         d.box_lo = make_float3(lo[0], lo[1], lo[2]);
         d.box_inv = make_float3(inv[0], inv[1], inv[2]);
     }
-    d.nodes = s->nodes.as<float4>();
+    d.nodes = s->nodes.as<uint4>();
     d.tris = s->tris.as<float4>();
     d.n_nodes = out.n_nodes;
     d.n_tris = (uint32_t)total;
@@ -601,7 +607,7 @@ kz_status kz_scene_build(kz_scene* s) {
     s->info.n_triangles = total;
     s->info.n_lights = lights.size();
     s->info.n_bvh_nodes = out.n_nodes;
-    s->info.bvh_bytes = (uint64_t)out.n_nodes * 64;
+    s->info.bvh_bytes = (uint64_t)out.n_nodes * kz::kWideWords * 4;
     s->info.triangle_bytes = total * 48;
     s->info.bvh_depth = out.depth;
     s->info.built = 1;

@@ -5,6 +5,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <stdexcept>
+#include <utility>
 
 namespace kz {
 namespace {
@@ -178,105 +180,218 @@ inline float u2f(uint32_t u) {
     return f;
 }
 
+inline uint32_t f2u(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+void emit_tri(const BvhBuildInput& in, uint32_t t, std::vector<float>& tris, std::vector<uint32_t>& order) {
+    const float* v = in.tri_verts + (size_t)t * 9;
+    uint32_t geom = in.tri_geom ? in.tri_geom[t] : 0u;
+    uint32_t mat = in.geom_material ? (uint32_t)in.geom_material[geom] : 0u;
+    float r[12] = {v[0], v[1], v[2], u2f(t), v[3], v[4], v[5], u2f(geom), v[6], v[7], v[8], u2f(mat)};
+    tris.insert(tris.end(), r, r + 12);
+    order.push_back(t);
+}
+
+// A subtree of the binary build seen by the wide collapse: an inner build
+// node (bnode >= 0) or a run of triangles idx[first, first + count).
+struct WItem {
+    int32_t bnode = -1;
+    uint32_t first = 0, count = 0;
+    Box box;
+};
+
+constexpr uint32_t kWideLeafMax = 3;
+
+struct Collapser {
+    Builder& b;
+    explicit Collapser(Builder& bb) : b(bb) {}
+
+    WItem item_of(int32_t id) const {
+        const BNode& c = b.nodes[(size_t)id];
+        WItem w;
+        w.box = c.box;
+        if (c.left >= 0) {
+            w.bnode = id;
+        } else {
+            w.first = c.first;
+            w.count = c.count;
+        }
+        return w;
+    }
+    static bool expandable(const WItem& w) { return w.bnode >= 0 || w.count > kWideLeafMax; }
+
+    Box range_box(uint32_t first, uint32_t count) const {
+        Box bx;
+        for (uint32_t i = first; i < first + count; ++i) bx.grow(b.tb[b.idx[i]]);
+        return bx;
+    }
+
+    void expand(const WItem& w, WItem& l, WItem& r) {
+        if (w.bnode >= 0) {
+            const BNode& n = b.nodes[(size_t)w.bnode];
+            l = item_of(n.left);
+            r = item_of(n.right);
+            return;
+        }
+        // a leaf left larger than 3 triangles by the depth cap: halve it by
+        // count along the widest centroid axis
+        Box cb;
+        for (uint32_t i = w.first; i < w.first + w.count; ++i) cb.grow(&b.cen[(size_t)b.idx[i] * 3]);
+        int a = 0;
+        for (int k = 1; k < 3; ++k)
+            if (cb.hi[k] - cb.lo[k] > cb.hi[a] - cb.lo[a]) a = k;
+        const uint32_t mid = w.first + w.count / 2;
+        std::nth_element(b.idx.begin() + w.first, b.idx.begin() + mid, b.idx.begin() + w.first + w.count,
+                         [&](uint32_t p, uint32_t q) {
+                             float cp = b.cen[(size_t)p * 3 + a], cq = b.cen[(size_t)q * 3 + a];
+                             return cp < cq || (cp == cq && p < q);
+                         });
+        l = WItem{-1, w.first, mid - w.first, range_box(w.first, mid - w.first)};
+        r = WItem{-1, mid, w.first + w.count - mid, range_box(mid, w.first + w.count - mid)};
+    }
+};
+
+// Smallest power-of-two quantum q with 255 * q >= ext (>= 2^-100).
+int quantum_exponent(double ext) {
+    int e = -100;
+    if (ext > 0.0) {
+        e = std::max(-100, (int)std::ceil(std::log2(ext / 255.0)));
+        while (std::ldexp(255.0, e) < ext) ++e;
+        while (e > -100 && std::ldexp(255.0, e - 1) >= ext) --e;
+    }
+    if (e > 112) throw std::length_error("scene extent too large for the wide BVH");
+    return e;
+}
+
 }  // namespace
 
-void build_bvh(const BvhBuildInput& in, int max_leaf, BvhBuildOutput& out) {
-    Builder b(in, max_leaf);
+void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out) {
+    Builder b(in, (int)kWideLeafMax);
     b.run();
-    const auto& bn = b.nodes;
-
-    // Device layout: one device node per inner build node, preorder; a leaf
-    // root becomes child 0 of a synthetic root.
-    out.nodes.clear();
+    Collapser col(b);
+    out.nodes.assign(kWideWords, 0u);
     out.tris.clear();
     out.order.clear();
     out.tris.reserve((size_t)in.ntris * 12);
     out.order.reserve(in.ntris);
+    out.depth = 1;
 
-    auto emit_leaf = [&](const BNode& nd) -> int32_t {
-        uint32_t rec = (uint32_t)out.order.size();
-        for (uint32_t i = nd.first; i < nd.first + nd.count; ++i) {
-            uint32_t t = b.idx[i];
-            const float* v = in.tri_verts + (size_t)t * 9;
-            uint32_t geom = in.tri_geom ? in.tri_geom[t] : 0u;
-            uint32_t mat = in.geom_material ? (uint32_t)in.geom_material[geom] : 0u;
-            float r[12] = {v[0], v[1], v[2], u2f(t), v[3], v[4], v[5], u2f(geom), v[6], v[7], v[8], u2f(mat)};
-            out.tris.insert(out.tris.end(), r, r + 12);
-            out.order.push_back(t);
-        }
-        return ~(int32_t)rec;
+    WItem root;
+    if (!b.nodes.empty()) root = col.item_of(0);
+    struct Pending {
+        WItem item;
+        uint32_t node, depth;
     };
-
-    struct Item { int32_t build_node; uint32_t dev_node; };
-    std::vector<Item> stack;
-    auto alloc_dev = [&]() -> uint32_t {
-        uint32_t id = (uint32_t)(out.nodes.size() / 16);
-        out.nodes.resize(out.nodes.size() + 16, 0.f);
-        return id;
-    };
-    auto set_child = [&](uint32_t dev, int slot, const Box& box, int32_t link, uint32_t count) {
-        float* n = &out.nodes[(size_t)dev * 16];
-        const Box& bx = box;
-        float* xy = n + slot * 4;
-        xy[0] = bx.lo[0];
-        xy[1] = bx.hi[0];
-        xy[2] = bx.lo[1];
-        xy[3] = bx.hi[1];
-        n[8 + slot * 2] = bx.lo[2];
-        n[9 + slot * 2] = bx.hi[2];
-        n[12 + slot] = u2f((uint32_t)link);
-        n[14 + slot] = u2f(count);
-    };
-
-    uint32_t root = alloc_dev();
-    if (bn.empty() || bn[0].left < 0) {
-        // Leaf root (few triangles): child 0 is the leaf, child 1 repeats its
-        // box with no triangles (finite boxes only; the slab test has no
-        // empty-box encoding). An empty scene keeps an all-zero root and is
-        // never traversed.
-        if (!bn.empty() && bn[0].count > 0) {
-            int32_t link = emit_leaf(bn[0]);
-            set_child(root, 0, bn[0].box, link, bn[0].count);
-            set_child(root, 1, bn[0].box, link, 0);
-        } else {
-            Box point;  // empty scene: two empty leaves, never an inner link
-            for (int a = 0; a < 3; ++a) point.lo[a] = point.hi[a] = 0.f;
-            set_child(root, 0, point, ~0, 0);
-            set_child(root, 1, point, ~0, 0);
-        }
-    } else {
-        stack.push_back({0, root});
-        while (!stack.empty()) {
-            Item it = stack.back();
-            stack.pop_back();
-            const BNode& nd = bn[(size_t)it.build_node];
-            const int32_t ch[2] = {nd.left, nd.right};
-            // children that are inner nodes get device nodes; push right first
-            // so the left subtree is laid out directly after its parent
-            int32_t links[2];
-            for (int s = 0; s < 2; ++s) {
-                const BNode& c = bn[(size_t)ch[s]];
-                if (c.left < 0) {
-                    links[s] = emit_leaf(c);
-                    set_child(it.dev_node, s, c.box, links[s], c.count);
+    std::vector<Pending> queue{{root, 0u, 1u}};
+    for (size_t head = 0; head < queue.size(); ++head) {
+        const Pending pd = queue[head];
+        out.depth = std::max(out.depth, pd.depth);
+        // greedy collapse: open the largest expandable child until 8 slots
+        WItem ch[8];
+        int nch = 0;
+        ch[nch++] = pd.item;
+        while (nch < 8) {
+            int best = -1;
+            float best_area = -1.f;
+            for (int k = 0; k < nch; ++k)
+                if (Collapser::expandable(ch[k]) && ch[k].box.area() > best_area) {
+                    best = k;
+                    best_area = ch[k].box.area();
                 }
+            if (best < 0) break;
+            WItem l, r;
+            col.expand(ch[best], l, r);
+            ch[best] = l;
+            ch[nch++] = r;
+        }
+        // drop empty runs (an empty scene only)
+        int m = 0;
+        for (int k = 0; k < nch; ++k)
+            if (ch[k].bnode >= 0 || ch[k].count > 0) ch[m++] = ch[k];
+        nch = m;
+
+        uint32_t* w = &out.nodes[(size_t)pd.node * kWideWords];
+        if (nch == 0) {  // empty scene: a node with no slots, never hit
+            w[3] = 127u | 127u << 8 | 127u << 16;
+            continue;
+        }
+
+        // slot assignment: child towards octant s of the node centre
+        Box nb;
+        for (int k = 0; k < nch; ++k) nb.grow(ch[k].box);
+        float cen[8][3];
+        for (int k = 0; k < nch; ++k)
+            for (int a = 0; a < 3; ++a)
+                cen[k][a] = 0.5f * (ch[k].box.lo[a] + ch[k].box.hi[a]) - 0.5f * (nb.lo[a] + nb.hi[a]);
+        struct Cand { float score; int child, slot; };
+        std::vector<Cand> cand;
+        cand.reserve((size_t)nch * 8);
+        for (int k = 0; k < nch; ++k)
+            for (int sl = 0; sl < 8; ++sl) {
+                float sc = 0.f;
+                for (int a = 0; a < 3; ++a) sc += ((sl >> a) & 1) ? cen[k][a] : -cen[k][a];
+                cand.push_back({sc, k, sl});
             }
-            uint32_t dev_children[2] = {0, 0};
-            for (int s = 0; s < 2; ++s) {
-                const BNode& c = bn[(size_t)ch[s]];
-                if (c.left >= 0) {
-                    dev_children[s] = alloc_dev();
-                    set_child(it.dev_node, s, c.box, (int32_t)dev_children[s], 0);
-                }
+        std::stable_sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) { return x.score > y.score; });
+        int slot_child[8];
+        bool child_done[8] = {false};
+        for (int sl = 0; sl < 8; ++sl) slot_child[sl] = -1;
+        for (const Cand& c : cand)
+            if (!child_done[c.child] && slot_child[c.slot] < 0) {
+                slot_child[c.slot] = c.child;
+                child_done[c.child] = true;
             }
-            for (int s = 1; s >= 0; --s) {
-                const BNode& c = bn[(size_t)ch[s]];
-                if (c.left >= 0) stack.push_back({ch[s], dev_children[s]});
+
+        // quantization frame
+        int ex[3];
+        for (int a = 0; a < 3; ++a) {
+            ex[a] = quantum_exponent((double)nb.hi[a] - (double)nb.lo[a]);
+            w[a] = f2u(nb.lo[a]);
+        }
+        uint32_t imask = 0, meta[8] = {0};
+        uint8_t qlo[3][8] = {{0}}, qhi[3][8] = {{0}};
+        const uint32_t child_base = (uint32_t)(out.nodes.size() / kWideWords);
+        const uint32_t tri_base = (uint32_t)out.order.size();
+        uint32_t n_inner = 0, tri_off = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            const int k = slot_child[sl];
+            if (k < 0) continue;
+            const WItem& c = ch[k];
+            for (int a = 0; a < 3; ++a) {
+                const double q = std::ldexp(1.0, ex[a]);
+                double lo = std::floor(((double)c.box.lo[a] - (double)nb.lo[a]) / q);
+                double hi = std::ceil(((double)c.box.hi[a] - (double)nb.lo[a]) / q);
+                qlo[a][sl] = (uint8_t)std::min(255.0, std::max(0.0, lo));
+                qhi[a][sl] = (uint8_t)std::min(255.0, std::max(0.0, hi));
+            }
+            if (Collapser::expandable(c)) {
+                imask |= 1u << sl;
+                meta[sl] = 0x20u | (24u + (uint32_t)sl);
+                out.nodes.resize(out.nodes.size() + kWideWords, 0u);
+                queue.push_back({c, child_base + n_inner, pd.depth + 1});
+                ++n_inner;
+            } else {
+                meta[sl] = (((1u << c.count) - 1u) << 5) | tri_off;
+                for (uint32_t i = c.first; i < c.first + c.count; ++i) emit_tri(in, b.idx[i], out.tris, out.order);
+                tri_off += c.count;
             }
         }
+        w = &out.nodes[(size_t)pd.node * kWideWords];  // the resize above may move the array
+        w[3] = (uint32_t)(ex[0] + 127) | (uint32_t)(ex[1] + 127) << 8 | (uint32_t)(ex[2] + 127) << 16 | imask << 24;
+        w[4] = child_base;
+        w[5] = tri_base;
+        for (int sl = 0; sl < 8; ++sl) w[6 + sl / 4] |= meta[sl] << (8 * (sl % 4));
+        for (int a = 0; a < 3; ++a)
+            for (int sl = 0; sl < 8; ++sl) {
+                w[8 + 4 * a + sl / 4] |= (uint32_t)qlo[a][sl] << (8 * (sl % 4));
+                w[10 + 4 * a + sl / 4] |= (uint32_t)qhi[a][sl] << (8 * (sl % 4));
+            }
     }
-    out.n_nodes = (uint32_t)(out.nodes.size() / 16);
-    out.depth = b.max_depth;
+    out.n_nodes = (uint32_t)(out.nodes.size() / kWideWords);
+    if (out.depth > (uint32_t)kWideStack) throw std::length_error("wide BVH deeper than the traversal stack");
 }
 
 }  // namespace kz

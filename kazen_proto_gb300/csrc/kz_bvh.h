@@ -2,19 +2,9 @@
 //
 // Replaces the reference accelerators (BVHAccel, random-axis median split,
 // src/core/accel.cpp:83-183; EmbreeAccel HIGH-quality build,
-// src/core/accel.cpp:185-315) with a binned-SAH binary BVH whose nodes are
-// laid out for 16-byte vector fetches on the GPU.
-//
-// Device node (64 bytes, 4 x float4), both children's boxes in one node:
-//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   n3 = (link0, link1, count0, count1) as int32
-// link >= 0 is an inner node index; link < 0 is a leaf whose triangle records
-// start at ~link and number `count`. An empty child has an inverted box.
-// Triangle record (48 bytes, 3 x float4), in leaf order:
-//   (v0.xyz, global triangle id), (v1.xyz, geom id), (v2.xyz, material id)
-// with the integer fields stored as raw 32-bit patterns.
+// src/core/accel.cpp:185-315) with a binned-SAH binary BVH collapsed into an
+// 8-wide BVH with quantized child boxes, laid out for 16-byte vector fetches
+// on the GPU.
 #pragma once
 
 #include <cstdint>
@@ -29,18 +19,42 @@ struct BvhBuildInput {
     const int32_t* geom_material;  // material id per geom
 };
 
-struct BvhBuildOutput {
-    std::vector<float> nodes;      // n_nodes * 16 floats
+// The binary build: binned SAH (32 bins per axis), leaves of at most 3
+// triangles (larger only where the depth cap kMaxBvhDepth is hit; the wide
+// collapse halves those by count).
+constexpr int kMaxBvhDepth = 60;
+
+// 8-wide BVH with quantized child boxes, collapsed from a binned-SAH binary
+// BVH (leaves of at most 3 triangles). Node = 80 bytes, 20 x 32-bit words:
+//   w0..w2   p (float): lower corner of the node box
+//   w3       ex | ey << 8 | ez << 16 | imask << 24; an axis' quantum is
+//            2^(e - 127); imask bit s = slot s holds an inner node
+//   w4       index of the first inner child (inner children are consecutive,
+//            in slot order)
+//   w5       first triangle record of the node's leaves
+//   w6, w7   meta byte per slot: 0 empty; inner: 0x20 | (24 + s); leaf:
+//            (unary triangle count: 1, 3 or 7) << 5 | offset from w5
+//   w8..w19  per axis x, y, z: 8 low bytes (2 words) then 8 high bytes
+//            (2 words): child box = p + [q_lo, q_hi] * quantum, rounded
+//            outward so it contains the exact child box.
+// Slots are assigned so that slot s's child lies towards the octant
+// (+x if s & 1, +y if s & 2, +z if s & 4) of the node centre; a ray visits
+// inner children in the order of slot ^ (its direction octant), which
+// approximates near-first without sorting.
+// Triangle record (48 bytes, 3 x float4), in the order the leaves reference
+// them: (v0.xyz, global triangle id), (v1.xyz, geom id), (v2.xyz, material
+// id), the integer fields stored as raw 32-bit patterns.
+constexpr int kWideWords = 20;
+constexpr int kWideStack = 96;  // >= wide depth: binary depth cap + 32 count splits
+
+struct WideBvhOutput {
+    std::vector<uint32_t> nodes;   // n_nodes * kWideWords
     std::vector<float> tris;       // ntris * 12 floats
     std::vector<uint32_t> order;   // record -> global triangle id
     uint32_t n_nodes = 0;
-    uint32_t depth = 0;
+    uint32_t depth = 0;            // wide levels
 };
 
-// Binned SAH (32 bins per axis), at most `max_leaf` triangles per leaf
-// (larger only when centroids coincide or the depth limit is hit). Depth is
-// capped at kMaxBvhDepth so the fixed traversal stack cannot overflow.
-constexpr int kMaxBvhDepth = 60;
-void build_bvh(const BvhBuildInput& in, int max_leaf, BvhBuildOutput& out);
+void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out);
 
 }  // namespace kz

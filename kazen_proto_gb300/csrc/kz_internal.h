@@ -22,7 +22,7 @@ struct DevLight {
 };
 
 struct DevScene {
-    const float4* nodes = nullptr;      // n_nodes * 4
+    const uint4* nodes = nullptr;       // n_nodes * 5 (80-byte 8-wide nodes)
     const float4* tris = nullptr;       // n_tris * 3, leaf order
     uint32_t n_nodes = 0, n_tris = 0;
     const uint32_t* geom_offset = nullptr;  // first global triangle id per mesh

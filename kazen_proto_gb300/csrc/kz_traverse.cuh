@@ -9,20 +9,22 @@
 //  * closest hit in (tmin, tmax], equal t resolved to the smaller global
 //    triangle id, so the result is independent of traversal order and of the
 //    BVH shape (bit-exact against any exact restatement);
-//  * a binary BVH with both child boxes in one 64-byte node, read with
-//    16-byte non-coherent loads, near-child-first order and a short stack of
-//    (node, entry distance) pairs in local memory.
-// Box distances are widened by a relative margin far above their rounding
-// error, so no box holding a hit at t <= t_best is culled.
+//  * an 8-wide BVH with quantized child boxes (80-byte nodes, five 16-byte
+//    non-coherent loads), in the manner of H. Ylitie, T. Karras, S. Laine,
+//    "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+//    BVHs", HPG 2017: one node test yields a 32-bit mask of inner children
+//    (in an octant-derived near-first order) and leaf triangles; a stack of
+//    (child base, mask) groups in local memory.
+// Box distances are widened by a margin above their rounding error (see
+// wide_axis), so no box holding a hit at t <= t_best is culled.
 #pragma once
 
+#include "kz_bvh.h"
 #include "kz_device.cuh"
 
 namespace kz {
 
-constexpr int kStackSize = 64;
-constexpr float kBoxLo = 1.0f - 1.0f / 65536.0f;
-constexpr float kBoxHi = 1.0f + 1.0f / 65536.0f;
+static_assert(kWideWords == 20, "a wide node is five 16-byte vectors");
 
 struct TRay {
     f3 o, inv;
@@ -86,17 +88,34 @@ __device__ __forceinline__ bool tri_test(const TRay& r, float4 a, float4 b, floa
     return true;
 }
 
-__device__ __forceinline__ bool box_test(float lx, float hx, float ly, float hy, float lz, float hz, const TRay& r,
-                                         float tcur, float& tnear) {
-    const float tx0 = (lx - r.o.x) * r.inv.x, tx1 = (hx - r.o.x) * r.inv.x;
-    const float ty0 = (ly - r.o.y) * r.inv.y, ty1 = (hy - r.o.y) * r.inv.y;
-    const float tz0 = (lz - r.o.z) * r.inv.z, tz1 = (hz - r.o.z) * r.inv.z;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-    tn *= tn > 0.f ? kBoxLo : kBoxHi;
-    tf *= tf > 0.f ? kBoxHi : kBoxLo;
-    tnear = fmaxf(tn, r.tmin);
-    return tnear <= fminf(tf, tcur);
+// The same test with the barycentric divisions left to the caller:
+// u = V / det, v = W / det for the hit that is kept.
+__device__ __forceinline__ bool tri_test_t(const TRay& r, float4 a, float4 b, float4 c, float& t, float& V_, float& W_,
+                                           float& det_) {
+    const float okx = comp(r.o, r.kx), oky = comp(r.o, r.ky), okz = comp(r.o, r.kz);
+    const float Akx = pick(a, r.kx) - okx, Aky = pick(a, r.ky) - oky, Akz = pick(a, r.kz) - okz;
+    const float Bkx = pick(b, r.kx) - okx, Bky = pick(b, r.ky) - oky, Bkz = pick(b, r.kz) - okz;
+    const float Ckx = pick(c, r.kx) - okx, Cky = pick(c, r.ky) - oky, Ckz = pick(c, r.kz) - okz;
+    const float Ax = Akx - r.Sx * Akz, Ay = Aky - r.Sy * Akz;
+    const float Bx = Bkx - r.Sx * Bkz, By = Bky - r.Sy * Bkz;
+    const float Cx = Ckx - r.Sx * Ckz, Cy = Cky - r.Sy * Ckz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    const float det = U + V + W;
+    if (det == 0.f) return false;
+    const float T = U * (r.Sz * Akz) + V * (r.Sz * Bkz) + W * (r.Sz * Ckz);
+    t = T / det;
+    V_ = V;
+    W_ = W;
+    det_ = det;
+    return true;
 }
 
 struct HitRec {
@@ -105,29 +124,105 @@ struct HitRec {
     int32_t rec;    // triangle record, -1 on a miss
 };
 
-template <bool kCount>
-__device__ __forceinline__ void leaf_closest(const float4* __restrict__ tris, const TRay& r, int first, int count,
-                                             HitRec& h, uint32_t& ntri) {
-    for (int k = 0; k < count; ++k) {
-        const float4* tp = tris + (size_t)(first + k) * 3;
-        const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-        if (kCount) ++ntri;
-        float t, bu, bv;
-        if (!tri_test(r, a, b, c, t, bu, bv)) continue;
-        const uint32_t prim = __float_as_uint(a.w);
-        if (t > r.tmin && (t < h.t || (t == h.t && prim < h.prim))) {
-            h.t = t;
-            h.u = bu;
-            h.v = bv;
-            h.prim = prim;
-            h.rec = first + k;
-        }
-    }
+// ---- 8-wide quantized BVH (layout in kz_bvh.h) ------------------------------
+//
+// A child box plane at p + q * 2^E on one axis is reached at
+//   t(q) = (p + q 2^E - o) / d = b + q 2^E inv,  b = (p - o) inv.
+// The byte q becomes f = 1 + q 2^-15 with one byte permute (0x3F80_qq00 as
+// float bits), so t(q) = fma(f, A, B) with A = 2^(E+15) inv (exact: a power
+// of two times inv) and B = b - A. Each term carries rounding error below
+// 2^-24 (6 |b| + 3 |A|); the per-node margin 2^-16 (|b| + |A| / 32) exceeds it,
+// so the near plane is lowered and the far plane raised by more than any
+// rounding and no box holding a hit at t <= t_best is culled. An overflowing
+// A or b turns the axis' distances into NaN, which the min/max below ignore:
+// such an axis culls nothing.
+struct WideAxis {
+    float A, Bn, Bf;
+    uint32_t n0, n1, f0, f1;  // near / far plane bytes (slots 0-3, 4-7)
+};
+
+__device__ __forceinline__ WideAxis wide_axis(float p, uint32_t e, float o, float inv, uint4 q) {
+    WideAxis ax;
+    ax.A = __uint_as_float((e + 15u) << 23) * inv;
+    const float b = (p - o) * inv;
+    const float B = b - ax.A;
+    const float d = (fabsf(b) + fabsf(ax.A) * 0.03125f) * 1.52587890625e-05f;
+    ax.Bn = B - d;
+    ax.Bf = B + d;
+    const bool neg = inv < 0.f;  // entering through the high plane
+    ax.n0 = neg ? q.z : q.x;
+    ax.n1 = neg ? q.w : q.y;
+    ax.f0 = neg ? q.x : q.z;
+    ax.f1 = neg ? q.y : q.w;
+    return ax;
 }
 
-// Closest hit. Returns false only if the stack would overflow (ruled out by
-// the builder's depth cap) or more nodes are visited than the tree holds (a
-// corrupt node array); the caller reports KZ_ERR_STACK and the ray misses.
+template <int kSlot>
+__device__ __forceinline__ float wide_t(const WideAxis& ax, bool near_plane) {
+    const uint32_t w = near_plane ? (kSlot < 4 ? ax.n0 : ax.n1) : (kSlot < 4 ? ax.f0 : ax.f1);
+    const float f = __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((kSlot & 3) << 4)));
+    return fmaf(f, ax.A, near_plane ? ax.Bn : ax.Bf);
+}
+
+template <int kSlot>
+__device__ __forceinline__ void wide_slot(const WideAxis& X, const WideAxis& Y, const WideAxis& Z, uint32_t meta,
+                                          float tmin, float tcur, uint32_t& hits) {
+    const float tn = fmaxf(fmaxf(fmaxf(wide_t<kSlot>(X, true), wide_t<kSlot>(Y, true)), wide_t<kSlot>(Z, true)), tmin);
+    const float tf = fminf(fminf(fminf(wide_t<kSlot>(X, false), wide_t<kSlot>(Y, false)), wide_t<kSlot>(Z, false)), tcur);
+    const uint32_t m = (meta >> (8 * (kSlot & 3))) & 0xFFu;
+    if (tn <= tf) hits |= (m >> 5) << (m & 31u);
+}
+
+// Tests the 8 child boxes of a node. Returns the hit mask: bits 24-31 the
+// inner children in visiting order (bit 31 first), bits 0-23 the triangles
+// (relative to tri_base) of the leaves hit.
+__device__ __forceinline__ uint32_t wide_node(const uint4* __restrict__ np, const TRay& r, uint32_t octp, float tcur,
+                                              uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
+    const uint4 h0 = __ldg(np), h1 = __ldg(np + 1);
+    const uint4 qx = __ldg(np + 2), qy = __ldg(np + 3), qz = __ldg(np + 4);
+    child_base = h1.x;
+    tri_base = h1.y;
+    imask = h0.w >> 24;
+    const WideAxis X = wide_axis(__uint_as_float(h0.x), h0.w & 0xFFu, r.o.x, r.inv.x, qx);
+    const WideAxis Y = wide_axis(__uint_as_float(h0.y), (h0.w >> 8) & 0xFFu, r.o.y, r.inv.y, qy);
+    const WideAxis Z = wide_axis(__uint_as_float(h0.z), (h0.w >> 16) & 0xFFu, r.o.z, r.inv.z, qz);
+    // inner slots carry 24 + slot in their low bits; XOR the ray's octant in
+    // so that the nearest octant lands on bit 31
+    uint32_t m0 = h1.z, m1 = h1.w;
+    m0 ^= ((m0 >> 4) & (m0 >> 3) & 0x01010101u) * octp;
+    m1 ^= ((m1 >> 4) & (m1 >> 3) & 0x01010101u) * octp;
+    uint32_t hits = 0;
+    wide_slot<0>(X, Y, Z, m0, r.tmin, tcur, hits);
+    wide_slot<1>(X, Y, Z, m0, r.tmin, tcur, hits);
+    wide_slot<2>(X, Y, Z, m0, r.tmin, tcur, hits);
+    wide_slot<3>(X, Y, Z, m0, r.tmin, tcur, hits);
+    wide_slot<4>(X, Y, Z, m1, r.tmin, tcur, hits);
+    wide_slot<5>(X, Y, Z, m1, r.tmin, tcur, hits);
+    wide_slot<6>(X, Y, Z, m1, r.tmin, tcur, hits);
+    wide_slot<7>(X, Y, Z, m1, r.tmin, tcur, hits);
+    return hits;
+}
+
+// XOR mask that maps a slot to its visiting rank: 7 for the octant the ray
+// enters first (slot bits set on the axes whose direction is negative).
+__device__ __forceinline__ uint32_t wide_octant(const TRay& r) {
+    return 7u ^ ((r.inv.x < 0.f ? 1u : 0u) | (r.inv.y < 0.f ? 2u : 0u) | (r.inv.z < 0.f ? 4u : 0u));
+}
+
+// Next inner child of a node group (base, bits): bits 24-31 the remaining
+// hits in visiting order, bits 0-7 the node's inner-slot mask.
+__device__ __forceinline__ uint32_t wide_pop_child(uint32_t base, uint32_t& bits, uint32_t octp) {
+    const uint32_t pos = 31u - __clz(bits);
+    bits ^= 1u << pos;
+    const uint32_t slot = (pos - 24u) ^ octp;
+    return base + __popc(bits & ((1u << slot) - 1u));
+}
+
+// Closest hit in (tmin, tmax]. Returns false only if the stack would
+// overflow (the builder bounds the depth by the stack size) or more nodes are
+// visited than the tree holds (a corrupt node array); the caller reports
+// KZ_ERR_STACK and the ray misses. The barycentric divisions are done once,
+// for the final hit (the same IEEE divisions as tri_test).
 template <bool kCount>
 __device__ bool trace_closest(const DevScene& s, const TRay& r, float tmax, HitRec& h, uint32_t& nnode,
                               uint32_t& ntri) {
@@ -135,100 +230,103 @@ __device__ bool trace_closest(const DevScene& s, const TRay& r, float tmax, HitR
     h.u = h.v = 0.f;
     h.prim = KZ_INVALID_ID;
     h.rec = -1;
-    int stack_node[kStackSize];
-    float stack_t[kStackSize];
+    float bV = 0.f, bW = 0.f, bdet = 1.f;
+    const uint32_t octp = wide_octant(r);
+    uint2 stack[kWideStack];
     int sp = 0;
-    int node = 0;
+    uint32_t gbase = 0, gbits = 0x80000000u;  // the root as the only child of a virtual node
     uint32_t visits = 0;
+    bool ok = true;
     for (;;) {
-        if (++visits > s.n_nodes || (uint32_t)node >= s.n_nodes) return false;
-        const float4* np = s.nodes + (size_t)node * 4;
-        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-        const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        const uint32_t node = wide_pop_child(gbase, gbits, octp);
+        if (gbits > 0x00FFFFFFu) {
+            if (sp >= kWideStack) { ok = false; break; }
+            stack[sp++] = make_uint2(gbase, gbits);
+        }
+        if (++visits > s.n_nodes || node >= s.n_nodes) { ok = false; break; }
+        uint32_t tri_base, imask;
+        const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, h.t, gbase, tri_base, imask);
         if (kCount) ++nnode;
-        float tn0, tn1;
-        const bool h0 = box_test(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, h.t, tn0);
-        const bool h1 = box_test(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, h.t, tn1);
-        if (h0 && n3.x < 0) leaf_closest<kCount>(s.tris, r, ~n3.x, n3.z, h, ntri);
-        if (h1 && n3.y < 0) leaf_closest<kCount>(s.tris, r, ~n3.y, n3.w, h, ntri);
-        const bool g0 = h0 && n3.x >= 0 && tn0 <= h.t;
-        const bool g1 = h1 && n3.y >= 0 && tn1 <= h.t;
-        if (g0 && g1) {
-            int near = n3.x, far = n3.y;
-            float tfar = tn1;
-            if (tn1 < tn0) {
-                near = n3.y;
-                far = n3.x;
-                tfar = tn0;
+        gbits = (hm & 0xFF000000u) | imask;
+        uint32_t tbits = hm & 0x00FFFFFFu;
+        while (tbits) {
+            const uint32_t rec = tri_base + (__ffs(tbits) - 1);
+            tbits &= tbits - 1u;
+            if (rec >= s.n_tris) { ok = false; break; }
+            const float4* tp = s.tris + (size_t)rec * 3;
+            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (kCount) ++ntri;
+            float t, V, W, det;
+            if (!tri_test_t(r, a, b, c, t, V, W, det)) continue;
+            const uint32_t prim = __float_as_uint(a.w);
+            if (t > r.tmin && (t < h.t || (t == h.t && prim < h.prim))) {
+                h.t = t;
+                bV = V;
+                bW = W;
+                bdet = det;
+                h.prim = prim;
+                h.rec = (int32_t)rec;
             }
-            if (sp >= kStackSize) return false;
-            stack_node[sp] = far;
-            stack_t[sp] = tfar;
-            ++sp;
-            node = near;
-            continue;
         }
-        if (g0) { node = n3.x; continue; }
-        if (g1) { node = n3.y; continue; }
-        for (;;) {
-            if (sp == 0) return true;
-            --sp;
-            if (stack_t[sp] <= h.t) break;
+        if (!ok) break;
+        while (gbits <= 0x00FFFFFFu && sp > 0) {
+            const uint2 e = stack[--sp];
+            gbase = e.x;
+            gbits = e.y;
         }
-        node = stack_node[sp];
+        if (gbits <= 0x00FFFFFFu) break;
     }
+    if (!ok) {
+        h.t = tmax;
+        h.prim = KZ_INVALID_ID;
+        h.rec = -1;
+        return false;
+    }
+    if (h.rec >= 0) {
+        h.u = bV / bdet;
+        h.v = bW / bdet;
+    }
+    return true;
 }
 
-// Any hit in (tmin, tmax].
+// Any hit in (tmin, tmax]; `overflow` as for trace_closest.
 template <bool kCount>
 __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& overflow, uint32_t& nnode,
                           uint32_t& ntri) {
-    int stack_node[kStackSize];
+    const uint32_t octp = wide_octant(r);
+    uint2 stack[kWideStack];
     int sp = 0;
-    int node = 0;
+    uint32_t gbase = 0, gbits = 0x80000000u;
     uint32_t visits = 0;
     overflow = false;
     for (;;) {
-        if (++visits > s.n_nodes || (uint32_t)node >= s.n_nodes) {
-            overflow = true;
-            return false;
+        const uint32_t node = wide_pop_child(gbase, gbits, octp);
+        if (gbits > 0x00FFFFFFu) {
+            if (sp >= kWideStack) { overflow = true; return false; }
+            stack[sp++] = make_uint2(gbase, gbits);
         }
-        const float4* np = s.nodes + (size_t)node * 4;
-        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-        const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        if (++visits > s.n_nodes || node >= s.n_nodes) { overflow = true; return false; }
+        uint32_t tri_base, imask;
+        const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, tmax, gbase, tri_base, imask);
         if (kCount) ++nnode;
-        float tn0, tn1;
-        const bool h0 = box_test(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, tmax, tn0);
-        const bool h1 = box_test(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, tmax, tn1);
-        for (int side = 0; side < 2; ++side) {
-            const bool hit = side ? h1 : h0;
-            const int link = side ? n3.y : n3.x;
-            const int cnt = side ? n3.w : n3.z;
-            if (!hit || link >= 0) continue;
-            const int first = ~link;
-            for (int k = 0; k < cnt; ++k) {
-                const float4* tp = s.tris + (size_t)(first + k) * 3;
-                if (kCount) ++ntri;
-                float t, bu, bv;
-                if (tri_test(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), t, bu, bv) && t > r.tmin && t <= tmax)
-                    return true;
-            }
+        gbits = (hm & 0xFF000000u) | imask;
+        uint32_t tbits = hm & 0x00FFFFFFu;
+        while (tbits) {
+            const uint32_t rec = tri_base + (__ffs(tbits) - 1);
+            tbits &= tbits - 1u;
+            if (rec >= s.n_tris) { overflow = true; return false; }
+            const float4* tp = s.tris + (size_t)rec * 3;
+            if (kCount) ++ntri;
+            float t, V, W, det;
+            if (tri_test_t(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), t, V, W, det) && t > r.tmin && t <= tmax)
+                return true;
         }
-        const bool g0 = h0 && n3.x >= 0;
-        const bool g1 = h1 && n3.y >= 0;
-        if (g0 && g1) {
-            if (sp >= kStackSize) {
-                overflow = true;
-                return false;
-            }
-            stack_node[sp++] = n3.y;
-            node = n3.x;
-            continue;
+        while (gbits <= 0x00FFFFFFu && sp > 0) {
+            const uint2 e = stack[--sp];
+            gbase = e.x;
+            gbits = e.y;
         }
-        if (g0) { node = n3.x; continue; }
-        if (g1) { node = n3.y; continue; }
-        if (sp == 0) return false;
-        node = stack_node[--sp];
+        if (gbits <= 0x00FFFFFFu) return false;
     }
 }
 
