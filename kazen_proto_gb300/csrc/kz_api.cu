@@ -140,7 +140,7 @@ struct kz_scene {
     uint32_t* status_host = nullptr;  // pinned
 
     // batch scratch (host-memory calls)
-    DevBuf s_rays, s_t, s_prim, s_geom, s_u, s_v, s_occ, s_ctr;
+    DevBuf s_rays, s_t, s_prim, s_geom, s_u, s_v, s_occ, s_ctr, s_next;
 
     // wavefront buffers
     DevBuf pa[5], pb[5], sh[3], ctr, film, film64;
@@ -153,7 +153,7 @@ struct kz_scene {
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
         DevBuf* all[] = {&nodes, &tris, &geom_offset, &geom_light, &mats, &lights, &light_cdf, &light_tris,
-                         &status, &s_rays, &s_t, &s_prim, &s_geom, &s_u, &s_v, &s_occ, &s_ctr, &ctr, &film, &film64};
+                         &status, &s_rays, &s_t, &s_prim, &s_geom, &s_u, &s_v, &s_occ, &s_ctr, &s_next, &ctr, &film, &film64};
         for (DevBuf* b : all) b->release();
         for (auto& b : pa) b.release();
         for (auto& b : pb) b.release();
@@ -329,7 +329,7 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
                 kz::launch_trace_shadow_guided(s->dev, sq, cap, ctr, film, film64, gh->gs->recs, gh->gs->nee,
                                                pp.max_depth, block, strm);
             else
-                kz::launch_trace_shadow(s->dev, sq, cap, ctr, count, film, film64, block, strm);
+                kz::launch_trace_shadow_dev(s->dev, sq, cap, ctr, count, film, film64, strm);
             kz::launch_finish(ctr, strm);
             if (e) KZ_CUDA(cudaEventRecord(e[4], strm));
             st.kernel_launches += gh ? 7 : 6;
@@ -675,8 +675,11 @@ kz_status kz_intersect_closest(kz_scene* s, const kz_ray* rays, uint64_t n, kz_h
         KZ_CUDA(cudaStreamSynchronize(st));
         return KZ_OK;
     }
+    KZ_TRY(s->s_next.ensure(sizeof(unsigned long long)));
+    KZ_CUDA(cudaMemsetAsync(s->s_next.ptr, 0, sizeof(unsigned long long), st));
     if (mem == KZ_MEM_DEVICE) {
-        kz::launch_intersect_closest(s->dev, rays, n, hits, s->status.as<uint32_t>(), st);
+        kz::launch_intersect_closest(s->dev, rays, n, hits, s->s_next.as<unsigned long long>(),
+                                     s->status.as<uint32_t>(), st);
         KZ_CUDA(cudaGetLastError());
         return KZ_OK;
     }
@@ -689,7 +692,8 @@ kz_status kz_intersect_closest(kz_scene* s, const kz_ray* rays, uint64_t n, kz_h
     KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
     kz_hits dh{s->s_t.as<float>(), s->s_prim.as<uint32_t>(), hits.geom_id ? s->s_geom.as<uint32_t>() : nullptr,
                hits.u ? s->s_u.as<float>() : nullptr, hits.v ? s->s_v.as<float>() : nullptr};
-    kz::launch_intersect_closest(s->dev, s->s_rays.as<kz_ray>(), n, dh, s->status.as<uint32_t>(), st);
+    kz::launch_intersect_closest(s->dev, s->s_rays.as<kz_ray>(), n, dh, s->s_next.as<unsigned long long>(),
+                                 s->status.as<uint32_t>(), st);
     KZ_CUDA(cudaGetLastError());
     KZ_CUDA(cudaMemcpyAsync(hits.t, dh.t, n * 4, cudaMemcpyDeviceToHost, st));
     KZ_CUDA(cudaMemcpyAsync(hits.prim_id, dh.prim_id, n * 4, cudaMemcpyDeviceToHost, st));
@@ -1285,7 +1289,7 @@ extern "C" kz_status kz_scene_release_scratch(kz_scene* s) {
     if (!s->cuda_ready) return KZ_OK;
     KZ_CUDA(cudaSetDevice(s->device));
     KZ_CUDA(cudaStreamSynchronize(s->stream));
-    DevBuf* all[] = {&s->s_rays, &s->s_t, &s->s_prim, &s->s_geom, &s->s_u, &s->s_v, &s->s_occ, &s->s_ctr,
+    DevBuf* all[] = {&s->s_rays, &s->s_t, &s->s_prim, &s->s_geom, &s->s_u, &s->s_v, &s->s_occ, &s->s_ctr, &s->s_next,
                      &s->film, &s->film64};
     for (DevBuf* b : all) b->release();
     for (auto& b : s->pa) b.release();

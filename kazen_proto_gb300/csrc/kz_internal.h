@@ -124,6 +124,8 @@ struct DevCounters {
     unsigned long long path_bounces, shadow_rays, iterations;
     unsigned long long gen_first;  // first path id generated this iteration
     uint32_t gen_count, gen_slot;  // how many, and where in the buffer
+    uint32_t trace_next;           // persistent kernels: next path / shadow ray to fetch
+    uint32_t shadow_next;
 };
 
 // One job of a batched render: its scene, camera and film.
@@ -142,8 +144,9 @@ struct BatchCounters {
 };
 
 // ---- launchers (kz_kernels.cu) -------------------------------------------
+// `next` is a zeroed 64-bit fetch counter for the persistent kernel.
 void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
-                              uint32_t* status, cudaStream_t st);
+                              unsigned long long* next, uint32_t* status, cudaStream_t st);
 void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ,
                           uint32_t* status, cudaStream_t st);
 void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n,
@@ -187,6 +190,9 @@ void launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, ui
 void launch_guide_adam(float* w, float* m, float* v, const float* grad, __nv_bfloat16* wbf, float lr, int step,
                        cudaStream_t st);
 void launch_guide_to_bf16(const float* w, __nv_bfloat16* wbf, cudaStream_t st);
+// Persistent shadow pass of the device-driven loop.
+void launch_trace_shadow_dev(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
+                             float* film, double* film64, cudaStream_t st);
 void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
                          float* film, double* film64, uint32_t block, cudaStream_t st);
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st);

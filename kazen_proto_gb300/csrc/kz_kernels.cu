@@ -10,6 +10,7 @@
 // vertex in a fixed order whatever branches run:
 //   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
 //   [5] lobe pick   [6,7,8] lobe sample
+#include <algorithm>
 #include "kz_guide.cuh"
 #include "kz_internal.h"
 #include "kz_traverse.cuh"
@@ -40,21 +41,7 @@ __device__ __forceinline__ uint32_t warp_append(bool pred, uint32_t* counter) {
 }
 
 // ------------------------------------------------------------------ batch intersection
-__global__ void k_intersect_closest(DevScene s, const kz_ray* __restrict__ rays, uint64_t n, kz_hits hits,
-                                    uint32_t* status) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    const float4 a = __ldg(rp), b = __ldg(rp + 1);
-    TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
-    HitRec h;
-    uint32_t dn = 0, dt = 0;
-    if (!trace_closest<false>(s, r, b.w, h, dn, dt)) {
-        set_status(status, KZ_ERR_STACK);
-        h.t = b.w;
-        h.prim = KZ_INVALID_ID;
-        h.rec = -1;
-    }
+__device__ __forceinline__ void store_hit(const DevScene& s, kz_hits hits, uint64_t i, const HitRec& h) {
     hits.t[i] = h.t;
     uint32_t geom = KZ_INVALID_ID, local = KZ_INVALID_ID;
     if (h.rec >= 0) {
@@ -213,6 +200,67 @@ __global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint
         p.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec));
     }
     if (kCount) warp_count(dn, dt, &ctr->fetch[0]);
+}
+
+// Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
+// ray up, store(k, hit) writes the result.
+template <bool kCount, typename Ctr, typename Load, typename Store>
+__device__ __forceinline__ void persistent_closest(const DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
+                                                   Store store, uint32_t& dn, uint32_t& dt) {
+    uint2 stack[kWideStack];
+    ClosestState c;
+    TRay r;
+    float tmax = 0.f;
+    uint32_t octp = 0;
+    Ctr ray = 0;
+    persistent_rays(
+        n, next, kTraceRefill,
+        [&](Ctr k) {
+            ray = k;
+            load(k, r, tmax);
+            octp = wide_octant(r);
+            closest_begin(c, tmax);
+        },
+        [&]() {
+            const int rc = closest_step<kCount>(s, r, octp, c, stack, dn, dt);
+            if (rc == 0) return false;
+            HitRec h;
+            closest_finish(c, rc > 0, tmax, h);
+            if (rc < 0) set_status(status, KZ_ERR_STACK);
+            store(ray, h);
+            return true;
+        });
+}
+
+// Closest-hit pass of the device-driven loop (k_plan zeroes trace_next).
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_trace_paths_persistent(DevScene s, PathSoA p, DevCounters* ctr) {
+    uint32_t dn = 0, dt = 0;
+    persistent_closest<kCount>(
+        s, ctr->n_active, &ctr->trace_next, &ctr->status,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = p.o4[k], d = p.d4[k];
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = __int_as_float(0x7f800000);
+        },
+        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
+    if (kCount) warp_count(dn, dt, &ctr->fetch[0]);
+}
+
+// kz_intersect_closest: rays (o, tmin, d, tmax) in, hit fields out.
+__global__ void __launch_bounds__(256) k_intersect_closest_persistent(DevScene s, const kz_ray* __restrict__ rays,
+                                                                      unsigned long long n, kz_hits hits,
+                                                                      unsigned long long* next, uint32_t* status) {
+    uint32_t dn = 0, dt = 0;
+    persistent_closest<false>(
+        s, n, next, status,
+        [&](unsigned long long k, TRay& r, float& tmax) {
+            const float4* rp = reinterpret_cast<const float4*>(rays + k);
+            const float4 a = __ldg(rp), b = __ldg(rp + 1);
+            r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
+            tmax = b.w;
+        },
+        [&](unsigned long long k, const HitRec& h) { store_hit(s, hits, k, h); }, dn, dt);
 }
 
 __device__ __forceinline__ void film_add(float* film, double* film64, uint32_t idx, f3 c) {
@@ -588,6 +636,47 @@ __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, 
     if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
 }
 
+// Persistent form of k_trace_shadow for the device-driven loop (k_plan zeroes
+// shadow_next each iteration).
+template <bool kCount, bool kGuided>
+__global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, ShadowSoA sq, DevCounters* ctr,
+                                                                 float* film, double* film64, VRec* recs, NRec* nee,
+                                                                 uint32_t max_depth) {
+    uint32_t dn = 0, dt = 0;
+    uint2 stack[kWideStack];
+    AnyState c;
+    TRay r;
+    float tmax = 0.f;
+    uint32_t octp = 0, ray = 0;
+    persistent_rays(
+        ctr->n_shadow, &ctr->shadow_next, kTraceRefill,
+        [&](uint32_t k) {
+            ray = k;
+            const float4 o = sq.o4[k], d = sq.d4[k];
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = o.w;
+            octp = wide_octant(r);
+            any_begin(c);
+        },
+        [&]() {
+            const int rc = any_step<kCount>(s, r, octp, tmax, c, stack, dn, dt);
+            if (rc == 0) return false;
+            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
+            if (rc == 1) {
+                const float4 cc = sq.c4[ray];
+                film_add(film, film64, __float_as_uint(sq.d4[ray].w), xyz(cc));
+                if (kGuided && recs) {
+                    const uint32_t tag = __float_as_uint(cc.w);
+                    const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
+                    propagate(recs, rb, tag & 15u, xyz(cc));
+                    if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
+                }
+            }
+            return true;
+        });
+    if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
+}
+
 // Training samples from the records of a guided pass: every valid vertex
 // whose integrand estimate L*f*cos is positive, weighted by its luminance
 // over the pdf the direction was sampled with.
@@ -734,6 +823,8 @@ __global__ void k_plan(DevCounters* c, uint32_t cap) {
     c->n_active += n_new;
     c->n_next = 0;
     c->n_shadow = 0;
+    c->trace_next = 0;
+    c->shadow_next = 0;
     if (c->n_active) {
         c->iterations += 1;
         c->path_bounces += c->n_active;
@@ -767,12 +858,24 @@ __global__ void k_scale(float* film, double* film64, uint64_t n, float sf, doubl
 
 inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
+// Blocks of `block` threads resident on the whole device for kernel f.
+template <typename F>
+static unsigned resident_grid(F f, unsigned block) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, (int)block, 0);
+    return (unsigned)(sms > 0 ? sms : 1) * (unsigned)(per_sm > 0 ? per_sm : 1);
+}
+
 }  // namespace
 
-void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits, uint32_t* status,
-                              cudaStream_t st) {
+void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
+                              unsigned long long* next, uint32_t* status, cudaStream_t st) {
     if (!n) return;
-    k_intersect_closest<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, hits, status);
+    static const unsigned g = resident_grid(k_intersect_closest_persistent, 256);
+    k_intersect_closest_persistent<<<(unsigned)std::min<uint64_t>(g, grid_for(n, 256)), 256, 0, st>>>(s, rays, n, hits,
+                                                                                                     next, status);
 }
 void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ, uint32_t* status,
                           cudaStream_t st) {
@@ -810,11 +913,18 @@ void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* c
     if (count) k_trace_paths<true><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
     else k_trace_paths<false><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
 }
-void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t block,
+// The device-driven loop's closest-hit pass: persistent, 256-thread blocks,
+// as many as are resident.
+void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t,
                             cudaStream_t st) {
     if (!cap) return;
-    if (count) k_trace_paths<true><<<grid_for(cap, block), block, 0, st>>>(s, p, cap, ctr, &ctr->n_active);
-    else k_trace_paths<false><<<grid_for(cap, block), block, 0, st>>>(s, p, cap, ctr, &ctr->n_active);
+    if (count) {
+        static const unsigned g = resident_grid(k_trace_paths_persistent<true>, 256);
+        k_trace_paths_persistent<true><<<std::min(g, grid_for(cap, 256)), 256, 0, st>>>(s, p, ctr);
+    } else {
+        static const unsigned g = resident_grid(k_trace_paths_persistent<false>, 256);
+        k_trace_paths_persistent<false><<<std::min(g, grid_for(cap, 256)), 256, 0, st>>>(s, p, ctr);
+    }
 }
 void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st) { k_plan<<<1, 1, 0, st>>>(ctr, cap); }
 void launch_finish(DevCounters* ctr, cudaStream_t st) { k_finish<<<1, 1, 0, st>>>(ctr); }
@@ -855,8 +965,22 @@ void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max,
                                 double* film64, VRec* recs, NRec* nee, uint32_t max_depth, uint32_t block,
                                 cudaStream_t st) {
     if (!n_max) return;
-    k_trace_shadow<false, true><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, recs, nee,
-                                                                         max_depth);
+    static const unsigned g = resident_grid(k_trace_shadow_persistent<false, true>, 256);
+    k_trace_shadow_persistent<false, true><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
+        s, sq, ctr, film, film64, recs, nee, max_depth);
+}
+void launch_trace_shadow_dev(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
+                             float* film, double* film64, cudaStream_t st) {
+    if (!n_max) return;
+    if (count) {
+        static const unsigned g = resident_grid(k_trace_shadow_persistent<true, false>, 256);
+        k_trace_shadow_persistent<true, false><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
+            s, sq, ctr, film, film64, nullptr, nullptr, 0);
+    } else {
+        static const unsigned g = resident_grid(k_trace_shadow_persistent<false, false>, 256);
+        k_trace_shadow_persistent<false, false><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
+            s, sq, ctr, film, film64, nullptr, nullptr, 0);
+    }
 }
 void launch_guide_collect(const VRec* recs, const NRec* nee, uint64_t n_recs, float4* samples, uint32_t cap,
                           uint32_t* count, float* wsum, cudaStream_t st) {

@@ -218,115 +218,207 @@ __device__ __forceinline__ uint32_t wide_pop_child(uint32_t base, uint32_t& bits
     return base + __popc(bits & ((1u << slot) - 1u));
 }
 
-// Closest hit in (tmin, tmax]. Returns false only if the stack would
-// overflow (the builder bounds the depth by the stack size) or more nodes are
-// visited than the tree holds (a corrupt node array); the caller reports
-// KZ_ERR_STACK and the ray misses. The barycentric divisions are done once,
-// for the final hit (the same IEEE divisions as tri_test).
+// Closest-hit traversal state, advanced one node at a time (closest_step) so
+// that persistent kernels can interleave rays; trace_closest runs it to the
+// end. The barycentric divisions are deferred to closest_finish (the same
+// IEEE divisions as tri_test, for the kept hit only).
+struct ClosestState {
+    float t, V, W, det;
+    uint32_t prim;
+    int32_t rec;
+    uint32_t gbase, gbits;  // current node group
+    uint32_t visits;
+    int sp;
+};
+
+__device__ __forceinline__ void closest_begin(ClosestState& c, float tmax) {
+    c.t = tmax;
+    c.V = c.W = 0.f;
+    c.det = 1.f;
+    c.prim = KZ_INVALID_ID;
+    c.rec = -1;
+    c.gbase = 0;
+    c.gbits = 0x80000000u;  // the root as the only child of a virtual node
+    c.visits = 0;
+    c.sp = 0;
+}
+
+// Visits one node and tests its leaf triangles. Returns 0 while nodes remain,
+// 1 when the traversal is complete, -1 if it must abort: the stack would
+// overflow (the builder bounds the depth by the stack size), more nodes are
+// visited than the tree holds, or a record index is out of range (a corrupt
+// node array).
+template <bool kCount>
+__device__ __forceinline__ int closest_step(const DevScene& s, const TRay& r, uint32_t octp, ClosestState& c,
+                                            uint2* stack, uint32_t& nnode, uint32_t& ntri) {
+    const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
+    if (c.gbits > 0x00FFFFFFu) {
+        if (c.sp >= kWideStack) return -1;
+        stack[c.sp++] = make_uint2(c.gbase, c.gbits);
+    }
+    if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
+    uint32_t tri_base, imask;
+    const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, c.t, c.gbase, tri_base, imask);
+    if (kCount) ++nnode;
+    c.gbits = (hm & 0xFF000000u) | imask;
+    uint32_t tbits = hm & 0x00FFFFFFu;
+    while (tbits) {
+        const uint32_t rec = tri_base + (__ffs(tbits) - 1);
+        tbits &= tbits - 1u;
+        if (rec >= s.n_tris) return -1;
+        const float4* tp = s.tris + (size_t)rec * 3;
+        const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+        if (kCount) ++ntri;
+        float t, V, W, det;
+        if (!tri_test_t(r, a, b, cc, t, V, W, det)) continue;
+        const uint32_t prim = __float_as_uint(a.w);
+        if (t > r.tmin && (t < c.t || (t == c.t && prim < c.prim))) {
+            c.t = t;
+            c.V = V;
+            c.W = W;
+            c.det = det;
+            c.prim = prim;
+            c.rec = (int32_t)rec;
+        }
+    }
+    while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
+        const uint2 e = stack[--c.sp];
+        c.gbase = e.x;
+        c.gbits = e.y;
+    }
+    return c.gbits <= 0x00FFFFFFu ? 1 : 0;
+}
+
+// Hit record of a finished traversal; an aborted one (ok == false) misses.
+__device__ __forceinline__ void closest_finish(const ClosestState& c, bool ok, float tmax, HitRec& h) {
+    if (!ok || c.rec < 0) {
+        h.t = ok ? c.t : tmax;
+        h.u = h.v = 0.f;
+        h.prim = KZ_INVALID_ID;
+        h.rec = -1;
+        return;
+    }
+    h.t = c.t;
+    h.u = c.V / c.det;
+    h.v = c.W / c.det;
+    h.prim = c.prim;
+    h.rec = c.rec;
+}
+
+// Closest hit in (tmin, tmax]. Returns false if the traversal aborted
+// (closest_step == -1); the caller reports KZ_ERR_STACK and the ray misses.
 template <bool kCount>
 __device__ bool trace_closest(const DevScene& s, const TRay& r, float tmax, HitRec& h, uint32_t& nnode,
                               uint32_t& ntri) {
-    h.t = tmax;
-    h.u = h.v = 0.f;
-    h.prim = KZ_INVALID_ID;
-    h.rec = -1;
-    float bV = 0.f, bW = 0.f, bdet = 1.f;
     const uint32_t octp = wide_octant(r);
     uint2 stack[kWideStack];
-    int sp = 0;
-    uint32_t gbase = 0, gbits = 0x80000000u;  // the root as the only child of a virtual node
-    uint32_t visits = 0;
-    bool ok = true;
-    for (;;) {
-        const uint32_t node = wide_pop_child(gbase, gbits, octp);
-        if (gbits > 0x00FFFFFFu) {
-            if (sp >= kWideStack) { ok = false; break; }
-            stack[sp++] = make_uint2(gbase, gbits);
-        }
-        if (++visits > s.n_nodes || node >= s.n_nodes) { ok = false; break; }
-        uint32_t tri_base, imask;
-        const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, h.t, gbase, tri_base, imask);
-        if (kCount) ++nnode;
-        gbits = (hm & 0xFF000000u) | imask;
-        uint32_t tbits = hm & 0x00FFFFFFu;
-        while (tbits) {
-            const uint32_t rec = tri_base + (__ffs(tbits) - 1);
-            tbits &= tbits - 1u;
-            if (rec >= s.n_tris) { ok = false; break; }
-            const float4* tp = s.tris + (size_t)rec * 3;
-            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-            if (kCount) ++ntri;
-            float t, V, W, det;
-            if (!tri_test_t(r, a, b, c, t, V, W, det)) continue;
-            const uint32_t prim = __float_as_uint(a.w);
-            if (t > r.tmin && (t < h.t || (t == h.t && prim < h.prim))) {
-                h.t = t;
-                bV = V;
-                bW = W;
-                bdet = det;
-                h.prim = prim;
-                h.rec = (int32_t)rec;
-            }
-        }
-        if (!ok) break;
-        while (gbits <= 0x00FFFFFFu && sp > 0) {
-            const uint2 e = stack[--sp];
-            gbase = e.x;
-            gbits = e.y;
-        }
-        if (gbits <= 0x00FFFFFFu) break;
-    }
-    if (!ok) {
-        h.t = tmax;
-        h.prim = KZ_INVALID_ID;
-        h.rec = -1;
-        return false;
-    }
-    if (h.rec >= 0) {
-        h.u = bV / bdet;
-        h.v = bW / bdet;
-    }
-    return true;
+    ClosestState c;
+    closest_begin(c, tmax);
+    int rc;
+    do {
+        rc = closest_step<kCount>(s, r, octp, c, stack, nnode, ntri);
+    } while (rc == 0);
+    closest_finish(c, rc > 0, tmax, h);
+    return rc > 0;
 }
 
-// Any hit in (tmin, tmax]; `overflow` as for trace_closest.
+// Any-hit traversal state, advanced one node at a time like ClosestState.
+struct AnyState {
+    uint32_t gbase, gbits;
+    uint32_t visits;
+    int sp;
+};
+
+__device__ __forceinline__ void any_begin(AnyState& c) {
+    c.gbase = 0;
+    c.gbits = 0x80000000u;
+    c.visits = 0;
+    c.sp = 0;
+}
+
+// One node of an any-hit query in (tmin, tmax]: 0 while nodes remain, 1 no
+// hit (complete), 2 hit, -1 abort (as closest_step).
+template <bool kCount>
+__device__ __forceinline__ int any_step(const DevScene& s, const TRay& r, uint32_t octp, float tmax, AnyState& c,
+                                        uint2* stack, uint32_t& nnode, uint32_t& ntri) {
+    const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
+    if (c.gbits > 0x00FFFFFFu) {
+        if (c.sp >= kWideStack) return -1;
+        stack[c.sp++] = make_uint2(c.gbase, c.gbits);
+    }
+    if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
+    uint32_t tri_base, imask;
+    const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, tmax, c.gbase, tri_base, imask);
+    if (kCount) ++nnode;
+    c.gbits = (hm & 0xFF000000u) | imask;
+    uint32_t tbits = hm & 0x00FFFFFFu;
+    while (tbits) {
+        const uint32_t rec = tri_base + (__ffs(tbits) - 1);
+        tbits &= tbits - 1u;
+        if (rec >= s.n_tris) return -1;
+        const float4* tp = s.tris + (size_t)rec * 3;
+        if (kCount) ++ntri;
+        float t, V, W, det;
+        if (tri_test_t(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), t, V, W, det) && t > r.tmin && t <= tmax)
+            return 2;
+    }
+    while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
+        const uint2 e = stack[--c.sp];
+        c.gbase = e.x;
+        c.gbits = e.y;
+    }
+    return c.gbits <= 0x00FFFFFFu ? 1 : 0;
+}
+
+// Any hit in (tmin, tmax]; `overflow` is set when the traversal aborted
+// (any_step == -1; the caller reports KZ_ERR_STACK).
 template <bool kCount>
 __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& overflow, uint32_t& nnode,
                           uint32_t& ntri) {
     const uint32_t octp = wide_octant(r);
     uint2 stack[kWideStack];
-    int sp = 0;
-    uint32_t gbase = 0, gbits = 0x80000000u;
-    uint32_t visits = 0;
-    overflow = false;
+    AnyState c;
+    any_begin(c);
+    int rc;
+    do {
+        rc = any_step<kCount>(s, r, octp, tmax, c, stack, nnode, ntri);
+    } while (rc == 0);
+    overflow = rc < 0;
+    return rc == 2;
+}
+
+// Persistent ray loop: each warp keeps its lanes busy by fetching new rays
+// (one atomic per warp) whenever at least `refill` of its lanes are idle,
+// instead of running until its slowest ray ends. Warp-synchronous: one ballot
+// per step; start(k) sets up ray k on the calling lane, step() advances it by
+// one node and returns true once the ray is finished and its result written.
+// Every traversal is bounded, so a warp leaves once the queue [0, n) is
+// drained. Refilling only in groups (8 lanes) keeps the set-up code from
+// running for one or two lanes at a time.
+constexpr uint32_t kTraceRefill = 8;
+
+template <typename Ctr, typename Start, typename Step>
+__device__ __forceinline__ void persistent_rays(Ctr n, Ctr* next, uint32_t refill, Start start, Step step) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool busy = false, more = true;
     for (;;) {
-        const uint32_t node = wide_pop_child(gbase, gbits, octp);
-        if (gbits > 0x00FFFFFFu) {
-            if (sp >= kWideStack) { overflow = true; return false; }
-            stack[sp++] = make_uint2(gbase, gbits);
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
+        if (!more && idle == 0xFFFFFFFFu) break;
+        const uint32_t n_idle = __popc(idle);
+        if (more && n_idle >= refill) {
+            Ctr base = 0;
+            if (lane == 0) base = atomicAdd(next, (Ctr)n_idle);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + n_idle >= n) more = false;
+            if (!busy) {
+                const Ctr k = base + __popc(idle & ((1u << lane) - 1u));
+                if (k < n) {
+                    busy = true;
+                    start(k);
+                }
+            }
         }
-        if (++visits > s.n_nodes || node >= s.n_nodes) { overflow = true; return false; }
-        uint32_t tri_base, imask;
-        const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, tmax, gbase, tri_base, imask);
-        if (kCount) ++nnode;
-        gbits = (hm & 0xFF000000u) | imask;
-        uint32_t tbits = hm & 0x00FFFFFFu;
-        while (tbits) {
-            const uint32_t rec = tri_base + (__ffs(tbits) - 1);
-            tbits &= tbits - 1u;
-            if (rec >= s.n_tris) { overflow = true; return false; }
-            const float4* tp = s.tris + (size_t)rec * 3;
-            if (kCount) ++ntri;
-            float t, V, W, det;
-            if (tri_test_t(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), t, V, W, det) && t > r.tmin && t <= tmax)
-                return true;
-        }
-        while (gbits <= 0x00FFFFFFu && sp > 0) {
-            const uint2 e = stack[--sp];
-            gbase = e.x;
-            gbits = e.y;
-        }
-        if (gbits <= 0x00FFFFFFu) return false;
+        if (busy && step()) busy = false;
     }
 }
 
