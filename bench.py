@@ -291,8 +291,8 @@ def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
 # ---------------------------------------------------------------- batched uneven jobs
 def batch_bench(n_jobs=256):
     """256 seeded soup jobs (50k-500k triangles; 64..512 squared; 4/16/64
-    spp; depth 4 or 8): one persistent launch (CUDA graph, autotuned) against
-    the same jobs rendered one kz_render call each."""
+    spp; depth 4 or 8): one kz_render_batch call (autotuned mode and shape,
+    CUDA graphs) against the same jobs rendered one kz_render call each."""
     from kazen_proto_gb300 import api, autotune, scenes
 
     t0 = time.perf_counter()
@@ -317,6 +317,11 @@ def batch_bench(n_jobs=256):
         bounces_single += r.last_stats["path_bounces"]
         errs.append(float(np.abs(img - ref).max() / max(1e-6, float(np.abs(ref).max()))))
         j["scene"].release_scratch()
+    # the megakernel mode at its defaults, for comparison
+    mcfg = api.batch_config(mode=api.BATCH_MEGAKERNEL, use_graph=True)
+    t0 = time.perf_counter()
+    _, mst = api.render_batch(jobs, mcfg)
+    wall_m = time.perf_counter() - t0
     for j in jobs:
         j["scene"].close()
     mb = st["path_bounces"] / (st["device_ms"] / 1e3) / 1e6
@@ -325,6 +330,9 @@ def batch_bench(n_jobs=256):
             "autotuned": best, "autotune_candidates": len(table), "persistent_lanes": st["threads"],
             "batched_graph": {"device_ms": round(st["device_ms"], 2), "wall_s": round(wall_b, 3),
                               "mpaths_bounces_per_s": round(mb, 1)},
+            "megakernel_graph": {"device_ms": round(mst["device_ms"], 2), "wall_s": round(wall_m, 3),
+                                 "mpaths_bounces_per_s": round(mst["path_bounces"] / (mst["device_ms"] / 1e3) / 1e6,
+                                                               1)},
             "one_launch_each": {"wall_s": round(singles_wall, 3),
                                 "mpaths_bounces_per_s": round(bounces_single / singles_wall / 1e6, 1)},
             "speedup_wall": round(singles_wall / wall_b, 3),

@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define KZ_ABI_VERSION 1
+#define KZ_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 typedef int32_t kz_status;
@@ -312,12 +312,20 @@ kz_status kz_render_guided(kz_scene* scene, kz_guide* guide, const kz_camera* ca
 
 /* ---- batched rendering ------------------------------------------------------
  * Many independent jobs (each its own scene, camera, film, spp and depth) in
- * one persistent kernel launch, optionally captured in a CUDA graph: lanes
- * keep a path each and refill from a global path counter every
- * refill_period vertices. Not in the reference (its renderer runs one scene
- * at a time, src/core/renderer.cpp:18-90); every job's film equals what
- * kz_render produces for it (same PCG32 streams). All scenes must be built
- * on the same device; the call runs on the first job's scene stream. */
+ * one call. Not in the reference (its renderer runs one scene at a time,
+ * src/core/renderer.cpp:18-90); every job's film equals what kz_render
+ * produces for it (same PCG32 streams). Two modes:
+ *  KZ_BATCH_WAVEFRONT (default): one wavefront over all jobs' paths, driven
+ *    by device counters; the stage kernels find each path's scene, camera and
+ *    film through its job index, so small jobs share the GPU instead of
+ *    underfilling it. With use_graph, each batch of iterations is one CUDA
+ *    graph launch (one host synchronisation per batch).
+ *  KZ_BATCH_MEGAKERNEL: one persistent kernel; lanes keep a path each and
+ *    refill from a global path counter every refill_period vertices.
+ * All scenes must be built on the same device; the call runs on the first
+ * job's scene stream. */
+#define KZ_BATCH_WAVEFRONT  0
+#define KZ_BATCH_MEGAKERNEL 1
 typedef struct kz_batch_job {
     kz_scene* scene;
     kz_camera camera;
@@ -328,17 +336,21 @@ typedef struct kz_batch_job {
 } kz_batch_job;
 
 typedef struct kz_batch_config {
-    uint32_t block_size;        /* threads per block (0 = 128)               */
-    uint32_t ctas_per_sm;       /* resident blocks per SM (0 = 2)            */
-    uint32_t refill_period;     /* vertices between lane refills (0 = 1)     */
+    uint32_t block_size;        /* threads per block (0 = 256 wavefront,
+                                   128 megakernel)                           */
+    uint32_t ctas_per_sm;       /* megakernel: resident blocks per SM (0 = 2) */
+    uint32_t refill_period;     /* megakernel: vertices between lane refills
+                                   (0 = 1)                                   */
     uint32_t use_graph;         /* 1: launch through a captured CUDA graph   */
+    uint32_t mode;              /* KZ_BATCH_WAVEFRONT or KZ_BATCH_MEGAKERNEL */
+    uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^21)     */
 } kz_batch_config;
 
 typedef struct kz_batch_stats {
     uint64_t paths;
     uint64_t path_bounces;
     uint64_t shadow_rays;
-    uint64_t threads;           /* persistent lanes (the wavefront in flight) */
+    uint64_t threads;           /* paths in flight (wavefront slots or lanes) */
     double   device_ms;         /* CUDA-event time of the launch (graph)      */
 } kz_batch_stats;
 

@@ -110,7 +110,7 @@ class KzBatchJob(C.Structure):
 
 class KzBatchConfig(C.Structure):
     _fields_ = [("block_size", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("refill_period", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("mode", C.c_uint32), ("wavefront_size", C.c_uint32)]
 
 
 class KzBatchStats(C.Structure):

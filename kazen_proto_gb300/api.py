@@ -451,18 +451,26 @@ def render_guided(scene: Scene, guide: Guide, camera: Camera, width: int, height
 
 
 # ---------------------------------------------------------------- batched rendering
-def batch_config(block_size=0, ctas_per_sm=0, refill_period=0, use_graph=True) -> N.KzBatchConfig:
+BATCH_WAVEFRONT = 0
+BATCH_MEGAKERNEL = 1
+
+
+def batch_config(block_size=0, ctas_per_sm=0, refill_period=0, use_graph=True, mode=BATCH_WAVEFRONT,
+                 wavefront_size=0) -> N.KzBatchConfig:
     c = N.KzBatchConfig()
     c.block_size = block_size
     c.ctas_per_sm = ctas_per_sm
     c.refill_period = refill_period
     c.use_graph = 1 if use_graph else 0
+    c.mode = mode
+    c.wavefront_size = wavefront_size
     return c
 
 
 def render_batch(jobs, cfg=None):
     """jobs: list of dicts {scene, camera, width, height, spp, max_depth, seed[, rr_min_depth]}.
-    Returns (list of (H, W, 3) images, stats). One persistent launch for all jobs."""
+    Returns (list of (H, W, 3) images, stats). All jobs in one wavefront (or one
+    persistent megakernel launch, cfg.mode = BATCH_MEGAKERNEL)."""
     arr = (N.KzBatchJob * len(jobs))()
     outs = []
     for k, j in enumerate(jobs):

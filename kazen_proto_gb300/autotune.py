@@ -1,8 +1,8 @@
-"""Autotuner of the persistent batch renderer (kz_render_batch).
+"""Autotuner of the batch renderer (kz_render_batch).
 
-Sweeps block size, resident blocks per SM (together the number of
-persistent lanes: the wavefront in flight) and the lane refill period on a
-sample of the jobs, keeps the fastest by CUDA-event time, and stores it in
+Sweeps, on a sample of the jobs, the wavefront mode's paths in flight and
+block size, and the megakernel mode's block size, resident blocks per SM and
+lane refill period; keeps the fastest by CUDA-event time and stores it in
 kazen_proto_gb300/_build/autotune.json for later calls on the same machine.
 """
 from __future__ import annotations
@@ -15,21 +15,34 @@ from . import api
 HERE = os.path.dirname(os.path.abspath(__file__))
 PATH = os.path.join(HERE, "_build", "autotune.json")
 
+WAVEFRONT_SIZES = (1 << 19, 1 << 20, 1 << 21, 1 << 22)
+WAVE_BLOCKS = (128, 256)
 BLOCKS = (64, 128, 256)
 CTAS_PER_SM = (1, 2, 4)
 PERIODS = (1, 2, 4)
+
+
+def candidates():
+    out = [{"mode": api.BATCH_WAVEFRONT, "block_size": b, "wavefront_size": w}
+           for w in WAVEFRONT_SIZES for b in WAVE_BLOCKS]
+    out += [{"mode": api.BATCH_MEGAKERNEL, "block_size": b, "ctas_per_sm": c, "refill_period": p}
+            for b in BLOCKS for c in CTAS_PER_SM for p in PERIODS]
+    return out
+
+
+def config_of(c, use_graph=True):
+    return api.batch_config(c.get("block_size", 0), c.get("ctas_per_sm", 0), c.get("refill_period", 0), use_graph,
+                            c.get("mode", api.BATCH_WAVEFRONT), c.get("wavefront_size", 0))
 
 
 def tune(jobs, reps=2, save=True):
     """jobs: built batch jobs (see scenes.build_batch_scenes). Returns
     (best config dict, table of (config, ms))."""
     table = []
-    for b in BLOCKS:
-        for c in CTAS_PER_SM:
-            for p in PERIODS:
-                cfg = api.batch_config(b, c, p, use_graph=True)
-                ms = min(api.render_batch(jobs, cfg)[1]["device_ms"] for _ in range(reps))
-                table.append(({"block_size": b, "ctas_per_sm": c, "refill_period": p}, ms))
+    for c in candidates():
+        cfg = config_of(c)
+        ms = min(api.render_batch(jobs, cfg)[1]["device_ms"] for _ in range(reps))
+        table.append((c, ms))
     best = min(table, key=lambda x: x[1])[0]
     if save:
         os.makedirs(os.path.dirname(PATH), exist_ok=True)
@@ -49,6 +62,4 @@ def load():
 
 
 def tuned_config(use_graph=True):
-    best = load() or {}
-    return api.batch_config(best.get("block_size", 0), best.get("ctas_per_sm", 0), best.get("refill_period", 0),
-                            use_graph)
+    return config_of(load() or {}, use_graph)

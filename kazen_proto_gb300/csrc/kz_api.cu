@@ -1298,18 +1298,133 @@ extern "C" kz_status kz_scene_release_scratch(kz_scene* s) {
     return KZ_OK;
 }
 
+namespace {
+
+// Wavefront mode of kz_render_batch: the device-driven loop of run_wavefront
+// over all jobs at once, on the first job's scene stream and scratch. One
+// batch of iterations (plan, generate, trace, shade, shadow, finish) is
+// enqueued, or replayed as a captured graph, between host synchronisations.
+kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_batch_config& cfg, int32_t mem,
+                          const kz::DevJob* djobs, const std::vector<float*>& fptr, const std::vector<uint64_t>& npix,
+                          uint64_t total, kz_batch_stats* out_stats) {
+    kz_scene* s = jobs[0].scene;
+    cudaStream_t strm = s->stream;
+    const uint64_t want = cfg.wavefront_size ? cfg.wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
+    const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(want, total), 1u << 30));
+    const uint32_t block = cfg.block_size;
+    uint32_t max_depth = 1;
+    for (uint32_t j = 0; j < n_jobs; ++j) max_depth = std::max(max_depth, jobs[j].max_depth);
+    kz::PathSoA A, B;
+    KZ_TRY(alloc_paths(s->pa, cap, A));
+    KZ_TRY(alloc_paths(s->pb, cap, B));
+    for (int k = 0; k < 3; ++k) KZ_TRY(s->sh[k].ensure((size_t)cap * sizeof(float4)));
+    kz::ShadowSoA sq{s->sh[0].as<float4>(), s->sh[1].as<float4>(), s->sh[2].as<float4>()};
+    KZ_TRY(s->ctr.ensure(sizeof(kz::DevCounters)));
+    kz::DevCounters* ctr = s->ctr.as<kz::DevCounters>();
+    for (uint32_t j = 0; j < n_jobs; ++j) KZ_CUDA(cudaMemsetAsync(fptr[j], 0, npix[j] * 12, strm));
+    {
+        kz::DevCounters init{};
+        init.total = total;
+        *s->ctr_host = init;
+        KZ_CUDA(cudaMemcpyAsync(ctr, s->ctr_host, sizeof(kz::DevCounters), cudaMemcpyHostToDevice, strm));
+    }
+    // an even number of iterations per batch, so the path buffers end where
+    // they started and a captured batch can be replayed as is
+    uint32_t iters = std::max<uint32_t>(4, max_depth + 1);
+    iters += iters & 1u;
+    auto enqueue = [&]() {
+        kz::PathSoA a = A, b = B;
+        for (uint32_t it = 0; it < iters; ++it) {
+            kz::launch_plan(ctr, cap, strm);
+            kz::launch_generate_batch_dev(djobs, n_jobs, a, ctr, cap, block, strm);
+            kz::launch_trace_paths_batch(djobs, a, cap, ctr, strm);
+            kz::launch_shade_batch(djobs, a, cap, b, sq, ctr, block, strm);
+            kz::launch_trace_shadow_batch(djobs, sq, cap, ctr, strm);
+            kz::launch_finish(ctr, strm);
+            std::swap(a, b);
+        }
+    };
+    kz::prepare_batch_wavefront();
+    cudaGraphExec_t exec = nullptr;
+    struct ExecGuard {
+        cudaGraphExec_t& e;
+        ~ExecGuard() {
+            if (e) cudaGraphExecDestroy(e);
+        }
+    } xg{exec};
+    if (cfg.use_graph) {
+        cudaGraph_t graph = nullptr;
+        KZ_CUDA(cudaStreamBeginCapture(strm, cudaStreamCaptureModeThreadLocal));
+        enqueue();
+        cudaError_t ce = cudaStreamEndCapture(strm, &graph);
+        if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KZ_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(KZ_ERR_CUDA, "cudaEventCreate failed");
+    }
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } evg{e0, e1};
+    KZ_CUDA(cudaEventRecord(e0, strm));
+    for (;;) {
+        if (exec) KZ_CUDA(cudaGraphLaunch(exec, strm));
+        else enqueue();
+        KZ_CUDA(cudaGetLastError());
+        KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
+        KZ_CUDA(cudaStreamSynchronize(strm));
+        const kz::DevCounters& hc = *s->ctr_host;
+        if (hc.status) return fail((kz_status)hc.status, "device status %u during batched rendering", hc.status);
+        if (hc.n_active == 0 && hc.next_path >= hc.total) break;
+    }
+    for (uint32_t j = 0; j < n_jobs; ++j)
+        kz::launch_scale(fptr[j], nullptr, npix[j] * 3, 1.0f / (float)jobs[j].spp, 0.0, strm);
+    KZ_CUDA(cudaEventRecord(e1, strm));
+    if (mem == KZ_MEM_HOST)
+        for (uint32_t j = 0; j < n_jobs; ++j)
+            KZ_CUDA(cudaMemcpyAsync(jobs[j].out_rgb, fptr[j], npix[j] * 12, cudaMemcpyDeviceToHost, strm));
+    KZ_CUDA(cudaStreamSynchronize(strm));
+    float ms = 0.f;
+    KZ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (out_stats) {
+        const kz::DevCounters& hc = *s->ctr_host;
+        out_stats->paths = total;
+        out_stats->path_bounces = hc.path_bounces;
+        out_stats->shadow_rays = hc.shadow_rays;
+        out_stats->threads = cap;
+        out_stats->device_ms = ms;
+    }
+    return KZ_OK;
+}
+
+}  // namespace
+
 extern "C" kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, const kz_batch_config* cfg_in,
                                      int32_t mem, kz_batch_stats* out_stats) {
     KZ_TRY(check_mem(mem));
     if (n_jobs == 0) return KZ_OK;
     if (!jobs) return fail(KZ_ERR_INVALID_ARG, "jobs is NULL");
     kz_batch_config cfg = cfg_in ? *cfg_in : kz_batch_config{};
-    if (cfg.block_size == 0) cfg.block_size = 128;
+    if (cfg.mode != KZ_BATCH_WAVEFRONT && cfg.mode != KZ_BATCH_MEGAKERNEL)
+        return fail(KZ_ERR_INVALID_ARG, "unknown batch mode %u", cfg.mode);
+    const bool wavefront = cfg.mode == KZ_BATCH_WAVEFRONT;
+    if (cfg.block_size == 0) cfg.block_size = wavefront ? 256 : 128;
     if (cfg.ctas_per_sm == 0) cfg.ctas_per_sm = 2;
     if (cfg.refill_period == 0) cfg.refill_period = 1;
     if (cfg.block_size % 32 != 0 || cfg.block_size > 256)
         return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32 and <= 256");
     if (cfg.ctas_per_sm > 64) return fail(KZ_ERR_INVALID_ARG, "ctas_per_sm must be <= 64");
+    if (wavefront && n_jobs > kz::kMaxBatchJobs)
+        return fail(KZ_ERR_INVALID_ARG, "at most %u jobs per wavefront batch", kz::kMaxBatchJobs);
     // lock every distinct scene once, in address order
     std::vector<kz_scene*> scenes;
     for (uint32_t j = 0; j < n_jobs; ++j) {
@@ -1368,6 +1483,7 @@ extern "C" kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, 
     KZ_TRY(djobs.ensure(n_jobs * sizeof(kz::DevJob)));
     KZ_TRY(ctrs.ensure(sizeof(kz::BatchCounters)));
     KZ_CUDA(cudaMemcpyAsync(djobs.ptr, dj.data(), n_jobs * sizeof(kz::DevJob), cudaMemcpyHostToDevice, st));
+    if (wavefront) return batch_wavefront(jobs, n_jobs, cfg, mem, djobs.as<kz::DevJob>(), fptr, npix, total, out_stats);
     int sms = 0;
     KZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s0->device));
     const uint32_t ctas = (uint32_t)sms * cfg.ctas_per_sm;

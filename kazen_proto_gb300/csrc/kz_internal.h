@@ -215,6 +215,16 @@ void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint3
 // Persistent batch renderer: grid = ctas blocks of `block` threads; each lane
 // keeps one path in registers and refills from the global counter every
 // `period` vertices (warp-aggregated fetch).
+// Batched wavefront stages over the job table (device-driven counters).
+void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst, DevCounters* ctr, uint32_t cap,
+                               uint32_t block, cudaStream_t st);
+void launch_trace_paths_batch(const DevJob* jobs, PathSoA p, uint32_t cap, DevCounters* ctr, cudaStream_t st);
+void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
+                        uint32_t block, cudaStream_t st);
+void launch_trace_shadow_batch(const DevJob* jobs, ShadowSoA sq, uint32_t cap, DevCounters* ctr, cudaStream_t st);
+// Queries the persistent stages' grid sizes (call before a stream capture).
+void prepare_batch_wavefront();
+constexpr uint32_t kMaxBatchJobs = 1u << 20;  // job index in 20 bits of a path's flags
 void launch_render_batch(const DevJob* jobs, uint32_t n_jobs, unsigned long long total, BatchCounters* bc,
                          uint32_t period, uint32_t ctas, uint32_t block, cudaStream_t st);
 void launch_guide_infer_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, const DevCounters* ctr,

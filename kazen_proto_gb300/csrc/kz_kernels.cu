@@ -19,6 +19,10 @@ namespace kz {
 namespace {
 
 constexpr uint32_t kSpecularFlag = 1u << 8;
+// Batched wavefront: bits 12-31 of a path's d4.w hold its job index (0 for a
+// single render); continuations keep them, shadow rays carry the job in c4.w.
+constexpr uint32_t kJobShift = 12;
+constexpr uint32_t kJobMask = 0xFFFFF000u;
 
 __device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
     if (status) atomicCAS(status, 0u, code);
@@ -204,8 +208,9 @@ __global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint
 
 // Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
 // ray up, store(k, hit) writes the result.
+// `s` is the lane's scene; load may repoint it per ray (batched jobs).
 template <bool kCount, typename Ctr, typename Load, typename Store>
-__device__ __forceinline__ void persistent_closest(const DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
+__device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
                                                    Store store, uint32_t& dn, uint32_t& dt) {
     uint2 stack[kWideStack];
     ClosestState c;
@@ -443,8 +448,8 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     out.shadow = true;
                     out.s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
                     out.s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
-                    const uint32_t tag =
-                        kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u)) : 0u;
+                    const uint32_t tag = kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u))
+                                                 : flags >> kJobShift;
                     out.s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
                     if (kGuided && gs.nee && guided) {
                         // training sample: the light direction with its
@@ -513,7 +518,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             if (alive) {
                 out.cont = true;
                 out.o_next = make_float4(P.x, P.y, P.z, pdf);
-                out.d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float(depth + 1));
+                out.d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float((depth + 1) | (flags & kJobMask)));
                 out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
                 out.rng_next = rng.state;
             }
@@ -572,8 +577,9 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                 const f3 dn = normalize(fr.to_world(smp.wo));
                 out.cont = true;
                 out.o_next = make_float4(P.x, P.y, P.z, pdf_dir);
-                out.d_next = make_float4(dn.x, dn.y, dn.z,
-                                     __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u)));
+                out.d_next = make_float4(
+                    dn.x, dn.y, dn.z,
+                    __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u) | (flags & kJobMask)));
                 out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
                 out.rng_next = rng.state;
             }
@@ -811,6 +817,105 @@ __global__ void __launch_bounds__(256) k_render_batch(const DevJob* __restrict__
     }
 }
 
+// ------------------------------------------------------------------ batched wavefront
+// Many jobs in one wavefront: paths of all jobs share the path buffers and
+// the stage kernels; each path finds its scene, camera, parameters and film
+// through its job index (d4.w bits 12-31, c4.w for shadow rays). Global path
+// ids [0, total) are generated in job order; a path's own id is local to its
+// job, so every job renders exactly what kz_render renders for it.
+
+__global__ void k_generate_batch_dev(const DevJob* __restrict__ jobs, uint32_t n_jobs, PathSoA dst,
+                                     const DevCounters* c) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= c->gen_count) return;
+    const unsigned long long g = c->gen_first + j;
+    const uint32_t job = find_job(jobs, n_jobs, g);
+    const DevJob& J = jobs[job];
+    const uint32_t k = c->gen_slot + j;
+    generate_camera_path(J.cam, J.pp, dst, k, g - J.path_begin);
+    dst.d4[k].w = __uint_as_float(__float_as_uint(dst.d4[k].w) | (job << kJobShift));
+}
+
+// The traversal reads only these fields of a scene.
+__device__ __forceinline__ void trace_fields(DevScene& dst, const DevScene& src) {
+    dst.nodes = src.nodes;
+    dst.tris = src.tris;
+    dst.n_nodes = src.n_nodes;
+    dst.n_tris = src.n_tris;
+}
+
+__global__ void __launch_bounds__(256) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
+                                                           DevCounters* ctr) {
+    uint32_t dn = 0, dt = 0;
+    DevScene ls;
+    persistent_closest<false>(
+        ls, ctr->n_active, &ctr->trace_next, &ctr->status,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = p.o4[k], d = p.d4[k];
+            trace_fields(ls, jobs[__float_as_uint(d.w) >> kJobShift].scene);
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = __int_as_float(0x7f800000);
+        },
+        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
+}
+
+__global__ void __launch_bounds__(256) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
+                                                     ShadowSoA sq, DevCounters* ctr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n_in = ctr->n_active;
+    ShadeOut so;
+    if (i < n_in) {
+        const float4 d4 = in.d4[i];
+        const DevJob& J = jobs[__float_as_uint(d4.w) >> kJobShift];
+        shade_vertex<false>(J.scene, J.pp, in.hit[i], in.o4[i], d4, in.b4[i], in.rng[i], GuideShade{}, nullptr, so);
+        if (!is_zero(so.Lsum)) film_add(J.film, nullptr, so.film_idx, so.Lsum);
+    }
+    const bool cont = so.cont, shadow = so.shadow;
+    const uint32_t slot = warp_append(cont, &ctr->n_next);
+    if (cont) {
+        out.o4[slot] = so.o_next;
+        out.d4[slot] = so.d_next;
+        out.b4[slot] = so.b_next;
+        out.rng[slot] = so.rng_next;
+    }
+    const uint32_t sslot = warp_append(shadow, &ctr->n_shadow);
+    if (shadow) {
+        sq.o4[sslot] = so.s_o;
+        sq.d4[sslot] = so.s_d;
+        sq.c4[sslot] = so.s_c;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
+                                                            DevCounters* ctr) {
+    uint32_t dn = 0, dt = 0;
+    uint2 stack[kWideStack];
+    AnyState c;
+    TRay r;
+    DevScene ls;
+    float tmax = 0.f;
+    uint32_t octp = 0, ray = 0, job = 0;
+    persistent_rays(
+        ctr->n_shadow, &ctr->shadow_next, kTraceRefill,
+        [&](uint32_t k) {
+            ray = k;
+            const float4 o = sq.o4[k], d = sq.d4[k];
+            job = __float_as_uint(sq.c4[k].w);
+            trace_fields(ls, jobs[job].scene);
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = o.w;
+            octp = wide_octant(r);
+            any_begin(c);
+        },
+        [&]() {
+            const int rc = any_step<false>(ls, r, octp, tmax, c, stack, dn, dt);
+            if (rc == 0) return false;
+            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
+            if (rc == 1) film_add(jobs[job].film, nullptr, __float_as_uint(sq.d4[ray].w), xyz(sq.c4[ray]));
+            return true;
+        });
+}
+
 // ------------------------------------------------------------------ device-driven loop
 __global__ void k_plan(DevCounters* c, uint32_t cap) {
     const uint64_t remaining = c->total - c->next_path;
@@ -1001,6 +1106,36 @@ void launch_render_batch(const DevJob* jobs, uint32_t n_jobs, unsigned long long
                          uint32_t period, uint32_t ctas, uint32_t block, cudaStream_t st) {
     if (!n_jobs || !total) return;
     k_render_batch<<<ctas, block, 0, st>>>(jobs, n_jobs, total, bc, period ? period : 1u);
+}
+void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst, DevCounters* ctr, uint32_t cap,
+                               uint32_t block, cudaStream_t st) {
+    if (!cap) return;
+    k_generate_batch_dev<<<grid_for(cap, block), block, 0, st>>>(jobs, n_jobs, dst, ctr);
+}
+static unsigned grid_trace_batch() {
+    static const unsigned g = resident_grid(k_trace_paths_batch, 256);
+    return g;
+}
+static unsigned grid_shadow_batch() {
+    static const unsigned g = resident_grid(k_trace_shadow_batch, 256);
+    return g;
+}
+void prepare_batch_wavefront() {
+    (void)grid_trace_batch();
+    (void)grid_shadow_batch();
+}
+void launch_trace_paths_batch(const DevJob* jobs, PathSoA p, uint32_t cap, DevCounters* ctr, cudaStream_t st) {
+    if (!cap) return;
+    k_trace_paths_batch<<<std::min(grid_trace_batch(), grid_for(cap, 256)), 256, 0, st>>>(jobs, p, ctr);
+}
+void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
+                        uint32_t block, cudaStream_t st) {
+    if (!cap) return;
+    k_shade_batch<<<grid_for(cap, block), block, 0, st>>>(jobs, in, out, sq, ctr);
+}
+void launch_trace_shadow_batch(const DevJob* jobs, ShadowSoA sq, uint32_t cap, DevCounters* ctr, cudaStream_t st) {
+    if (!cap) return;
+    k_trace_shadow_batch<<<std::min(grid_shadow_batch(), grid_for(cap, 256)), 256, 0, st>>>(jobs, sq, ctr);
 }
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
     if (!n) return;

@@ -1,5 +1,6 @@
-"""Batched rendering: many uneven jobs in one persistent launch (optionally a
-CUDA graph) must give each job the same film as rendering it alone."""
+"""Batched rendering: many uneven jobs in one wavefront (or one persistent
+megakernel launch), optionally through CUDA graphs, must give each job the
+same film as rendering it alone."""
 import numpy as np
 import pytest
 
@@ -27,9 +28,16 @@ def singles(jobs):
     return out
 
 
-@pytest.mark.parametrize("cfg", [dict(block_size=128, ctas_per_sm=2, refill_period=1, use_graph=True),
-                                 dict(block_size=64, ctas_per_sm=1, refill_period=4, use_graph=False),
-                                 dict(block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True)])
+MEGA = api.BATCH_MEGAKERNEL
+WAVE = api.BATCH_WAVEFRONT
+
+
+@pytest.mark.parametrize("cfg", [dict(mode=WAVE, use_graph=True),
+                                 dict(mode=WAVE, block_size=128, wavefront_size=4096, use_graph=False),
+                                 dict(mode=WAVE, block_size=64, wavefront_size=1000, use_graph=True),
+                                 dict(mode=MEGA, block_size=128, ctas_per_sm=2, refill_period=1, use_graph=True),
+                                 dict(mode=MEGA, block_size=64, ctas_per_sm=1, refill_period=4, use_graph=False),
+                                 dict(mode=MEGA, block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True)])
 def test_batch_matches_single_renders(gpu, jobs, cfg):
     imgs, st = api.render_batch(jobs, api.batch_config(**cfg))
     ref = singles(jobs)
@@ -44,7 +52,12 @@ def test_batch_matches_single_renders(gpu, jobs, cfg):
 def test_autotuner_picks_a_candidate(gpu, jobs, tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "PATH", str(tmp_path / "autotune.json"))
     best, table = autotune.tune(jobs, reps=1)
-    assert len(table) == len(autotune.BLOCKS) * len(autotune.CTAS_PER_SM) * len(autotune.PERIODS)
+    assert len(table) == len(autotune.candidates())
     assert best in [c for c, _ in table] and autotune.load() == best
     imgs, _ = api.render_batch(jobs, autotune.tuned_config())
     assert all(np.isfinite(i).all() for i in imgs)
+
+
+def test_batch_rejects_unknown_mode(gpu, jobs):
+    with pytest.raises(api.N.KazenError):
+        api.render_batch(jobs[:1], api.batch_config(mode=7))

@@ -45,10 +45,11 @@ def test_struct_layouts_match_header():
     assert C.sizeof(N.KzLobe) == 64
     assert C.sizeof(N.KzMaterial) == 16 + 8 * 64
     assert N.RAY_DTYPE.itemsize == 32
+    assert C.sizeof(N.KzBatchConfig) == 24
 
 
 def test_abi_version_and_device_query(native_lib):
-    assert native_lib.kz_abi_version() == 1
+    assert native_lib.kz_abi_version() == 2
     assert native_lib.kz_device_count() >= 0
 
 
