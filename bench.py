@@ -269,7 +269,7 @@ def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
     g = api.Guide(seed=3)
     t0 = time.perf_counter()
     img_g, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=1 << 20, max_depth=max_depth, seed=7,
-                                          gcfg=api.guide_config(spp_per_pass=4, learning_rate=1e-2,
+                                          gcfg=api.guide_config(spp_per_pass=16, steps_per_pass=4, learning_rate=1e-2,
                                                                 max_train_steps=256, time_budget_ms=T * 1e3))
     Tg = time.perf_counter() - t0
     e_guided = rel_mse(img_g, ref)

@@ -435,9 +435,9 @@ def guide_config(alpha=0.5, learning_rate=1e-2, spp_per_pass=1, train=True, max_
 
 
 def render_guided(scene: Scene, guide: Guide, camera: Camera, width: int, height: int, spp: int, max_depth: int,
-                  seed=0, gcfg=None, fp64=False, wavefront_size=0):
+                  seed=0, gcfg=None, fp64=False, wavefront_size=0, flags=0):
     """Guided render; returns (image, fp64 image or None, render stats, guide stats)."""
-    cfg = render_config(spp, max_depth, seed, wavefront_size)
+    cfg = render_config(spp, max_depth, seed, wavefront_size, flags=flags)
     gcfg = gcfg or guide_config()
     film = N.KzFilmDesc(width, height)
     cam = camera.to_c()

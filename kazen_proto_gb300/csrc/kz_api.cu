@@ -1215,6 +1215,10 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
         st.shadow_rays += pst.shadow_rays;
         st.iterations += pst.iterations;
         st.kernel_launches += pst.kernel_launches;
+        st.generate_ms += pst.generate_ms;
+        st.trace_ms += pst.trace_ms;
+        st.shade_ms += pst.shade_ms;
+        st.shadow_ms += pst.shadow_ms;
         st.paths += total;
         spp_done += spp_pass;
         pass += 1;

@@ -56,7 +56,8 @@ __device__ __forceinline__ float guide_feature(int j, f3 p01, f3 n, float band_s
 struct VmfMixture {
     f3 mu[kGuideLobes];
     float kappa[kGuideLobes];
-    float w[kGuideLobes];  // lobe probabilities (softmax)
+    float w[kGuideLobes];   // lobe probabilities (softmax)
+    float lc[kGuideLobes];  // shading form: log(w) + log norm(kappa) - kappa
 };
 
 __device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
@@ -85,6 +86,43 @@ __device__ __forceinline__ float mixture_pdf(const VmfMixture& m, f3 w) {
     float p = 0.f;
     for (int k = 0; k < kGuideLobes; ++k)
         p += m.w[k] * expf(vmf_log_norm(m.kappa[k]) + m.kappa[k] * (dot(m.mu[k], w) - 1.f));
+    return p;
+}
+
+// Shading form of the mixture: the same lobes with each lobe's weight and
+// normalisation folded into one log factor, so a pdf evaluation is one
+// exponential per lobe; uses the fast hardware exp/log (relative error near
+// 2^-21, far below the network's own BF16 error). Sampling and the pdf both
+// use this form, so the estimator's weights match the sampled density.
+__device__ __forceinline__ void mixture_for_shading(const float* r, VmfMixture& m) {
+    float mx = -1e30f;
+    for (int k = 0; k < kGuideLobes; ++k) mx = fmaxf(mx, r[5 * k + 4]);
+    float s = 0.f;
+    for (int k = 0; k < kGuideLobes; ++k) {
+        const float* q = r + 5 * k;
+        const float l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const float il = l2 > 1e-24f ? rsqrtf(l2) : 0.f;
+        m.mu[k] = il > 0.f ? mk(q[0] * il, q[1] * il, q[2] * il) : mk(0.f, 0.f, 1.f);
+        const float z = q[3];
+        const float sp = z > 20.f ? z : __logf(1.f + __expf(z));
+        m.kappa[k] = fminf(kKappaMin + sp, kKappaMax);
+        m.w[k] = __expf(q[4] - mx);
+        s += m.w[k];
+    }
+    const float is = 1.f / s;
+    for (int k = 0; k < kGuideLobes; ++k) {
+        m.w[k] *= is;
+        const float kap = m.kappa[k];
+        // log(kappa / (2 pi (1 - exp(-2 kappa))))
+        const float ln = __logf(kap) - 1.8378770664093453f - __logf(1.f - __expf(-2.f * kap));
+        m.lc[k] = __logf(fmaxf(m.w[k], 1e-30f)) + ln - kap;
+    }
+}
+
+__device__ __forceinline__ float mixture_pdf_shading(const VmfMixture& m, f3 w) {
+    float p = 0.f;
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; ++k) p += __expf(m.lc[k] + m.kappa[k] * dot(m.mu[k], w));
     return p;
 }
 

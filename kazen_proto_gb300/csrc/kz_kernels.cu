@@ -408,7 +408,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
         const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
         VmfMixture mix;
-        if (kGuided && guided) mixture_from_raw(raw, mix);
+        if (kGuided && guided) mixture_for_shading(raw, mix);
         const float alpha = gs.alpha;
 
         // 2. next-event estimation
@@ -441,7 +441,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     f = f + hmul(ld3(lb.weight), e.f);
                     bpdf += lp[k] * e.pdf;
                 }
-                if (kGuided && guided) bpdf = alpha * mixture_pdf(mix, ldir) + (1.f - alpha) * bpdf;
+                if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
                 if (!is_zero(f)) {
                     const float w = power_heuristic(lpdf, bpdf);
                     const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
@@ -508,7 +508,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     f = f + hmul(ld3(lb.weight), e.f);
                     pdf += lp[k] * e.pdf;
                 }
-                pdf = alpha * mixture_pdf(mix, wdir) + (1.f - alpha) * pdf;
+                pdf = alpha * mixture_pdf_shading(mix, wdir) + (1.f - alpha) * pdf;
             }
             alive = ok && pdf > 0.f && !is_zero(f);
             if (alive) {

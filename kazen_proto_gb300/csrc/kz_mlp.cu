@@ -78,17 +78,39 @@ __device__ __forceinline__ void to_afrag(const float (&c)[NT][4], uint32_t (&a)[
     }
 }
 
+// sin and cos of 2^b * pi * bs * x. The argument is reduced exactly,
+// t - 2 rint(t / 2) in [-1, 1], before the fast hardware sine and cosine,
+// whose absolute error on [-pi, pi] (~2^-21) is far below the BF16 rounding
+// the features then get.
+__device__ __forceinline__ void band_sincos(float x, int b, float bs, float& sn, float& cs) {
+    const float t = x * (float)(1 << b) * bs;
+    const float r = t - 2.f * rintf(0.5f * t);
+    __sincosf(kPi * r, &sn, &cs);
+}
+
 // Input features of rows g and g+8 straight into A fragments (4 k-tiles).
+// Lane t holds columns 16 kt + 2t (+1) and 16 kt + 2t + 8 (+9): for the
+// position axes kt = 0..2, the sin/cos pairs of bands t and t + 4 (the
+// layout of guide_feature); k-tile 3 holds the normal and zero padding.
 __device__ __forceinline__ void feature_afrag(uint32_t (&a)[4][4], f3 p0, f3 n0, f3 p1, f3 n1, float bs, int lane) {
     const int t = lane & 3;
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        const int c = 16 * kt + 2 * t;
-        a[kt][0] = pack2(guide_feature(c, p0, n0, bs), guide_feature(c + 1, p0, n0, bs));
-        a[kt][1] = pack2(guide_feature(c, p1, n1, bs), guide_feature(c + 1, p1, n1, bs));
-        a[kt][2] = pack2(guide_feature(c + 8, p0, n0, bs), guide_feature(c + 9, p0, n0, bs));
-        a[kt][3] = pack2(guide_feature(c + 8, p1, n1, bs), guide_feature(c + 9, p1, n1, bs));
+    for (int kt = 0; kt < 3; ++kt) {
+        float s0, c0, s1, c1, s2, c2, s3, c3;
+        band_sincos(comp(p0, kt), t, bs, s0, c0);
+        band_sincos(comp(p1, kt), t, bs, s1, c1);
+        band_sincos(comp(p0, kt), t + 4, bs, s2, c2);
+        band_sincos(comp(p1, kt), t + 4, bs, s3, c3);
+        a[kt][0] = pack2(s0, c0);
+        a[kt][1] = pack2(s1, c1);
+        a[kt][2] = pack2(s2, c2);
+        a[kt][3] = pack2(s3, c3);
     }
+    const int c = 48 + 2 * t;
+    a[3][0] = pack2(guide_feature(c, p0, n0, bs), guide_feature(c + 1, p0, n0, bs));
+    a[3][1] = pack2(guide_feature(c, p1, n1, bs), guide_feature(c + 1, p1, n1, bs));
+    a[3][2] = 0u;  // columns 56..63: padding
+    a[3][3] = 0u;
 }
 
 // Stage the BF16 weights into shared memory: W1..W3 [64][72], W4 [40][72]
@@ -126,6 +148,7 @@ __device__ void stage_weights(const __nv_bfloat16* __restrict__ Wg, __nv_bfloat1
 }
 
 constexpr size_t kSmemInfer = (size_t)(64 * 3 + 40) * kStrideW * 2;
+constexpr uint32_t kInferCtasPerSm = 6;  // 33 KB of weights each: six fit in shared memory
 constexpr size_t kSmemTrainW = kSmemInfer + (size_t)(64 * 2) * kStrideW * 2 + (size_t)64 * kStrideW4T * 2;
 constexpr int kTrainWarps = 4;
 constexpr size_t kSmemTrain = kSmemTrainW + (size_t)kTrainWarps * 16 * 41 * 4;
@@ -470,7 +493,7 @@ void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const Gu
                               cudaStream_t st) {
     if (!n) return;
     const uint32_t tiles = (n + 15) / 16;
-    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
+    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * kInferCtasPerSm);
     k_guide_infer<true><<<grid, 128, kSmemInfer, st>>>(s, p, nullptr, n, gd, raw, nullptr);
 }
 
@@ -478,7 +501,7 @@ void launch_guide_infer_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, co
                                   const GuideDev& gd, float* raw, cudaStream_t st) {
     if (!cap) return;
     const uint32_t tiles = (cap + 15) / 16;
-    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
+    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * kInferCtasPerSm);
     k_guide_infer<true><<<grid, 128, kSmemInfer, st>>>(s, p, nullptr, cap, gd, raw, &ctr->n_active);
 }
 
@@ -487,7 +510,7 @@ void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd
     DevScene none;
     PathSoA np{};
     const uint32_t tiles = (n + 15) / 16;
-    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * 4);
+    const uint32_t grid = min((tiles + 3) / 4, (uint32_t)sm_count() * kInferCtasPerSm);
     k_guide_infer<false><<<grid, 128, kSmemInfer, st>>>(none, np, pts, n, gd, raw, nullptr);
 }
 
