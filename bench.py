@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--no-traversal", action="store_true")
     p.add_argument("--no-guiding", action="store_true")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--profile-guide", action="store_true",
+                   help="one small guided render with training (slit room 128x128, 32 spp), for ncu captures "
+                        "of the guiding network kernels; prints its stats and exits")
     return p.parse_args()
 
 
@@ -339,15 +342,34 @@ def batch_bench(n_jobs=256):
             "max_rel_film_difference": max(errs)}
 
 
+TRACE_KERNEL = "k_trace_paths_persistent"
+
+
 def load_traffic():
-    """DRAM bytes per ray of k_trace_paths from the committed ncu summary."""
+    """DRAM bytes per ray of the closest-hit kernel from the committed ncu summary."""
     import re
-    path = os.path.join(ROOT, "profiles", "k_trace_paths_terrain_profile.md")
+    path = os.path.join(ROOT, "profiles", "k_trace_paths_persistent_terrain_profile.md")
     if os.path.exists(path):
         m = re.search(r"^dram_bytes_per_ray:\s*([0-9.]+)", open(path).read(), re.M)
         if m:
-            return {"kernel": "k_trace_paths", "dram_bytes_per_ray": float(m.group(1))}
+            return {"kernel": TRACE_KERNEL, "dram_bytes_per_ray": float(m.group(1))}
     return None
+
+
+def profile_guide():
+    """Small guided render with online training: the command the guiding
+    network's ncu captures run."""
+    from kazen_proto_gb300 import api, build as kbuild, scenes
+    kbuild.build()
+    R, D = 128, 10
+    d = scenes.slit_room_scene(R, R, max_depth=D)
+    s = d.build()
+    g = api.Guide(seed=3)
+    _, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=32, max_depth=D, seed=7,
+                                      gcfg=api.guide_config(spp_per_pass=16, steps_per_pass=4, learning_rate=1e-2))
+    print(json.dumps({"workload": "slit_room_128x128_32spp_guided_training", "render": st, "guide": gst}))
+    g.close()
+    s.close()
 
 
 # ---------------------------------------------------------------- our arm
@@ -452,7 +474,7 @@ def run_ours(args):
     rays_launch = rays_frame / iters_frame
     tr = load_traffic()
     traffic = None
-    if tr and tr.get("kernel") == "k_trace_paths" and tr.get("dram_bytes_per_ray"):
+    if tr and tr.get("kernel") == TRACE_KERNEL and tr.get("dram_bytes_per_ray"):
         traffic = round(tr["dram_bytes_per_ray"] * rays_launch)
     value = units / secs / 1e6
     frame_ms = total_ms / args.steps
@@ -464,7 +486,7 @@ def run_ours(args):
         "e2e": {"value": round(e_units / e_secs / 1e6, 3), "unit": UNIT,
                 "h2d_bytes_per_step": 64 + 40, "d2h_bytes_per_step": W * H * 12,
                 "note": "kz_render with a host film buffer: camera+config in, W*H*3 float out per frame"},
-        "roofline": {"bound": "hbm", "kernel": "k_trace_paths", "achieved": round(achieved, 1), "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": TRACE_KERNEL, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "alg_bytes_per_launch": round(alg_bytes_ray * rays_launch),
                      "launch_ms": round(trace_ms_frame / iters_frame, 4),
@@ -527,7 +549,9 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.profile_guide:
+        profile_guide()
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_ours(a)
