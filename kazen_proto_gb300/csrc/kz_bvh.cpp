@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <stdexcept>
 #include <utility>
 
@@ -83,13 +84,11 @@ struct Builder {
                 cb.grow(&cen[(size_t)idx[i] * 3]);
             }
             nodes[tk.node].box = bb;
+            nodes[tk.node].first = tk.first;  // inner nodes keep their range too
+            nodes[tk.node].count = tk.count;
             uint32_t mid = 0;
             bool split = tk.count > 1 && (int)tk.depth < kMaxBvhDepth - 1 && choose_split(tk.first, tk.count, bb, cb, mid);
-            if (!split) {
-                nodes[tk.node].first = tk.first;
-                nodes[tk.node].count = tk.count;
-                continue;
-            }
+            if (!split) continue;
             int32_t l = (int32_t)nodes.size();
             nodes.emplace_back();
             int32_t r = (int32_t)nodes.size();
@@ -254,6 +253,132 @@ struct Collapser {
     }
 };
 
+// Leaves the depth cap left larger than kWideLeafMax become inner nodes,
+// halved by count along the widest centroid axis until every leaf fits a
+// wide slot. Children are appended after their parent, as in the build.
+void split_big_leaves(Builder& b) {
+    for (size_t id = 0; id < b.nodes.size(); ++id) {
+        if (b.nodes[id].left >= 0 || b.nodes[id].count <= kWideLeafMax) continue;
+        const uint32_t first = b.nodes[id].first, count = b.nodes[id].count;
+        Box cb;
+        for (uint32_t i = first; i < first + count; ++i) cb.grow(&b.cen[(size_t)b.idx[i] * 3]);
+        int a = 0;
+        for (int k = 1; k < 3; ++k)
+            if (cb.hi[k] - cb.lo[k] > cb.hi[a] - cb.lo[a]) a = k;
+        const uint32_t mid = first + count / 2;
+        std::nth_element(b.idx.begin() + first, b.idx.begin() + mid, b.idx.begin() + first + count,
+                         [&](uint32_t p, uint32_t q) {
+                             float cp = b.cen[(size_t)p * 3 + a], cq = b.cen[(size_t)q * 3 + a];
+                             return cp < cq || (cp == cq && p < q);
+                         });
+        const uint32_t rng[2][2] = {{first, mid - first}, {mid, first + count - mid}};
+        int32_t kids[2];
+        for (int c = 0; c < 2; ++c) {
+            BNode n;
+            n.first = rng[c][0];
+            n.count = rng[c][1];
+            for (uint32_t i = n.first; i < n.first + n.count; ++i) n.box.grow(b.tb[b.idx[i]]);
+            kids[c] = (int32_t)b.nodes.size();
+            b.nodes.push_back(n);
+        }
+        b.nodes[id].left = kids[0];
+        b.nodes[id].right = kids[1];
+    }
+}
+
+// SAH-optimal assignment of binary subtrees to the 8 slots of wide nodes
+// (H. Ylitie, T. Karras, S. Laine, HPG 2017, section 4.1): cost(n, i) is the
+// least SAH cost of covering subtree n with at most i slots, each a leaf of
+// <= 3 triangles or a wide node; a wide node costs node_cost * area plus the
+// best 8-slot distribution of its two children, a leaf tri_cost * area *
+// triangles. Filled bottom-up (children follow parents in the node array).
+struct SahCollapse {
+    const Builder& b;
+    float node_cost, tri_cost;
+    std::vector<float> cost;        // [node][i - 1], i = 1..8
+    std::vector<uint8_t> split;     // [node][i - 1]: k slots to the left child of the best distribution of i
+    std::vector<uint8_t> from_prev; // [node][i - 1]: cost(n, i) == cost(n, i - 1)
+    std::vector<uint8_t> as_leaf;   // cost(n, 1) is the leaf's
+
+    SahCollapse(const Builder& bb, float cn, float ct) : b(bb), node_cost(cn), tri_cost(ct) {
+        const size_t n = b.nodes.size();
+        cost.assign(n * 8, 0.f);
+        split.assign(n * 8, 0);
+        from_prev.assign(n * 8, 0);
+        as_leaf.assign(n, 0);
+        const float inf = std::numeric_limits<float>::infinity();
+        for (size_t id = n; id-- > 0;) {
+            const BNode& nd = b.nodes[id];
+            const float A = nd.box.area();
+            const float leaf = nd.count <= kWideLeafMax ? tri_cost * A * (float)nd.count : inf;
+            float* c = &cost[id * 8];
+            if (nd.left < 0) {
+                for (int i = 0; i < 8; ++i) c[i] = leaf;
+                as_leaf[id] = 1;
+                continue;
+            }
+            const float* cl = &cost[(size_t)nd.left * 8];
+            const float* cr = &cost[(size_t)nd.right * 8];
+            float dist[9];
+            for (int j = 2; j <= 8; ++j) {
+                dist[j] = inf;
+                for (int k = 1; k < j; ++k) {
+                    const float v = cl[k - 1] + cr[j - k - 1];
+                    if (v < dist[j]) {
+                        dist[j] = v;
+                        split[id * 8 + j - 1] = (uint8_t)k;
+                    }
+                }
+            }
+            const float inner = dist[8] + node_cost * A;
+            as_leaf[id] = leaf <= inner ? 1 : 0;
+            c[0] = std::min(leaf, inner);
+            for (int i = 2; i <= 8; ++i) {
+                if (c[i - 2] <= dist[i]) {
+                    c[i - 1] = c[i - 2];
+                    from_prev[id * 8 + i - 1] = 1;
+                } else {
+                    c[i - 1] = dist[i];
+                }
+            }
+        }
+    }
+
+    WItem slot_of(int32_t id) const {
+        const BNode& nd = b.nodes[(size_t)id];
+        WItem w;
+        w.box = nd.box;
+        if (as_leaf[(size_t)id]) {
+            w.first = nd.first;
+            w.count = nd.count;
+        } else {
+            w.bnode = id;
+        }
+        return w;
+    }
+    // Slots covering subtree id with at most i of them.
+    void gather(int32_t id, int i, WItem* out, int& n) const {
+        const BNode& nd = b.nodes[(size_t)id];
+        while (i > 1 && from_prev[(size_t)id * 8 + i - 1]) --i;
+        if (i == 1 || nd.left < 0) {
+            out[n++] = slot_of(id);
+            return;
+        }
+        const int k = split[(size_t)id * 8 + i - 1];
+        gather(nd.left, k, out, n);
+        gather(nd.right, i - k, out, n);
+    }
+    // The slots of the wide node made from inner build node id.
+    int children(int32_t id, WItem* out) const {
+        const BNode& nd = b.nodes[(size_t)id];
+        const int k = split[(size_t)id * 8 + 7];
+        int n = 0;
+        gather(nd.left, k, out, n);
+        gather(nd.right, 8 - k, out, n);
+        return n;
+    }
+};
+
 // Smallest power-of-two quantum q with 255 * q >= ext (>= 2^-100).
 int quantum_exponent(double ext) {
     int e = -100;
@@ -268,10 +393,13 @@ int quantum_exponent(double ext) {
 
 }  // namespace
 
-void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out) {
-    Builder b(in, (int)kWideLeafMax);
+void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out, const WideBuildOptions& opt) {
+    Builder b(in, opt.sah_collapse ? std::max(1, std::min(opt.binary_max_leaf, (int)kWideLeafMax)) : (int)kWideLeafMax);
     b.run();
+    split_big_leaves(b);
     Collapser col(b);
+    std::unique_ptr<SahCollapse> sah;
+    if (opt.sah_collapse && !b.nodes.empty()) sah.reset(new SahCollapse(b, opt.node_cost, opt.tri_cost));
     out.nodes.assign(kWideWords, 0u);
     out.tris.clear();
     out.order.clear();
@@ -280,7 +408,7 @@ void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out) {
     out.depth = 1;
 
     WItem root;
-    if (!b.nodes.empty()) root = col.item_of(0);
+    if (!b.nodes.empty()) root = sah ? sah->slot_of(0) : col.item_of(0);
     struct Pending {
         WItem item;
         uint32_t node, depth;
@@ -289,11 +417,12 @@ void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out) {
     for (size_t head = 0; head < queue.size(); ++head) {
         const Pending pd = queue[head];
         out.depth = std::max(out.depth, pd.depth);
-        // greedy collapse: open the largest expandable child until 8 slots
         WItem ch[8];
         int nch = 0;
-        ch[nch++] = pd.item;
-        while (nch < 8) {
+        if (sah && pd.item.bnode >= 0) nch = sah->children(pd.item.bnode, ch);
+        else ch[nch++] = pd.item;
+        // greedy collapse: open the largest expandable child until 8 slots
+        while (!sah && nch < 8) {
             int best = -1;
             float best_area = -1.f;
             for (int k = 0; k < nch; ++k)

@@ -55,6 +55,16 @@ struct WideBvhOutput {
     uint32_t depth = 0;            // wide levels
 };
 
-void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out);
+// Collapse of the binary build into wide nodes: SAH-optimal slot assignment
+// (default) or greedy (open the largest-area child until 8 slots). Costs are
+// relative SAH weights of a wide-node visit and of one triangle test.
+struct WideBuildOptions {
+    bool sah_collapse = true;
+    float node_cost = 1.0f;
+    float tri_cost = 0.3f;
+    int binary_max_leaf = 1;  // leaf size of the binary build the SAH collapse regroups (<= 3)
+};
+
+void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out, const WideBuildOptions& opt = WideBuildOptions{});
 
 }  // namespace kz
