@@ -261,8 +261,10 @@ kz_status kz_render(kz_scene* scene, const kz_camera* camera,
  * online on the radiance samples the tracer produces maps a shading point
  * (position in the scene box, 8-band sin/cos encoding, plus the geometric
  * normal: 51 inputs) through 3 hidden layers of 64 ReLU units to an 8-lobe
- * von Mises-Fisher mixture over incident directions (mean 3, concentration
- * 1, weight 1 per lobe: 40 outputs). BF16 weights, FP32 accumulation, Adam.
+ * von Mises-Fisher mixture over incident directions (anchor 3, concentration
+ * 1, weight 1 per lobe: 40 outputs; a lobe's mean direction points from the
+ * shading point to its anchor, both in scene-box coordinates, measured in
+ * world units). BF16 weights, FP32 accumulation, Adam.
  * The renderer samples it with probability alpha and the BSDF otherwise and
  * weighs with the one-sample MIS pdf, so every image is unbiased whatever
  * the network has learned. */

@@ -7,7 +7,8 @@
 //
 // Network: 51 inputs (position in the scene box, 3 axes x 8 frequency bands x
 // {sin, cos} = 48, plus the geometric normal) -> 64 -> 64 -> 64 (ReLU) -> 40
-// raw outputs = 8 lobes x (mean direction 3, concentration 1, weight 1).
+// raw outputs = 8 lobes x (anchor point 3, concentration 1, weight 1); a
+// lobe's mean direction points from the shading point to its anchor.
 // vMF density (S. Jakob, "Numerically stable sampling of the von
 // Mises-Fisher distribution on S^2", 2012):
 //   v(w) = kappa / (2 pi (1 - exp(-2 kappa))) * exp(kappa (mu.w - 1)).
@@ -62,14 +63,24 @@ struct VmfMixture {
 
 __device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
 
-__device__ __forceinline__ void mixture_from_raw(const float* r, VmfMixture& m) {
+// Lobe axis: from the shading point p01 to the lobe's anchor (raw outputs
+// 0..2, both in scene-box coordinates), in world units (ext = box extent).
+// A light seen through an aperture, or a bright patch, is then one fixed
+// anchor for every shading point instead of a direction that turns with the
+// position; a far anchor still acts as a fixed direction.
+__device__ __forceinline__ f3 lobe_axis(const float* q, f3 p01, f3 ext) {
+    return hmul(mk(q[0], q[1], q[2]) - p01, ext);
+}
+
+__device__ __forceinline__ void mixture_from_raw(const float* r, f3 p01, f3 ext, VmfMixture& m) {
     float mx = -1e30f;
     for (int k = 0; k < kGuideLobes; ++k) mx = fmaxf(mx, r[5 * k + 4]);
     float s = 0.f;
     for (int k = 0; k < kGuideLobes; ++k) {
         const float* q = r + 5 * k;
-        float l = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
-        m.mu[k] = l > 1e-12f ? mk(q[0] / l, q[1] / l, q[2] / l) : mk(0.f, 0.f, 1.f);
+        const f3 a = lobe_axis(q, p01, ext);
+        const float l = sqrtf(dot(a, a));
+        m.mu[k] = l > 1e-12f ? mk(a.x / l, a.y / l, a.z / l) : mk(0.f, 0.f, 1.f);
         m.kappa[k] = fminf(kKappaMin + softplus(q[3]), kKappaMax);
         m.w[k] = expf(q[4] - mx);
         s += m.w[k];
@@ -94,15 +105,16 @@ __device__ __forceinline__ float mixture_pdf(const VmfMixture& m, f3 w) {
 // exponential per lobe; uses the fast hardware exp/log (relative error near
 // 2^-21, far below the network's own BF16 error). Sampling and the pdf both
 // use this form, so the estimator's weights match the sampled density.
-__device__ __forceinline__ void mixture_for_shading(const float* r, VmfMixture& m) {
+__device__ __forceinline__ void mixture_for_shading(const float* r, f3 p01, f3 ext, VmfMixture& m) {
     float mx = -1e30f;
     for (int k = 0; k < kGuideLobes; ++k) mx = fmaxf(mx, r[5 * k + 4]);
     float s = 0.f;
     for (int k = 0; k < kGuideLobes; ++k) {
         const float* q = r + 5 * k;
-        const float l2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const f3 a = lobe_axis(q, p01, ext);
+        const float l2 = dot(a, a);
         const float il = l2 > 1e-24f ? rsqrtf(l2) : 0.f;
-        m.mu[k] = il > 0.f ? mk(q[0] * il, q[1] * il, q[2] * il) : mk(0.f, 0.f, 1.f);
+        m.mu[k] = il > 0.f ? mk(a.x * il, a.y * il, a.z * il) : mk(0.f, 0.f, 1.f);
         const float z = q[3];
         const float sp = z > 20.f ? z : __logf(1.f + __expf(z));
         m.kappa[k] = fminf(kKappaMin + sp, kKappaMax);
@@ -154,9 +166,9 @@ __device__ __forceinline__ f3 mixture_sample(const VmfMixture& m, float u0, floa
 }
 
 // d(-log q(w)) / d(raw outputs), scaled by `scale`; returns -log q(w).
-__device__ __forceinline__ float mixture_nll_grad(const float* r, f3 w, float scale, float* g) {
+__device__ __forceinline__ float mixture_nll_grad(const float* r, f3 w, float scale, float* g, f3 p01, f3 ext) {
     VmfMixture m;
-    mixture_from_raw(r, m);
+    mixture_from_raw(r, p01, ext, m);
     float v[kGuideLobes], dlogv_dk[kGuideLobes];
     float q = 0.f;
     for (int k = 0; k < kGuideLobes; ++k) {
@@ -177,12 +189,14 @@ __device__ __forceinline__ float mixture_nll_grad(const float* r, f3 w, float sc
         const float kap_raw = kKappaMin + softplus(rk[3]);
         const float dk_dz = kap_raw < kKappaMax ? 1.f / (1.f + expf(-rk[3])) : 0.f;
         gk[3] = scale * (-resp * dlogv_dk[k] * dk_dz);
-        // mean direction: mu = m / |m|, d log v / d mu = kappa w
-        const float l = sqrtf(rk[0] * rk[0] + rk[1] * rk[1] + rk[2] * rk[2]);
+        // mean direction: mu = a / |a|, a = (anchor - p01) * ext;
+        // d log v / d mu = kappa w, d a / d anchor = diag(ext)
+        const f3 ax = lobe_axis(rk, p01, ext);
+        const float l = sqrtf(dot(ax, ax));
         if (l > 1e-12f) {
             const f3 mu = m.mu[k];
             const float c = dot(mu, w);
-            const f3 proj = (w - mu * c) * (1.f / l);  // (I - mu mu^T) w / |m|
+            const f3 proj = hmul((w - mu * c) * (1.f / l), ext);  // diag(ext) (I - mu mu^T) w / |a|
             const float s = -resp * m.kappa[k] * scale;
             gk[0] = s * proj.x;
             gk[1] = s * proj.y;

@@ -408,7 +408,9 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
         const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
         VmfMixture mix;
-        if (kGuided && guided) mixture_for_shading(raw, mix);
+        if (kGuided && guided)
+            mixture_for_shading(raw, hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z), mk(s.box_inv.x, s.box_inv.y, s.box_inv.z)),
+                                mk(1.f / s.box_inv.x, 1.f / s.box_inv.y, 1.f / s.box_inv.z), mix);
         const float alpha = gs.alpha;
 
         // 2. next-event estimation

@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_guide_train_fb(const float
     const int g = lane >> 2, t = lane & 3;
     float* so = reinterpret_cast<float*>(smem_raw + kSmemTrainW) + warp * 16 * 41;
     const uint32_t tiles = (n + 15) / 16;
+    const f3 ext = mk(1.f / gd.box_inv.x, 1.f / gd.box_inv.y, 1.f / gd.box_inv.z);
     float loss_acc = 0.f;
     for (uint32_t tile = blockIdx.x * kTrainWarps + warp; tile < tiles; tile += gridDim.x * kTrainWarps) {
         f3 p[2], nn[2];
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_guide_train_fb(const float
                 float raw[kGuideOut];
                 for (int k = 0; k < kGuideOut; ++k) raw[k] = so[lane * 41 + k];
                 const float w = fminf(a.w * inv_n, wcap);
-                loss_acc += w * mixture_nll_grad(raw, mk(c.x, c.y, c.z), w, gr);
+                loss_acc += w * mixture_nll_grad(raw, mk(c.x, c.y, c.z), w, gr, mk(a.x, a.y, a.z), ext);
             } else {
                 for (int k = 0; k < kGuideOut; ++k) gr[k] = 0.f;
             }

@@ -2,8 +2,11 @@
 
 Mirrors kazen_proto_gb300's guiding kernels: 51 input features (8-band
 sin/cos encoding of the position in the scene box + normal, padded to 64),
-three 64-wide ReLU layers, 40 outputs = 8 von Mises-Fisher lobes (mean,
-concentration = 0.05 + softplus, weight = softmax). `bf16=True` rounds to
+three 64-wide ReLU layers, 40 outputs = 8 von Mises-Fisher lobes (anchor
+point, concentration = 0.05 + softplus, weight = softmax). A lobe's mean
+direction points from the shading point p01 to its anchor, both in scene-box
+coordinates, measured in world units: normalize((anchor - p01) * ext), ext =
+the box extent. `bf16=True` rounds to
 bfloat16 (round to nearest even) exactly where the kernels store BF16:
 inputs, weights, activations after ReLU, and the back-propagated
 gradients; products accumulate in higher precision. The guiding network has
@@ -53,9 +56,16 @@ def softplus(x):
     return np.where(x > 20, x, np.log1p(np.exp(np.minimum(x, 20))))
 
 
-def mixture(raw):
+def lobe_axes(raw, p01, ext=(1.0, 1.0, 1.0)):
+    """(anchor - p01) * ext per lobe, (n, 8, 3)."""
     raw = np.asarray(raw, np.float64).reshape(-1, 8, 5)
-    m = raw[:, :, 0:3]
+    p01 = np.asarray(p01, np.float64).reshape(-1, 1, 3)
+    return (raw[:, :, 0:3] - p01) * np.asarray(ext, np.float64).reshape(1, 1, 3)
+
+
+def mixture(raw, p01, ext=(1.0, 1.0, 1.0)):
+    raw = np.asarray(raw, np.float64).reshape(-1, 8, 5)
+    m = lobe_axes(raw, p01, ext)
     ln = np.linalg.norm(m, axis=2, keepdims=True)
     mu = np.where(ln > 1e-12, m / np.maximum(ln, 1e-30), np.array([0, 0, 1.0]))
     kap = np.minimum(KAPPA_MIN + softplus(raw[:, :, 3]), KAPPA_MAX)
@@ -70,16 +80,16 @@ def vmf(mu, kap, d):
     return np.exp(lognorm + kap * ((mu * d[:, None, :]).sum(2) - 1))
 
 
-def pdf(raw, d):
-    mu, kap, w = mixture(raw)
+def pdf(raw, d, p01, ext=(1.0, 1.0, 1.0)):
+    mu, kap, w = mixture(raw, p01, ext)
     return (w * vmf(mu, kap, np.asarray(d, np.float64))).sum(1)
 
 
-def nll_and_grad(raw, d, scale):
+def nll_and_grad(raw, d, scale, p01, ext=(1.0, 1.0, 1.0)):
     """-log q(d) per row and d(scale * -log q)/d(raw) (n, 40), float64."""
     raw = np.asarray(raw, np.float64).reshape(-1, 8, 5)
     d = np.asarray(d, np.float64)
-    mu, kap, w = mixture(raw)
+    mu, kap, w = mixture(raw, p01, ext)
     v = vmf(mu, kap, d)
     q = np.maximum((w * v).sum(1), 1e-30)
     resp = w * v / q[:, None]
@@ -92,8 +102,9 @@ def nll_and_grad(raw, d, scale):
     g = np.zeros_like(raw)
     g[:, :, 4] = s * (w - resp)
     g[:, :, 3] = s * (-resp * dlogv * dk)
-    ln = np.linalg.norm(raw[:, :, 0:3], axis=2)
+    ln = np.linalg.norm(lobe_axes(raw, p01, ext), axis=2)
     proj = (d[:, None, :] - mu * cosd[:, :, None]) / np.maximum(ln, 1e-30)[:, :, None]
+    proj = proj * np.asarray(ext, np.float64).reshape(1, 1, 3)  # d axis / d anchor = diag(ext)
     g[:, :, 0:3] = np.where((ln > 1e-12)[:, :, None], (-resp * kap * s)[:, :, None] * proj, 0.0)
     return -np.log(q), g.reshape(-1, 40)
 
@@ -115,12 +126,12 @@ def forward(params, p01, n, use_bf16=True):
     return c
 
 
-def loss_and_grad(params, p01, n, d, weights, wscale, use_bf16=True):
+def loss_and_grad(params, p01, n, d, weights, wscale, use_bf16=True, ext=(1.0, 1.0, 1.0)):
     """Loss sum(w * wscale * -log q) and its gradient in the parameter layout."""
     r = bf16 if use_bf16 else (lambda a: np.asarray(a, np.float64))
     c = forward(params, p01, n, use_bf16)
     s = np.asarray(weights, np.float64) * wscale
-    nll, dO = nll_and_grad(c["O"], d, s)
+    nll, dO = nll_and_grad(c["O"], d, s, p01, ext)
     loss = float((s * nll).sum())
     W = c["W"]
     ft = np.float32 if use_bf16 else np.float64

@@ -1,6 +1,6 @@
 """CPU checks of the guiding network's restatement (oracle/guide_oracle.py):
 its analytic gradient against central finite differences in float64, and
-the vMF mixture's pdf normalisation."""
+the vMF mixture's pdf normalisation (anchor-point lobes, any box extent)."""
 import numpy as np
 import pytest
 
@@ -41,8 +41,28 @@ def test_mixture_pdf_integrates_to_one():
     m = 400000
     d = rng.standard_normal((m, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
-    q = G.pdf(np.repeat(raw, m, 0), d)
-    assert abs(q.mean() * 4 * np.pi - 1.0) < 0.02
+    p01 = np.repeat(rng.random((1, 3)), m, 0)
+    for ext in ((1.0, 1.0, 1.0), (3.0, 0.5, 2.0)):
+        q = G.pdf(np.repeat(raw, m, 0), d, p01, ext)
+        assert abs(q.mean() * 4 * np.pi - 1.0) < 0.02
+
+
+def test_gradient_with_box_extent_matches_finite_differences():
+    """The anchor gradient carries the box extent (d axis / d anchor = diag(ext))."""
+    rng = np.random.default_rng(3)
+    raw = rng.standard_normal((32, 40))
+    p01, _, d, w = batch(rng, 32)
+    ext = (3.0, 0.5, 2.0)
+    _, g = G.nll_and_grad(raw, d, w, p01, ext)
+    for i in rng.integers(0, 40, 25):
+        h = 1e-6
+        rp, rm = raw.copy(), raw.copy()
+        rp[:, i] += h
+        rm[:, i] -= h
+        lp = (w * G.nll_and_grad(rp, d, w, p01, ext)[0]).sum()
+        lm = (w * G.nll_and_grad(rm, d, w, p01, ext)[0]).sum()
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[:, i].sum()) <= 1e-5 + 1e-4 * abs(fd), (i, fd, g[:, i].sum())
 
 
 def test_bf16_rounding():
