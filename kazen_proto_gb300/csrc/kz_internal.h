@@ -209,6 +209,9 @@ void launch_generate_rays_dev(const kz_ray* rays, const PathParams& pp, PathSoA 
                               uint32_t block, cudaStream_t st);
 void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t block,
                             cudaStream_t st);
+void launch_shade_guided_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t cap, PathSoA out,
+                             ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
+                             uint32_t block, cudaStream_t st);
 void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq,
                       DevCounters* ctr, float* film, double* film64, const GuideShade* gs, uint32_t block,
                       cudaStream_t st);

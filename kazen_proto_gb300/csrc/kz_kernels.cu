@@ -1,164 +1,12 @@
-// kz_kernels.cu — sm_103a kernels of the kazen hot path: batch intersection,
-// closure batches, and the wavefront path integrator stages
-// (generate / trace / shade / shadow) over structure-of-arrays path state.
-//
-// The wavefront stages restate PathIntegrator::Li
-// (src/core/integrator.cpp:362-561 in kazen_proto) with the estimator
-// corrections listed at the top of k_shade. Random numbers: PCG32 stream
-// (seed, path id); a camera path first draws the pixel jitter (2 floats,
-// Renderer::render, src/core/renderer.cpp:57), then 9 floats per shaded
-// vertex in a fixed order whatever branches run:
-//   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
-//   [5] lobe pick   [6,7,8] lobe sample
-#include <algorithm>
-#include "kz_guide.cuh"
-#include "kz_internal.h"
-#include "kz_traverse.cuh"
+// kz_kernels.cu — sm_103a kernels of the kazen hot path other than traversal:
+// closure batches, path generation, shading (shade_vertex, kz_stages.cuh),
+// training-sample collection for guiding, the batched renderers (wavefront
+// stages over a job table, and the persistent megakernel) and the
+// device-driven loop's bookkeeping kernels.
+#include "kz_stages.cuh"
 
 namespace kz {
 namespace {
-
-constexpr uint32_t kSpecularFlag = 1u << 8;
-// Batched wavefront: bits 12-31 of a path's d4.w hold its job index (0 for a
-// single render); continuations keep them, shadow rays carry the job in c4.w.
-constexpr uint32_t kJobShift = 12;
-constexpr uint32_t kJobMask = 0xFFFFF000u;
-
-__device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
-    if (status) atomicCAS(status, 0u, code);
-}
-
-__device__ __forceinline__ f3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
-__device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
-
-// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
-__device__ __forceinline__ uint32_t warp_append(bool pred, uint32_t* counter) {
-    const unsigned mask = __activemask();
-    const unsigned ballot = __ballot_sync(mask, pred);
-    if (!pred) return 0xFFFFFFFFu;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
-    base = __shfl_sync(ballot, base, leader);
-    return base + (uint32_t)__popc(ballot & ((1u << lane) - 1u));
-}
-
-// ------------------------------------------------------------------ batch intersection
-__device__ __forceinline__ void store_hit(const DevScene& s, kz_hits hits, uint64_t i, const HitRec& h) {
-    hits.t[i] = h.t;
-    uint32_t geom = KZ_INVALID_ID, local = KZ_INVALID_ID;
-    if (h.rec >= 0) {
-        geom = __float_as_uint(__ldg(s.tris + (size_t)h.rec * 3 + 1).w);
-        local = h.prim - __ldg(s.geom_offset + geom);
-    }
-    hits.prim_id[i] = local;
-    if (hits.geom_id) hits.geom_id[i] = geom;
-    if (hits.u) hits.u[i] = h.u;
-    if (hits.v) hits.v[i] = h.v;
-}
-
-__global__ void k_intersect_any(DevScene s, const kz_ray* __restrict__ rays, uint64_t n, uint8_t* occ,
-                                uint32_t* status) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    const float4 a = __ldg(rp), b = __ldg(rp + 1);
-    TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
-    bool overflow;
-    uint32_t dn = 0, dt = 0;
-    bool hit = trace_any<false>(s, r, b.w, overflow, dn, dt);
-    if (overflow) set_status(status, KZ_ERR_STACK);
-    occ[i] = hit ? 1 : 0;
-}
-
-__global__ void k_intersect_stats(DevScene s, const kz_ray* __restrict__ rays, uint64_t n,
-                                  unsigned long long* counters, uint32_t* status) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t nn = 0, nt = 0;
-    if (i < n) {
-        const float4* rp = reinterpret_cast<const float4*>(rays + i);
-        const float4 a = __ldg(rp), b = __ldg(rp + 1);
-        TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
-        HitRec h;
-        if (!trace_closest<true>(s, r, b.w, h, nn, nt)) set_status(status, KZ_ERR_STACK);
-    }
-    // warp reduction, one atomic per warp
-    unsigned long long a0 = nn, a1 = nt;
-    for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_down_sync(0xffffffffu, a0, o);
-        a1 += __shfl_down_sync(0xffffffffu, a1, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(counters, a0);
-        atomicAdd(counters + 1, a1);
-    }
-}
-
-// ------------------------------------------------------------------ closures
-__global__ void k_closure_eval(const kz_lobe* __restrict__ lobes, const float* __restrict__ wi,
-                               const float* __restrict__ wo, uint64_t n, int conv, float* f, float* pdf) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const kz_lobe l = lobes[i];
-    const f3 a = ld3(wi + 3 * i), b = ld3(wo + 3 * i);
-    LobeEval e = conv == KZ_CONVENTION_REFERENCE ? lobe_eval_reference(l, a, b) : lobe_eval(l, a, b);
-    f[3 * i] = e.f.x;
-    f[3 * i + 1] = e.f.y;
-    f[3 * i + 2] = e.f.z;
-    pdf[i] = e.pdf;
-}
-
-__global__ void k_closure_sample(const kz_lobe* __restrict__ lobes, const float* __restrict__ wi,
-                                 const float* __restrict__ u, uint64_t n, float* wo, float* weight, float* pdf,
-                                 uint8_t* flags) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const kz_lobe l = lobes[i];
-    LobeSample s = lobe_sample(l, ld3(wi + 3 * i), u[3 * i], u[3 * i + 1], u[3 * i + 2]);
-    wo[3 * i] = s.wo.x;
-    wo[3 * i + 1] = s.wo.y;
-    wo[3 * i + 2] = s.wo.z;
-    weight[3 * i] = s.weight.x;
-    weight[3 * i + 1] = s.weight.y;
-    weight[3 * i + 2] = s.weight.z;
-    pdf[i] = s.pdf;
-    flags[i] = (uint8_t)((s.valid ? 1 : 0) | (s.delta ? 2 : 0));
-}
-
-// ------------------------------------------------------------------ wavefront stages
-__device__ __forceinline__ void generate_camera_path(const DevCamera& cam, const PathParams& pp, PathSoA dst,
-                                                     uint32_t k, uint64_t pid) {
-    const uint64_t pix = pid / pp.spp;
-    const uint32_t px = (uint32_t)(pix % cam.W), py = (uint32_t)(pix / cam.W);
-    Pcg rng;
-    rng.seed(pp.seed, pid);
-    const float jx = rng.nextf(), jy = rng.nextf();
-    // Camera::generate_ray (src/core/camera.cpp:5-37): horizontal fov,
-    // row 0 at the top unless flipped.
-    const float sx = ((float)px + jx) / (float)cam.W;
-    const float sy = ((float)py + jy) / (float)cam.H;
-    const float nx = 2.0f * sx - 1.0f;
-    const float ny = cam.flip * ((1.0f - 2.0f * sy) / cam.aspect);
-    const float cx = nx * cam.tan_half;
-    const float cy = ny * cam.tan_half;
-    const f3 d = normalize(ld3(cam.x) * cx + ld3(cam.y) * cy + ld3(cam.z) * (-1.0f));
-    dst.o4[k] = make_float4(cam.eye[0], cam.eye[1], cam.eye[2], 0.f);
-    dst.d4[k] = make_float4(d.x, d.y, d.z, __uint_as_float(kSpecularFlag));
-    dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
-    dst.rng[k] = rng.state;
-}
-
-__device__ __forceinline__ void generate_ray_path(const kz_ray* __restrict__ rays, const PathParams& pp, PathSoA dst,
-                                                  uint32_t k, uint64_t pid) {
-    Pcg rng;
-    rng.seed(pp.seed, pid);
-    const kz_ray r = rays[pid];
-    dst.o4[k] = make_float4(r.ox, r.oy, r.oz, 0.f);
-    dst.d4[k] = make_float4(r.dx, r.dy, r.dz, __uint_as_float(kSpecularFlag));
-    dst.b4[k] = make_float4(1.f, 1.f, 1.f, __uint_as_float((uint32_t)pid));
-    dst.rng[k] = rng.state;
-}
 
 __global__ void k_generate_camera(DevCamera cam, PathParams pp, PathSoA dst, uint32_t dst_offset,
                                   uint64_t first_path, uint32_t n_new) {
@@ -174,524 +22,7 @@ __global__ void k_generate_rays(const kz_ray* __restrict__ rays, PathParams pp, 
     generate_ray_path(rays, pp, dst, dst_offset + j, first_path + j);
 }
 
-// Sums two per-thread counters over the warp; one 64-bit atomic each.
-__device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long long* dst) {
-    unsigned long long x = a, y = b;
-    for (int o = 16; o > 0; o >>= 1) {
-        x += __shfl_down_sync(0xffffffffu, x, o);
-        y += __shfl_down_sync(0xffffffffu, y, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(dst, x);
-        atomicAdd(dst + 1, y);
-    }
-}
 
-template <bool kCount>
-__global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint32_t n, DevCounters* ctr,
-                                                     const uint32_t* n_dev) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n_dev) n = *n_dev;
-    uint32_t dn = 0, dt = 0;
-    if (i < n) {
-        const float4 o = p.o4[i], d = p.d4[i];
-        TRay r = make_tray(xyz(o), xyz(d), kRayEps);
-        HitRec h;
-        if (!trace_closest<kCount>(s, r, __int_as_float(0x7f800000), h, dn, dt)) {
-            set_status(&ctr->status, KZ_ERR_STACK);
-            h.rec = -1;
-        }
-        p.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec));
-    }
-    if (kCount) warp_count(dn, dt, &ctr->fetch[0]);
-}
-
-// Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
-// ray up, store(k, hit) writes the result.
-// `s` is the lane's scene; load may repoint it per ray (batched jobs).
-template <bool kCount, typename Ctr, typename Load, typename Store>
-__device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
-                                                   Store store, uint32_t& dn, uint32_t& dt) {
-    uint2 stack[kWideStack];
-    ClosestState c;
-    TRay r;
-    float tmax = 0.f;
-    uint32_t octp = 0;
-    Ctr ray = 0;
-    persistent_rays(
-        n, next, kTraceRefill,
-        [&](Ctr k) {
-            ray = k;
-            load(k, r, tmax);
-            octp = wide_octant(r);
-            closest_begin(c, tmax);
-        },
-        [&]() {
-            const int rc = closest_step<kCount>(s, r, octp, c, stack, dn, dt);
-            if (rc == 0) return false;
-            HitRec h;
-            closest_finish(c, rc > 0, tmax, h);
-            if (rc < 0) set_status(status, KZ_ERR_STACK);
-            store(ray, h);
-            return true;
-        });
-}
-
-// Closest-hit pass of the device-driven loop (k_plan zeroes trace_next).
-template <bool kCount>
-__global__ void __launch_bounds__(256) k_trace_paths_persistent(DevScene s, PathSoA p, DevCounters* ctr) {
-    uint32_t dn = 0, dt = 0;
-    persistent_closest<kCount>(
-        s, ctr->n_active, &ctr->trace_next, &ctr->status,
-        [&](uint32_t k, TRay& r, float& tmax) {
-            const float4 o = p.o4[k], d = p.d4[k];
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = __int_as_float(0x7f800000);
-        },
-        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
-    if (kCount) warp_count(dn, dt, &ctr->fetch[0]);
-}
-
-// kz_intersect_closest: rays (o, tmin, d, tmax) in, hit fields out.
-__global__ void __launch_bounds__(256) k_intersect_closest_persistent(DevScene s, const kz_ray* __restrict__ rays,
-                                                                      unsigned long long n, kz_hits hits,
-                                                                      unsigned long long* next, uint32_t* status) {
-    uint32_t dn = 0, dt = 0;
-    persistent_closest<false>(
-        s, n, next, status,
-        [&](unsigned long long k, TRay& r, float& tmax) {
-            const float4* rp = reinterpret_cast<const float4*>(rays + k);
-            const float4 a = __ldg(rp), b = __ldg(rp + 1);
-            r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
-            tmax = b.w;
-        },
-        [&](unsigned long long k, const HitRec& h) { store_hit(s, hits, k, h); }, dn, dt);
-}
-
-__device__ __forceinline__ void film_add(float* film, double* film64, uint32_t idx, f3 c) {
-    atomicAdd(film + 3 * (size_t)idx, c.x);
-    atomicAdd(film + 3 * (size_t)idx + 1, c.y);
-    atomicAdd(film + 3 * (size_t)idx + 2, c.z);
-    if (film64) {
-        atomicAdd(film64 + 3 * (size_t)idx, (double)c.x);
-        atomicAdd(film64 + 3 * (size_t)idx + 1, (double)c.y);
-        atomicAdd(film64 + 3 * (size_t)idx + 2, (double)c.z);
-    }
-}
-
-// DiscrectPDF::sample (src/base/dpdf.h:31-36): lower_bound over cdf[0..n].
-__device__ __forceinline__ uint32_t cdf_sample(const float* cdf, uint32_t n, float u) {
-    uint32_t lo = 0, cnt = n + 1;
-    while (cnt > 0) {
-        uint32_t step = cnt / 2, it = lo + step;
-        if (__ldg(cdf + it) < u) {
-            lo = it + 1;
-            cnt -= step + 1;
-        } else {
-            cnt = step;
-        }
-    }
-    int idx = (int)lo - 1;
-    if (idx < 0) idx = 0;
-    return min((uint32_t)idx, n - 1);
-}
-
-// One shaded vertex per thread. Estimator corrections relative to the
-// reference loop (each one keeps the estimator unbiased):
-//  * NEE uses f*|cos| once (the reference multiplies Diffuse's f*cos by cos
-//    again, integrator.cpp:475-480) and divides by the light pick pdf inside
-//    the MIS weight as well as outside;
-//  * BSDF sampling divides by the direction pdf (integrator.cpp:503-505
-//    multiplies by f only) and picks the lobe by its selection probability;
-//  * emission hits weigh against the light pdf of the sampled direction
-//    (integrator.cpp:452-462 reuses the previous light sample's pdf);
-//  * max_depth counts shaded vertices (the reference steps depth twice per
-//    loop, integrator.cpp:420,555).
-// Guided mode (learned path guiding, not in the reference) additionally:
-//  * on materials without delta lobes, samples the direction from the
-//    network's vMF mixture with probability alpha and from the BSDF mixture
-//    otherwise, with the one-sample MIS pdf alpha*q + (1-alpha)*p_bsdf in the
-//    path weight, the NEE MIS weight and the next emission hit's MIS weight;
-//  * records every such vertex (position, normal, direction, pdf,
-//    throughput after it) and adds each later contribution, divided by that
-//    throughput, to the vertex's incident-radiance estimate: the training
-//    data of the network.
-__device__ __forceinline__ void propagate(VRec* recs, uint64_t rbase, uint32_t depth, f3 c) {
-    for (uint32_t k = 0; k < depth; ++k) {
-        VRec& r = recs[rbase + k];
-        if (r.n.w == 0.f) continue;
-        const float4 b = r.beta;
-        r.L.x += b.x > 0.f ? c.x / b.x : 0.f;
-        r.L.y += b.y > 0.f ? c.y / b.y : 0.f;
-        r.L.z += b.z > 0.f ? c.z / b.z : 0.f;
-    }
-}
-
-struct ShadeOut {
-    bool cont = false, shadow = false;
-    float4 o_next, d_next, b_next, s_o, s_d, s_c;
-    unsigned long long rng_next = 0;
-    f3 Lsum = {0.f, 0.f, 0.f};  // contribution to the film pixel film_idx
-    uint32_t film_idx = 0;
-};
-
-// One shaded path vertex: emission, next-event estimation (the shadow ray is
-// returned, not traced), roulette and direction sampling. `raw` holds the
-// guiding network's outputs for this path (guided mode only).
-template <bool kGuided>
-__device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams& pp, const float4 hit,
-                                             const float4 o4, const float4 d4, const float4 b4,
-                                             unsigned long long rng_state, const GuideShade& gs, const float* raw,
-                                             ShadeOut& out) {
-    const int rec = __float_as_int(hit.w);
-    if (rec >= 0) {
-        const uint32_t pid = __float_as_uint(b4.w);
-        const uint32_t film_idx = pid / pp.spp;
-        const uint32_t flags = __float_as_uint(d4.w);
-        const uint32_t depth = flags & 0xffu;
-        const bool prev_spec = (flags & kSpecularFlag) != 0;
-        const float prev_pdf = o4.w;
-        Pcg rng;
-        rng.state = rng_state;
-        rng.inc = ((uint64_t)pid << 1u) | 1u;
-        float u[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
-
-        const float4* tp = s.tris + (size_t)rec * 3;
-        const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
-        const uint32_t geom = __float_as_uint(tb.w);
-        const kz_material& mat = s.materials[__float_as_uint(tc.w)];
-        const f3 v0 = xyz(ta), v1 = xyz(tb), v2 = xyz(tc);
-        const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
-        const f3 d = xyz(d4);
-        const f3 P = xyz(o4) + d * hit.x;
-        const Frame fr(Ng);
-        const f3 wi = -fr.to_local(d);
-        f3 beta = xyz(b4);
-        f3 Lsum = mk(0.f, 0.f, 0.f);
-        const uint32_t nl = s.n_lights;
-        const uint64_t rbase = kGuided ? ((uint64_t)pid - gs.pass_first) * pp.max_depth : 0;
-
-        // 1. emission (front face only: single_emissive_surface)
-        const f3 Le = ld3(mat.Le);
-        if (!is_zero(Le) && dot(d, Ng) < 0.f) {
-            float w = 1.f;
-            if (!prev_spec) {
-                const int li = __ldg(s.geom_light + geom);
-                if (li >= 0) {
-                    const float cos_l = -dot(d, Ng);
-                    const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
-                    w = power_heuristic(prev_pdf, lpdf);
-                }
-            }
-            Lsum = Lsum + hmul(beta, Le) * w;
-            // MIS-weighted, like the next-event samples it pairs with
-            if (kGuided && gs.recs) propagate(gs.recs, rbase, depth, Lsum);
-        }
-
-        // lobe selection probabilities (CompositeClosure::compute_pdfs)
-        const uint32_t nlobes = min(mat.n_lobes, (uint32_t)KZ_MAX_LOBES);
-        float lp[KZ_MAX_LOBES];
-        const float winv = 1.f / (beta.x + beta.y + beta.z);
-        float wsum = 0.f;
-        bool any_smooth = false, any_delta = false;
-        for (uint32_t k = 0; k < nlobes; ++k) {
-            const kz_lobe& lb = mat.lobes[k];
-            lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
-            wsum += lp[k];
-            const bool dl = lobe_is_delta(lb.closure_id);
-            any_smooth |= !dl;
-            any_delta |= dl;
-        }
-        if (wsum > 0.f)
-            for (uint32_t k = 0; k < nlobes; ++k) lp[k] /= wsum;
-        const bool guided = kGuided && any_smooth && !any_delta && wsum > 0.f;
-        VmfMixture mix;
-        if (kGuided && guided)
-            mixture_for_shading(raw, hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z), mk(s.box_inv.x, s.box_inv.y, s.box_inv.z)),
-                                mk(1.f / s.box_inv.x, 1.f / s.box_inv.y, 1.f / s.box_inv.z), mix);
-        const float alpha = gs.alpha;
-
-        // 2. next-event estimation
-        if (nl > 0 && any_smooth && wsum > 0.f) {
-            const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
-            const DevLight lt = s.lights[li];
-            const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
-            const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
-            const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
-            const float su0 = sqrtf(u[2]);
-            const float bu0 = 1.f - su0;
-            const float bv0 = u[3] * su0;
-            const f3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
-            const f3 nlgt = normalize(cross(a1 - a0, a2 - a0));
-            const f3 lv = p - P;
-            const float dist2 = dot(lv, lv);
-            const float dist = sqrtf(dist2);
-            const f3 ldir = mk(lv.x / dist, lv.y / dist, lv.z / dist);
-            const float cos_l = -dot(ldir, nlgt);
-            if (cos_l > 0.f) {
-                const float pdf_solid = dist2 / (cos_l * lt.area);
-                const float lpdf = pdf_solid * (1.0f / (float)nl);
-                const f3 wo = fr.to_local(ldir);
-                f3 f = mk(0.f, 0.f, 0.f);
-                float bpdf = 0.f;
-                for (uint32_t k = 0; k < nlobes; ++k) {
-                    const kz_lobe& lb = mat.lobes[k];
-                    if (lobe_is_delta(lb.closure_id)) continue;
-                    const LobeEval e = lobe_eval(lb, wi, wo);
-                    f = f + hmul(ld3(lb.weight), e.f);
-                    bpdf += lp[k] * e.pdf;
-                }
-                if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
-                if (!is_zero(f)) {
-                    const float w = power_heuristic(lpdf, bpdf);
-                    const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
-                    out.shadow = true;
-                    out.s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
-                    out.s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
-                    const uint32_t tag = kGuided ? (uint32_t)(((uint64_t)pid - gs.pass_first) << 4 | (depth & 15u))
-                                                 : flags >> kJobShift;
-                    out.s_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
-                    if (kGuided && gs.nee && guided) {
-                        // training sample: the light direction with its
-                        // MIS-weighted share of L*f*cos over the light pdf
-                        const f3 fl = hmul(f, ld3(lt.Le));
-                        const float wt = (0.2126f * fl.x + 0.7152f * fl.y + 0.0722f * fl.z) * (w / lpdf);
-                        const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
-                                            mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
-                        NRec& nr = gs.nee[rbase + depth];
-                        nr.p = make_float4(p01.x, p01.y, p01.z, wt);
-                        nr.n = make_float4(Ng.x, Ng.y, Ng.z, 0.f);
-                        nr.d = make_float4(ldir.x, ldir.y, ldir.z, 0.f);
-                    }
-                }
-            }
-        }
-
-        bool alive = depth + 1 < pp.max_depth;
-        // 3. Russian roulette (integrator.cpp:491-498)
-        if (alive && depth >= pp.rr_min) {
-            const float prob = fminf(max_comp(beta) * 0.9025f, 0.99f);
-            if (prob < u[4]) alive = false;
-            else beta = beta * (1.f / prob);
-        }
-        // 4. direction sampling
-        if (kGuided && guided && alive) {
-            // one-sample MIS of the learned vMF mixture and the BSDF mixture
-            f3 wo, wdir;
-            bool ok = true;
-            if (u[5] < alpha) {
-                wdir = mixture_sample(mix, u[5] / alpha, u[6], u[7]);
-                wo = fr.to_local(wdir);
-            } else {
-                const float us = (u[5] - alpha) / (1.f - alpha);
-                uint32_t sel = nlobes - 1;
-                float acc = 0.f;
-                for (uint32_t k = 0; k < nlobes; ++k) {
-                    acc += lp[k];
-                    if (us < acc) {
-                        sel = k;
-                        break;
-                    }
-                }
-                while (sel > 0 && lp[sel] == 0.f) --sel;
-                const LobeSample smp = lobe_sample(mat.lobes[sel], wi, u[6], u[7], u[8]);
-                ok = smp.valid;
-                wo = smp.wo;
-                wdir = normalize(fr.to_world(wo));
-            }
-            f3 f = mk(0.f, 0.f, 0.f);
-            float pdf = 0.f;
-            if (ok) {
-                for (uint32_t k = 0; k < nlobes; ++k) {
-                    const kz_lobe& lb = mat.lobes[k];
-                    const LobeEval e = lobe_eval(lb, wi, wo);
-                    f = f + hmul(ld3(lb.weight), e.f);
-                    pdf += lp[k] * e.pdf;
-                }
-                pdf = alpha * mixture_pdf_shading(mix, wdir) + (1.f - alpha) * pdf;
-            }
-            alive = ok && pdf > 0.f && !is_zero(f);
-            if (alive) {
-                beta = hmul(beta, f * (1.f / pdf));
-                alive = !is_zero(beta);
-            }
-            if (alive) {
-                out.cont = true;
-                out.o_next = make_float4(P.x, P.y, P.z, pdf);
-                out.d_next = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float((depth + 1) | (flags & kJobMask)));
-                out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
-                out.rng_next = rng.state;
-            }
-            if (alive && gs.recs) {
-                VRec& r = gs.recs[rbase + depth];
-                const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
-                                    mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));
-                r.p = make_float4(p01.x, p01.y, p01.z, pdf);
-                r.n = make_float4(Ng.x, Ng.y, Ng.z, 1.f);
-                // d.w: luminance of f*|cos| along the sampled direction,
-                // so the network learns the whole integrand L*f*cos
-                r.d = make_float4(wdir.x, wdir.y, wdir.z, 0.2126f * f.x + 0.7152f * f.y + 0.0722f * f.z);
-                r.beta = make_float4(beta.x, beta.y, beta.z, 0.f);
-                r.L = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        } else if (alive && wsum > 0.f) {
-            // BSDF sample (one-sample mixture over the non-delta lobes)
-            uint32_t sel = nlobes - 1;
-            float acc = 0.f;
-            for (uint32_t k = 0; k < nlobes; ++k) {
-                acc += lp[k];
-                if (u[5] < acc) {
-                    sel = k;
-                    break;
-                }
-            }
-            while (sel > 0 && lp[sel] == 0.f) --sel;
-            const kz_lobe& ls = mat.lobes[sel];
-            const LobeSample smp = lobe_sample(ls, wi, u[6], u[7], u[8]);
-            alive = smp.valid;
-            f3 weight = mk(0.f, 0.f, 0.f);
-            float pdf_dir = 0.f;
-            if (alive) {
-                if (smp.delta) {
-                    weight = hmul(ld3(ls.weight), smp.weight) * (1.f / lp[sel]);
-                } else {
-                    f3 f = mk(0.f, 0.f, 0.f);
-                    float pdf = 0.f;
-                    for (uint32_t k = 0; k < nlobes; ++k) {
-                        const kz_lobe& lb = mat.lobes[k];
-                        if (lobe_is_delta(lb.closure_id)) continue;
-                        const LobeEval e = lobe_eval(lb, wi, smp.wo);
-                        f = f + hmul(ld3(lb.weight), e.f);
-                        pdf += lp[k] * e.pdf;
-                    }
-                    alive = pdf > 0.f;
-                    if (alive) weight = f * (1.f / pdf);
-                    pdf_dir = pdf;
-                }
-            }
-            if (alive) {
-                beta = hmul(beta, weight);
-                alive = !is_zero(beta);
-            }
-            if (alive) {
-                const f3 dn = normalize(fr.to_world(smp.wo));
-                out.cont = true;
-                out.o_next = make_float4(P.x, P.y, P.z, pdf_dir);
-                out.d_next = make_float4(
-                    dn.x, dn.y, dn.z,
-                    __uint_as_float((depth + 1) | (smp.delta ? kSpecularFlag : 0u) | (flags & kJobMask)));
-                out.b_next = make_float4(beta.x, beta.y, beta.z, b4.w);
-                out.rng_next = rng.state;
-            }
-        }
-        out.Lsum = Lsum;
-            out.film_idx = film_idx;
-    }
-}
-
-// Plain shading is capped at 64 registers (4 blocks per SM): the occupancy
-// gained outweighs a few spills (measured: 5 % faster); the guided variant
-// keeps its registers (at 64 it spills 728 bytes per thread).
-template <bool kGuided>
-__global__ void __launch_bounds__(256, kGuided ? 1 : 4)
-    k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
-                                               ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
-                                               GuideShade gs, const uint32_t* n_dev) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n_dev) n_in = *n_dev;
-    ShadeOut so;
-    if (i < n_in) {
-        shade_vertex<kGuided>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
-                              kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
-        if (!is_zero(so.Lsum)) film_add(film, film64, so.film_idx, so.Lsum);
-    }
-    const bool cont = so.cont, shadow = so.shadow;
-    const uint32_t slot = warp_append(cont, &ctr->n_next);
-    if (cont) {
-        out.o4[slot] = so.o_next;
-        out.d4[slot] = so.d_next;
-        out.b4[slot] = so.b_next;
-        out.rng[slot] = so.rng_next;
-    }
-    const uint32_t sslot = warp_append(shadow, &ctr->n_shadow);
-    if (shadow) {
-        sq.o4[sslot] = so.s_o;
-        sq.d4[sslot] = so.s_d;
-        sq.c4[sslot] = so.s_c;
-    }
-}
-
-template <bool kCount, bool kGuided>
-__global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, DevCounters* ctr, float* film,
-                                                      double* film64, VRec* recs, NRec* nee, uint32_t max_depth) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t dn = 0, dt = 0;
-    if (i < ctr->n_shadow) {
-        const float4 o = sq.o4[i], d = sq.d4[i];
-        TRay r = make_tray(xyz(o), xyz(d), kRayEps);
-        bool overflow;
-        const bool occluded = trace_any<kCount>(s, r, o.w, overflow, dn, dt);
-        if (overflow) set_status(&ctr->status, KZ_ERR_STACK);
-        if (!occluded && !overflow) {
-            const float4 c = sq.c4[i];
-            film_add(film, film64, __float_as_uint(d.w), xyz(c));
-            if (kGuided && recs) {
-                const uint32_t tag = __float_as_uint(c.w);
-                const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
-                propagate(recs, rb, tag & 15u, xyz(c));
-                if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
-            }
-        }
-    }
-    if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
-}
-
-// Persistent form of k_trace_shadow for the device-driven loop (k_plan zeroes
-// shadow_next each iteration).
-template <bool kCount, bool kGuided>
-__global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, ShadowSoA sq, DevCounters* ctr,
-                                                                 float* film, double* film64, VRec* recs, NRec* nee,
-                                                                 uint32_t max_depth) {
-    uint32_t dn = 0, dt = 0;
-    uint2 stack[kWideStack];
-    AnyState c;
-    TRay r;
-    float tmax = 0.f;
-    uint32_t octp = 0, ray = 0;
-    persistent_rays(
-        ctr->n_shadow, &ctr->shadow_next, kTraceRefill,
-        [&](uint32_t k) {
-            ray = k;
-            const float4 o = sq.o4[k], d = sq.d4[k];
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = o.w;
-            octp = wide_octant(r);
-            any_begin(c);
-        },
-        [&]() {
-            const int rc = any_step<kCount>(s, r, octp, tmax, c, stack, dn, dt);
-            if (rc == 0) return false;
-            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
-            if (rc == 1) {
-                const float4 cc = sq.c4[ray];
-                film_add(film, film64, __float_as_uint(sq.d4[ray].w), xyz(cc));
-                if (kGuided && recs) {
-                    const uint32_t tag = __float_as_uint(cc.w);
-                    const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
-                    propagate(recs, rb, tag & 15u, xyz(cc));
-                    if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
-                }
-            }
-            return true;
-        });
-    if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
-}
-
-// Training samples from the records of a guided pass: every valid vertex
-// whose integrand estimate L*f*cos is positive, weighted by its luminance
-// over the pdf the direction was sampled with.
 __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __restrict__ nee, uint64_t n,
                                 float4* __restrict__ samples, uint32_t cap, uint32_t* count, float* wsum) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -723,203 +54,6 @@ __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __res
         samples[3 * (size_t)slot + 2] = c;
         atomicAdd(wsum, a.w);
     }
-}
-
-// ------------------------------------------------------------------ persistent batch renderer
-// Many independent jobs (scenes, cameras, films) in one launch. Lanes hold a
-// path each; every `period` vertices (or when a warp has no live path) free
-// lanes take the next global path ids with one atomic per warp, find their
-// job by binary search over the jobs' first path ids, and start a camera
-// path. Each vertex is traced, shaded (shade_vertex) and its shadow ray
-// traced inline. Loop exit is warp-uniform: the fetch counter only grows and
-// ends the loop once it passes the total with no live lane left.
-__device__ __forceinline__ uint32_t find_job(const DevJob* __restrict__ jobs, uint32_t n_jobs, unsigned long long g) {
-    uint32_t lo = 0, hi = n_jobs;  // last job with path_begin <= g
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (jobs[mid].path_begin <= g) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(256) k_render_batch(const DevJob* __restrict__ jobs, uint32_t n_jobs,
-                                                      unsigned long long total, BatchCounters* bc, uint32_t period) {
-    const int lane = threadIdx.x & 31;
-    bool active = false, exhausted = false;
-    uint32_t job = 0;
-    float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4, b4 = o4;
-    unsigned long long rng = 0;
-    unsigned long long n_bounce = 0, n_shadow = 0;
-    for (uint32_t step = 0;; ++step) {
-        const bool any_live = __any_sync(0xffffffffu, active);
-        if (!exhausted && (step % period == 0 || !any_live)) {
-            const unsigned want = __ballot_sync(0xffffffffu, !active);
-            if (want) {
-                const int leader = __ffs(want) - 1;
-                unsigned long long base = 0;
-                if (lane == leader) base = atomicAdd(&bc->next_path, (unsigned long long)__popc(want));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (!active) {
-                    const unsigned long long g = base + (unsigned)__popc(want & ((1u << lane) - 1u));
-                    if (g < total) {
-                        job = find_job(jobs, n_jobs, g);
-                        const DevJob& J = jobs[job];
-                        PathSoA one;
-                        one.o4 = &o4;
-                        one.d4 = &d4;
-                        one.b4 = &b4;
-                        one.rng = &rng;
-                        generate_camera_path(J.cam, J.pp, one, 0, g - J.path_begin);
-                        active = true;
-                    }
-                }
-                if (base + (unsigned)__popc(want) >= total) exhausted = true;
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) {
-            if (exhausted) break;
-            continue;
-        }
-        if (active) {
-            const DevJob& J = jobs[job];
-            TRay r = make_tray(xyz(o4), xyz(d4), kRayEps);
-            HitRec h;
-            uint32_t dn = 0, dt = 0;
-            if (!trace_closest<false>(J.scene, r, __int_as_float(0x7f800000), h, dn, dt)) {
-                set_status(&bc->status, KZ_ERR_STACK);
-                h.rec = -1;
-            }
-            ++n_bounce;
-            ShadeOut so;
-            shade_vertex<false>(J.scene, J.pp, make_float4(h.t, h.u, h.v, __int_as_float(h.rec)), o4, d4, b4, rng,
-                                GuideShade{}, nullptr, so);
-            if (!is_zero(so.Lsum)) film_add(J.film, nullptr, so.film_idx, so.Lsum);
-            if (so.shadow) {
-                ++n_shadow;
-                TRay sr = make_tray(xyz(so.s_o), xyz(so.s_d), kRayEps);
-                bool overflow;
-                const bool occ = trace_any<false>(J.scene, sr, so.s_o.w, overflow, dn, dt);
-                if (overflow) set_status(&bc->status, KZ_ERR_STACK);
-                if (!occ && !overflow) film_add(J.film, nullptr, __float_as_uint(so.s_d.w), xyz(so.s_c));
-            }
-            if (so.cont) {
-                o4 = so.o_next;
-                d4 = so.d_next;
-                b4 = so.b_next;
-                rng = so.rng_next;
-            } else {
-                active = false;
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        n_bounce += __shfl_down_sync(0xffffffffu, n_bounce, o);
-        n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, o);
-    }
-    if (lane == 0) {
-        atomicAdd(&bc->path_bounces, n_bounce);
-        atomicAdd(&bc->shadow_rays, n_shadow);
-    }
-}
-
-// ------------------------------------------------------------------ batched wavefront
-// Many jobs in one wavefront: paths of all jobs share the path buffers and
-// the stage kernels; each path finds its scene, camera, parameters and film
-// through its job index (d4.w bits 12-31, c4.w for shadow rays). Global path
-// ids [0, total) are generated in job order; a path's own id is local to its
-// job, so every job renders exactly what kz_render renders for it.
-
-__global__ void k_generate_batch_dev(const DevJob* __restrict__ jobs, uint32_t n_jobs, PathSoA dst,
-                                     const DevCounters* c) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= c->gen_count) return;
-    const unsigned long long g = c->gen_first + j;
-    const uint32_t job = find_job(jobs, n_jobs, g);
-    const DevJob& J = jobs[job];
-    const uint32_t k = c->gen_slot + j;
-    generate_camera_path(J.cam, J.pp, dst, k, g - J.path_begin);
-    dst.d4[k].w = __uint_as_float(__float_as_uint(dst.d4[k].w) | (job << kJobShift));
-}
-
-// The traversal reads only these fields of a scene.
-__device__ __forceinline__ void trace_fields(DevScene& dst, const DevScene& src) {
-    dst.nodes = src.nodes;
-    dst.tris = src.tris;
-    dst.n_nodes = src.n_nodes;
-    dst.n_tris = src.n_tris;
-}
-
-__global__ void __launch_bounds__(256) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
-                                                           DevCounters* ctr) {
-    uint32_t dn = 0, dt = 0;
-    DevScene ls;
-    persistent_closest<false>(
-        ls, ctr->n_active, &ctr->trace_next, &ctr->status,
-        [&](uint32_t k, TRay& r, float& tmax) {
-            const float4 o = p.o4[k], d = p.d4[k];
-            trace_fields(ls, jobs[__float_as_uint(d.w) >> kJobShift].scene);
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = __int_as_float(0x7f800000);
-        },
-        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
-}
-
-__global__ void __launch_bounds__(256, 4) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
-                                                     ShadowSoA sq, DevCounters* ctr) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n_in = ctr->n_active;
-    ShadeOut so;
-    if (i < n_in) {
-        const float4 d4 = in.d4[i];
-        const DevJob& J = jobs[__float_as_uint(d4.w) >> kJobShift];
-        shade_vertex<false>(J.scene, J.pp, in.hit[i], in.o4[i], d4, in.b4[i], in.rng[i], GuideShade{}, nullptr, so);
-        if (!is_zero(so.Lsum)) film_add(J.film, nullptr, so.film_idx, so.Lsum);
-    }
-    const bool cont = so.cont, shadow = so.shadow;
-    const uint32_t slot = warp_append(cont, &ctr->n_next);
-    if (cont) {
-        out.o4[slot] = so.o_next;
-        out.d4[slot] = so.d_next;
-        out.b4[slot] = so.b_next;
-        out.rng[slot] = so.rng_next;
-    }
-    const uint32_t sslot = warp_append(shadow, &ctr->n_shadow);
-    if (shadow) {
-        sq.o4[sslot] = so.s_o;
-        sq.d4[sslot] = so.s_d;
-        sq.c4[sslot] = so.s_c;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
-                                                            DevCounters* ctr) {
-    uint32_t dn = 0, dt = 0;
-    uint2 stack[kWideStack];
-    AnyState c;
-    TRay r;
-    DevScene ls;
-    float tmax = 0.f;
-    uint32_t octp = 0, ray = 0, job = 0;
-    persistent_rays(
-        ctr->n_shadow, &ctr->shadow_next, kTraceRefill,
-        [&](uint32_t k) {
-            ray = k;
-            const float4 o = sq.o4[k], d = sq.d4[k];
-            job = __float_as_uint(sq.c4[k].w);
-            trace_fields(ls, jobs[job].scene);
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = o.w;
-            octp = wide_octant(r);
-            any_begin(c);
-        },
-        [&]() {
-            const int rc = any_step<false>(ls, r, octp, tmax, c, stack, dn, dt);
-            if (rc == 0) return false;
-            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
-            if (rc == 1) film_add(jobs[job].film, nullptr, __float_as_uint(sq.d4[ray].w), xyz(sq.c4[ray]));
-            return true;
-        });
 }
 
 // ------------------------------------------------------------------ device-driven loop
@@ -967,47 +101,8 @@ __global__ void k_scale(float* film, double* film64, uint64_t n, float sf, doubl
     if (film64) film64[i] *= sd;
 }
 
-inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
-
-// Blocks of `block` threads resident on the whole device for kernel f.
-template <typename F>
-static unsigned resident_grid(F f, unsigned block) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, (int)block, 0);
-    return (unsigned)(sms > 0 ? sms : 1) * (unsigned)(per_sm > 0 ? per_sm : 1);
-}
-
 }  // namespace
 
-void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
-                              unsigned long long* next, uint32_t* status, cudaStream_t st) {
-    if (!n) return;
-    static const unsigned g = resident_grid(k_intersect_closest_persistent, 256);
-    k_intersect_closest_persistent<<<(unsigned)std::min<uint64_t>(g, grid_for(n, 256)), 256, 0, st>>>(s, rays, n, hits,
-                                                                                                     next, status);
-}
-void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ, uint32_t* status,
-                          cudaStream_t st) {
-    if (!n) return;
-    k_intersect_any<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, occ, status);
-}
-void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n, unsigned long long* counters,
-                            uint32_t* status, cudaStream_t st) {
-    if (!n) return;
-    k_intersect_stats<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, counters, status);
-}
-void launch_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n, int convention,
-                         float* f, float* pdf, cudaStream_t st) {
-    if (!n) return;
-    k_closure_eval<<<grid_for(n, 128), 128, 0, st>>>(lobes, wi, wo, n, convention, f, pdf);
-}
-void launch_closure_sample(const kz_lobe* lobes, const float* wi, const float* u, uint64_t n, float* wo,
-                           float* weight, float* pdf, uint8_t* flags, cudaStream_t st) {
-    if (!n) return;
-    k_closure_sample<<<grid_for(n, 128), 128, 0, st>>>(lobes, wi, u, n, wo, weight, pdf, flags);
-}
 void launch_generate_camera(const DevCamera& cam, const PathParams& pp, PathSoA dst, uint32_t dst_offset,
                             uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st) {
     if (!n_new) return;
@@ -1017,25 +112,6 @@ void launch_generate_rays(const kz_ray* rays, const PathParams& pp, PathSoA dst,
                           uint64_t first_path, uint32_t n_new, uint32_t block, cudaStream_t st) {
     if (!n_new) return;
     k_generate_rays<<<grid_for(n_new, block), block, 0, st>>>(rays, pp, dst, dst_offset, first_path, n_new);
-}
-void launch_trace_paths(const DevScene& s, PathSoA p, uint32_t n, DevCounters* ctr, bool count, uint32_t block,
-                        cudaStream_t st) {
-    if (!n) return;
-    if (count) k_trace_paths<true><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
-    else k_trace_paths<false><<<grid_for(n, block), block, 0, st>>>(s, p, n, ctr, nullptr);
-}
-// The device-driven loop's closest-hit pass: persistent, 256-thread blocks,
-// as many as are resident.
-void launch_trace_paths_dev(const DevScene& s, PathSoA p, uint32_t cap, DevCounters* ctr, bool count, uint32_t,
-                            cudaStream_t st) {
-    if (!cap) return;
-    if (count) {
-        static const unsigned g = resident_grid(k_trace_paths_persistent<true>, 256);
-        k_trace_paths_persistent<true><<<std::min(g, grid_for(cap, 256)), 256, 0, st>>>(s, p, ctr);
-    } else {
-        static const unsigned g = resident_grid(k_trace_paths_persistent<false>, 256);
-        k_trace_paths_persistent<false><<<std::min(g, grid_for(cap, 256)), 256, 0, st>>>(s, p, ctr);
-    }
 }
 void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st) { k_plan<<<1, 1, 0, st>>>(ctr, cap); }
 void launch_finish(DevCounters* ctr, cudaStream_t st) { k_finish<<<1, 1, 0, st>>>(ctr); }
@@ -1053,12 +129,12 @@ void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint3
                       DevCounters* ctr, float* film, double* film64, const GuideShade* gs, uint32_t block,
                       cudaStream_t st) {
     if (!cap) return;
-    if (gs)
-        k_shade<true><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64, *gs,
-                                                              &ctr->n_active);
-    else
-        k_shade<false><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64,
-                                                               GuideShade{}, &ctr->n_active);
+    if (gs) {
+        launch_shade_guided_dev(s, pp, in, cap, out, sq, ctr, film, film64, *gs, block, st);
+        return;
+    }
+    k_shade<false><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64, GuideShade{},
+                                                           &ctr->n_active);
 }
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
                   DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
@@ -1066,82 +142,10 @@ void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t 
     k_shade<false><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
                                                             GuideShade{}, nullptr);
 }
-void launch_shade_guided(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out,
-                         ShadowSoA sq, DevCounters* ctr, float* film, double* film64, const GuideShade& gs,
-                         uint32_t block, cudaStream_t st) {
-    if (!n_in) return;
-    k_shade<true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64, gs, nullptr);
-}
-void launch_trace_shadow_guided(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, float* film,
-                                double* film64, VRec* recs, NRec* nee, uint32_t max_depth, uint32_t block,
-                                cudaStream_t st) {
-    if (!n_max) return;
-    static const unsigned g = resident_grid(k_trace_shadow_persistent<false, true>, 256);
-    k_trace_shadow_persistent<false, true><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
-        s, sq, ctr, film, film64, recs, nee, max_depth);
-}
-void launch_trace_shadow_dev(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count,
-                             float* film, double* film64, cudaStream_t st) {
-    if (!n_max) return;
-    if (count) {
-        static const unsigned g = resident_grid(k_trace_shadow_persistent<true, false>, 256);
-        k_trace_shadow_persistent<true, false><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
-            s, sq, ctr, film, film64, nullptr, nullptr, 0);
-    } else {
-        static const unsigned g = resident_grid(k_trace_shadow_persistent<false, false>, 256);
-        k_trace_shadow_persistent<false, false><<<std::min(g, grid_for(n_max, 256)), 256, 0, st>>>(
-            s, sq, ctr, film, film64, nullptr, nullptr, 0);
-    }
-}
 void launch_guide_collect(const VRec* recs, const NRec* nee, uint64_t n_recs, float4* samples, uint32_t cap,
                           uint32_t* count, float* wsum, cudaStream_t st) {
     if (!n_recs) return;
     k_guide_collect<<<grid_for(2 * n_recs, 256), 256, 0, st>>>(recs, nee, n_recs, samples, cap, count, wsum);
-}
-void launch_trace_shadow(const DevScene& s, ShadowSoA sq, uint32_t n_max, DevCounters* ctr, bool count, float* film,
-                         double* film64, uint32_t block, cudaStream_t st) {
-    if (!n_max) return;
-    if (count)
-        k_trace_shadow<true, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr,
-                                                                              nullptr, 0);
-    else
-        k_trace_shadow<false, false><<<grid_for(n_max, block), block, 0, st>>>(s, sq, ctr, film, film64, nullptr,
-                                                                               nullptr, 0);
-}
-void launch_render_batch(const DevJob* jobs, uint32_t n_jobs, unsigned long long total, BatchCounters* bc,
-                         uint32_t period, uint32_t ctas, uint32_t block, cudaStream_t st) {
-    if (!n_jobs || !total) return;
-    k_render_batch<<<ctas, block, 0, st>>>(jobs, n_jobs, total, bc, period ? period : 1u);
-}
-void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst, DevCounters* ctr, uint32_t cap,
-                               uint32_t block, cudaStream_t st) {
-    if (!cap) return;
-    k_generate_batch_dev<<<grid_for(cap, block), block, 0, st>>>(jobs, n_jobs, dst, ctr);
-}
-static unsigned grid_trace_batch() {
-    static const unsigned g = resident_grid(k_trace_paths_batch, 256);
-    return g;
-}
-static unsigned grid_shadow_batch() {
-    static const unsigned g = resident_grid(k_trace_shadow_batch, 256);
-    return g;
-}
-void prepare_batch_wavefront() {
-    (void)grid_trace_batch();
-    (void)grid_shadow_batch();
-}
-void launch_trace_paths_batch(const DevJob* jobs, PathSoA p, uint32_t cap, DevCounters* ctr, cudaStream_t st) {
-    if (!cap) return;
-    k_trace_paths_batch<<<std::min(grid_trace_batch(), grid_for(cap, 256)), 256, 0, st>>>(jobs, p, ctr);
-}
-void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
-                        uint32_t block, cudaStream_t st) {
-    if (!cap) return;
-    k_shade_batch<<<grid_for(cap, block), block, 0, st>>>(jobs, in, out, sq, ctr);
-}
-void launch_trace_shadow_batch(const DevJob* jobs, ShadowSoA sq, uint32_t cap, DevCounters* ctr, cudaStream_t st) {
-    if (!cap) return;
-    k_trace_shadow_batch<<<std::min(grid_shadow_batch(), grid_for(cap, 256)), 256, 0, st>>>(jobs, sq, ctr);
 }
 void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, cudaStream_t st) {
     if (!n) return;
