@@ -50,9 +50,21 @@ def _newer(target: str, deps: list[str]) -> bool:
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
+def extra_flags() -> list[str]:
+    """Extra nvcc flags from KZ_NVCC_FLAGS (tuning builds, e.g. -DKZ_TRACE_REFILL=12)."""
+    return os.environ.get("KZ_NVCC_FLAGS", "").split()
+
+
 def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = nvcc_path()
+    # a change of the extra flags rebuilds everything
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags_now = " ".join(extra_flags())
+    if not os.path.exists(stamp) or open(stamp).read() != flags_now:
+        force = True
+        with open(stamp, "w") as f:
+            f.write(flags_now)
     hdrs = [os.path.join(CSRC, d) for d in DEPS] + [os.path.join(HERE, "..", "include", "kazen_gb300.h")]
     objs = []
     jobs = []
@@ -62,7 +74,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
         objs.append(obj)
         if not force and _newer(obj, [sp] + hdrs):
             continue
-        cmd = [nvcc, "-c", sp, "-o", obj] + common_flags()
+        cmd = [nvcc, "-c", sp, "-o", obj] + common_flags() + extra_flags()
         if ptxas_verbose and src.endswith(".cu"):
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)

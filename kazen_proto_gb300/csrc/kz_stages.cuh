@@ -500,7 +500,10 @@ static unsigned resident_grid(F f, unsigned block) {
 // gained outweighs a few spills (measured: 5 % faster); the guided variant
 // keeps its registers (at 64 it spills 728 bytes per thread).
 template <bool kGuided>
-__global__ void __launch_bounds__(256, kGuided ? 1 : 4)
+#ifndef KZ_SHADE_MIN_BLOCKS
+#define KZ_SHADE_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
                                                GuideShade gs, const uint32_t* n_dev) {

@@ -395,7 +395,10 @@ __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& ov
 // Every traversal is bounded, so a warp leaves once the queue [0, n) is
 // drained. Refilling only in groups (8 lanes) keeps the set-up code from
 // running for one or two lanes at a time.
-constexpr uint32_t kTraceRefill = 8;
+#ifndef KZ_TRACE_REFILL
+#define KZ_TRACE_REFILL 8
+#endif
+constexpr uint32_t kTraceRefill = KZ_TRACE_REFILL;
 
 template <typename Ctr, typename Start, typename Step>
 __device__ __forceinline__ void persistent_rays(Ctr n, Ctr* next, uint32_t refill, Start start, Step step) {
