@@ -1,7 +1,7 @@
 """The pyzen-compatible layer on the GPU: Renderer(spp, nthreads, callback)
 renders a scene built through the pyzen calls, calls on_tile_end once per
-tile in tile order, and the tiles hold exactly the image the C-ABI render
-of the same description gives; a scene file renders through the same call
+tile in tile order, and the tiles hold the image the C-ABI render of the
+same description gives (up to the order of FP32 film atomics); a scene file renders through the same call
 and the film writes to disk."""
 import os
 
@@ -32,7 +32,9 @@ def test_tiled_render_matches_direct_render(gpu):
     assert [x[0] for x in cb.seen] == list(range(s.film.get_tile_count()))
     assert all(n == t.width * t.height * 3 for (_, _, _, n), t in zip(cb.seen, s.film.tiles))
     direct = api.Renderer(spp=8, max_depth=6, seed=5).render(s._built, s.desc.camera, 64, 48)
-    assert np.array_equal(s.film.image(), direct)
+    # the same paths; only the order of the film's FP32 atomic additions differs
+    img = s.film.image().astype(np.float64)
+    assert float(np.mean((img - direct) ** 2 / (direct.astype(np.float64) ** 2 + 1e-2))) < 1e-10
     assert direct.mean() > 1e-3
     assert s.film.filename == "ignored.png"
 
