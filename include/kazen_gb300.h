@@ -58,13 +58,25 @@ typedef int32_t kz_status;
 
 /* ---- closure ids: the reference ClosureID values (src/shading/bsdf.h:16-75) */
 #define KZ_CLOSURE_DIFFUSE                        0   /* DiffuseID                       */
+#define KZ_CLOSURE_PHONG                          1   /* PhongID                         */
+#define KZ_CLOSURE_WARD                           3   /* WardID                          */
+#define KZ_CLOSURE_REFLECTION                     4   /* ReflectionID (delta)            */
+#define KZ_CLOSURE_REFRACTION                     5   /* RefractionID (delta)            */
+#define KZ_CLOSURE_TRANSPARENT                    6   /* TransparentID (delta)           */
+#define KZ_CLOSURE_TRANSLUCENT                    7   /* TranslucentID                   */
 #define KZ_CLOSURE_EMISSION                       10  /* EmissionID (Le only)            */
 #define KZ_CLOSURE_KP_MIRROR                      14  /* KpMirrorID                      */
 #define KZ_CLOSURE_KP_DIELECTRIC                  15  /* KpDielectricID                  */
+#define KZ_CLOSURE_KP_MICROFACET                  16  /* KpMicrofacetID                  */
 #define KZ_CLOSURE_KP_EMITTER                     17  /* KpEmitterID (Le only)           */
 #define KZ_CLOSURE_KP_GLOSS                       18  /* KpGlossID  (microfacet, refract 0) */
 #define KZ_CLOSURE_KP_GLASS                       19  /* KpGlassID  (microfacet, refract 1/2) */
+#define KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE           20  /* KpPrincipleDiffuseID            */
+#define KZ_CLOSURE_KP_PRINCIPLE_RETRO             21  /* KpPrincipleRetroID              */
+#define KZ_CLOSURE_KP_PRINCIPLE_FAKESS            22  /* KpPrincipleFakeSSID             */
+#define KZ_CLOSURE_KP_PRINCIPLE_SHEEN             23  /* KpPrincipleSheenID              */
 #define KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL     24  /* KpPrincipleSpecularReflectionID */
+#define KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT         26  /* KpPrincipleClearcoatID          */
 /* Not in the reference: GGX conductor with an RGB Schlick F0, built from the
  * reference GGX D/G/VNDF (src/shading/microfacet.h:95-291) and
  * fresnel_schlick(RGB F0) (src/shading/fresnel.h:185-187). */
@@ -84,7 +96,19 @@ typedef int32_t kz_status;
  *   KP_PRINCIPLE_SPECULAR_REFL  [0..2] = F0, [3..5] = N, [6] = xalpha,
  *                      [7] = yalpha, [8] = eta, [9] = metallic
  *   CONDUCTOR_GGX      [0..2] = F0, [3] = xalpha, [4] = yalpha
- *   KP_MIRROR          none
+ *   PHONG              [0..2] = N, [3] = exponent
+ *   WARD               [0..2] = N, [3..5] = T, [6] = xalpha, [7] = yalpha
+ *   REFLECTION         [0..2] = N, [3] = eta
+ *   REFRACTION         [0..2] = N, [3] = eta (inside over outside)
+ *   KP_MICROFACET      [0] = alpha, [1] = int_ior, [2] = ext_ior, [3] = kd
+ *   KP_PRINCIPLE_DIFFUSE  [0..2] = N
+ *   KP_PRINCIPLE_RETRO    [0..2] = N, [3] = roughness
+ *   KP_PRINCIPLE_FAKESS   [0] = roughness
+ *   KP_PRINCIPLE_SHEEN    [0..2] = N, [3] = sheen
+ *   KP_PRINCIPLE_CLEARCOAT [0..2] = N, [3] = roughness (GTR1 alpha, in (0, 1))
+ *   KP_MIRROR, TRANSPARENT, TRANSLUCENT  none
+ * Delta lobes (KP_MIRROR, KP_DIELECTRIC, REFLECTION, REFRACTION,
+ * TRANSPARENT) are sampled only; their eval is zero.
  */
 typedef struct kz_lobe {
     uint32_t closure_id;

@@ -35,6 +35,18 @@ KZ_CLOSURE_KP_GLOSS = 18
 KZ_CLOSURE_KP_GLASS = 19
 KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL = 24
 KZ_CLOSURE_CONDUCTOR_GGX = 64
+KZ_CLOSURE_PHONG = 1
+KZ_CLOSURE_WARD = 3
+KZ_CLOSURE_REFLECTION = 4
+KZ_CLOSURE_REFRACTION = 5
+KZ_CLOSURE_TRANSPARENT = 6
+KZ_CLOSURE_TRANSLUCENT = 7
+KZ_CLOSURE_KP_MICROFACET = 16
+KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE = 20
+KZ_CLOSURE_KP_PRINCIPLE_RETRO = 21
+KZ_CLOSURE_KP_PRINCIPLE_FAKESS = 22
+KZ_CLOSURE_KP_PRINCIPLE_SHEEN = 23
+KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT = 26
 KZ_DIST_GGX = 0
 KZ_DIST_BECKMANN = 1
 KZ_MAX_LOBES = 8

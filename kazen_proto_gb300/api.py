@@ -81,10 +81,76 @@ def conductor_ggx(F0=(0.95, 0.64, 0.54), alpha=0.2, weight=(1.0, 1.0, 1.0)):
     return lobe(N.KZ_CLOSURE_CONDUCTOR_GGX, weight, (F0[0], F0[1], F0[2], alpha, alpha))
 
 
-def principle_specular(F0=(0.04, 0.04, 0.04), alpha=0.2, eta=1.5, metallic=0.0, weight=(1.0, 1.0, 1.0)):
+def principle_specular(F0=(0.04, 0.04, 0.04), alpha=0.2, eta=1.5, metallic=0.0, weight=(1.0, 1.0, 1.0), yalpha=None):
     """`kp_principle_specular_reflection(F0, N, xalpha, yalpha, eta, metallic)` (bsdfs.cpp:688-730)."""
+    ya = alpha if yalpha is None else yalpha
     return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL, weight,
-                (F0[0], F0[1], F0[2], 0, 1, 0, alpha, alpha, eta, metallic))
+                (F0[0], F0[1], F0[2], 0, 1, 0, alpha, ya, eta, metallic))
+
+
+def phong(exponent=20.0, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`phong(N, exponent)` (bsdfs.cpp:43-81)."""
+    return lobe(N.KZ_CLOSURE_PHONG, weight, (*N_local, exponent))
+
+
+def ward(xalpha=0.1, yalpha=None, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0), T_local=(1.0, 0.0, 0.0)):
+    """`ward(N, T, xalpha, yalpha)` (bsdfs.cpp:92-148); anisotropy along the
+    local x (tangent) and z axes."""
+    ya = xalpha if yalpha is None else yalpha
+    return lobe(N.KZ_CLOSURE_WARD, weight, (*N_local, *T_local, xalpha, ya))
+
+
+def reflection(eta=1.5, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`reflection(N, eta)`: a perfect mirror without a Fresnel factor (bsdfs.cpp:150-167)."""
+    return lobe(N.KZ_CLOSURE_REFLECTION, weight, (*N_local, eta))
+
+
+def refraction(eta=1.5, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`refraction(N, eta)`: Snell transmission, eta = inside / outside (bsdfs.cpp:169-203)."""
+    return lobe(N.KZ_CLOSURE_REFRACTION, weight, (*N_local, eta))
+
+
+def transparent(weight=(1.0, 1.0, 1.0)):
+    """`transparent()`: straight through (bsdfs.cpp:205-217)."""
+    return lobe(N.KZ_CLOSURE_TRANSPARENT, weight)
+
+
+def translucent(weight=(1.0, 1.0, 1.0)):
+    """`translucent()`: Lambertian transmission (bsdfs.cpp:219-230)."""
+    return lobe(N.KZ_CLOSURE_TRANSLUCENT, weight)
+
+
+def kp_microfacet(alpha=0.1, int_ior=1.5046, ext_ior=1.000277, kd=0.5, weight=(1.0, 1.0, 1.0)):
+    """`kp_microfacet(alpha, int_ior, ext_ior, kd)`: Beckmann Cook-Torrance over a
+    diffuse base (bsdfs.cpp:300-336)."""
+    return lobe(N.KZ_CLOSURE_KP_MICROFACET, weight, (alpha, int_ior, ext_ior, kd))
+
+
+def principle_diffuse(weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`kp_principle_diffuse(N)` (bsdfs.cpp:563-584)."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE, weight, N_local)
+
+
+def principle_retro(roughness=0.5, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`kp_principle_retro(N, roughness)` (bsdfs.cpp:586-612)."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_RETRO, weight, (*N_local, roughness))
+
+
+def principle_fakess(roughness=0.5, weight=(1.0, 1.0, 1.0)):
+    """`kp_principle_fakess(roughness)` (bsdfs.cpp:614-647)."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_FAKESS, weight, (roughness,))
+
+
+def principle_sheen(sheen=1.0, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`kp_principle_sheen(N)` (bsdfs.cpp:649-673). OSL registers only N for
+    this closure, so the reference's `sheen` field is never written by a
+    shader; lowered shaders carry the sheen amount in the weight and use 1."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_SHEEN, weight, (*N_local, sheen))
+
+
+def principle_clearcoat(roughness=0.1, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0, 0.0)):
+    """`kp_principle_clearcoat(N, roughness)`: GTR1 alpha in (0, 1) (bsdfs.cpp:736-800)."""
+    return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT, weight, (*N_local, roughness))
 
 
 def material(lobes=(), Le=(0.0, 0.0, 0.0)) -> np.ndarray:

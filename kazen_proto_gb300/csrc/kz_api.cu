@@ -112,6 +112,43 @@ kz_status validate_lobe(const kz_lobe& l, uint32_t m, uint32_t k) {
         if (!(l.params[3] > 0.f) || !(l.params[4] > 0.f))
             return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be > 0", m, k);
         return KZ_OK;
+    case KZ_CLOSURE_PHONG:
+        if (!(l.params[3] >= 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: phong exponent must be >= 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_WARD:
+        if (!(l.params[6] > 0.f) || !(l.params[7] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: ward roughness must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_REFRACTION:
+        if (!(l.params[3] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: refraction eta must be > 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_REFLECTION:
+    case KZ_CLOSURE_TRANSPARENT:
+    case KZ_CLOSURE_TRANSLUCENT:
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE:
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN:
+        return KZ_OK;
+    case KZ_CLOSURE_KP_MICROFACET:
+        if (!(l.params[0] > 0.f) || !(l.params[1] > 0.f) || !(l.params[2] > 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: kp_microfacet alpha and iors must be > 0", m, k);
+        if (!(l.params[3] >= 0.f && l.params[3] <= 1.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: kp_microfacet kd must be in [0, 1]", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO:
+        if (!(l.params[3] >= 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be >= 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS:
+        if (!(l.params[0] >= 0.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: roughness must be >= 0", m, k);
+        return KZ_OK;
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT:
+        // GTR1 divides by log(alpha^2): alpha 1 is singular
+        if (!(l.params[3] > 0.f && l.params[3] < 1.f))
+            return fail(KZ_ERR_INVALID_ARG, "material %u lobe %u: clearcoat roughness must be in (0, 1)", m, k);
+        return KZ_OK;
     case KZ_CLOSURE_EMISSION:
     case KZ_CLOSURE_KP_EMITTER:
         return fail(KZ_ERR_INVALID_ARG,

@@ -284,7 +284,70 @@ struct LobeSample {
 };
 
 __device__ __forceinline__ bool lobe_is_delta(uint32_t id) {
-    return id == KZ_CLOSURE_KP_MIRROR || id == KZ_CLOSURE_KP_DIELECTRIC;
+    return id == KZ_CLOSURE_KP_MIRROR || id == KZ_CLOSURE_KP_DIELECTRIC || id == KZ_CLOSURE_REFLECTION ||
+           id == KZ_CLOSURE_REFRACTION || id == KZ_CLOSURE_TRANSPARENT;
+}
+
+// ------------------------------------------------------------------ helpers of the further lobes
+__device__ __forceinline__ float pow5(float x) {
+    const float x2 = x * x;
+    return x2 * x2 * x;
+}
+// Cosine-weighted direction about +y (Malley's method: a uniform disk
+// point lifted onto the hemisphere); pdf y / pi.
+__device__ __forceinline__ f3 cosine_hemisphere(float u0, float u1) {
+    float r = sqrtf(u0);
+    float sp, cp;
+    sincosf(2.f * kPi * u1, &sp, &cp);
+    float x = r * cp, z = r * sp;
+    float y = sqrtf(fmaxf(0.f, 1.f - x * x - z * z));
+    return mk(x, y, z);
+}
+// Orthonormal basis (b1, b2) completing the unit vector n: Duff et al.,
+// "Building an Orthonormal Basis, Revisited", JCGT 6(1), 2017.
+__device__ __forceinline__ void onb(f3 n, f3& b1, f3& b2) {
+    const float sign = n.z >= 0.f ? 1.f : -1.f;
+    const float a = -1.f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    b1 = mk(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    b2 = mk(b, sign + n.y * n.y * a, -n.y);
+}
+// Beckmann slope pdf D(m) cos(theta_m) (BeckmannPDF, src/shading/microfacet.cpp:10-23)
+__device__ __forceinline__ float beckmann_pdf_m(f3 m, float alpha) {
+    const float c = m.y;
+    if (c <= 0.f) return 0.f;
+    const float a2 = alpha * alpha;
+    const float s2 = 1.f - c * c;
+    const float t = s2 < 0.f ? 0.f : sqrtf(s2) / c;
+    return kInvPi * (expf(-(t * t) / a2) / (a2 * (c * c * c)));
+}
+// Walter et al. 2007 rational fit of the Beckmann Smith G1 (G1,
+// src/shading/microfacet.cpp:25-38)
+__device__ __forceinline__ float beckmann_g1_walter(f3 m, f3 v, float alpha) {
+    if (dot(v, m) / v.y <= 0.f) return 0.f;
+    const float s2 = 1.f - v.y * v.y;
+    const float t = s2 < 0.f ? 0.f : sqrtf(s2) / v.y;
+    const float b = 1.f / (alpha * t);
+    if (b >= 1.6f) return 1.f;
+    const float b2 = b * b;
+    return (3.535f * b + 2.181f * b2) / (1.f + 2.276f * b + 2.577f * b2);
+}
+// Ward exponent -tan^2(theta_m) (cos^2 phi_m / ax^2 + sin^2 phi_m / ay^2),
+// written without dividing by sin(theta_m).
+__device__ __forceinline__ float ward_exponent(f3 m, float ax, float ay) {
+    return -(sq(m.x / ax) + sq(m.z / ay)) / sq(m.y);
+}
+// Clearcoat GGX Smith G1 with the fixed alpha 0.25 (Disney 2012)
+__device__ __forceinline__ float clearcoat_g1(float c) {
+    const float t2 = (1.f - c * c) / (c * c);
+    return 2.f / (1.f + sqrtf(1.f + 0.0625f * t2));
+}
+// GTR1 (Berry) normal distribution, alpha in (0, 1), at the unit half
+// vector m; 1 + (a2 - 1) cos^2 is formed as a2 cos^2 + sin^2 so that a small
+// alpha near the peak does not cancel.
+__device__ __forceinline__ float gtr1_D(float alpha, f3 m) {
+    const float a2 = alpha * alpha;
+    return (a2 - 1.f) / (kPi * logf(a2) * (a2 * m.y * m.y + (m.x * m.x + m.z * m.z)));
 }
 
 __device__ __forceinline__ Mdf lobe_mdf(const kz_lobe& l, f3 wi, float& eta) {
@@ -401,21 +464,131 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         r.pdf = mdf.pdf(m);
         return r;
     }
-    default:  // KpMirror, KpDielectric (delta: eval 0, pdf 0) and Le-only ids
+    case KZ_CLOSURE_PHONG: {  // Phong::eval, bsdfs.cpp:43-59 (returns the sample weight)
+        const f3 N = mk(l.params[0], l.params[1], l.params[2]);
+        const float e = l.params[3];
+        const float cni = wo.y, cno = dot(N, wi);
+        if (cni > 0.f && cno > 0.f) {
+            const f3 R = (2.f * cno) * N - wi;
+            const float cri = dot(R, wo);
+            if (cri > 0.f) {
+                r.pdf = (e + 1.f) * (0.5f * kInvPi) * powf(cri, e);
+                const float v = cni * (e + 2.f) / (e + 1.f);
+                r.f = mk(v, v, v);
+            }
+        }
+        return r;
+    }
+    case KZ_CLOSURE_WARD: {  // Ward::eval, bsdfs.cpp:92-112
+        const float ax = l.params[6], ay = l.params[7];
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return r;
+        const f3 m = normalize(wi + wo);
+        const float sv = sqrtf(fmaxf(0.f, 1.f - ci * ci));
+        // stretched_roughness (microfacet.h:60-73) takes sin(theta) of wi here
+        const float A = ax == ay ? 1.f / sq(ax) : sq(m.x / (sv * ax)) + sq(m.z / (sv * ay));
+        const float t2 = fmaxf(0.f, 1.f - m.y * m.y) / (m.y * m.y);
+        const float tmp = expf(-t2 * A) / (4.f * kPi * ax * ay);
+        r.pdf = fmaxf(tmp / (dot(m, wi) * (m.y * m.y * m.y)), 0.f);
+        const float v = tmp / sqrtf(ci * co);
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_TRANSPARENT:  // Transparent::eval, bsdfs.cpp:205-209
+        r.f = mk(1.f, 1.f, 1.f);
+        r.pdf = 1.f;
+        return r;
+    case KZ_CLOSURE_TRANSLUCENT: {  // Translucent::eval, bsdfs.cpp:219-223
+        r.pdf = fmaxf(wo.y, 0.f) * kInvPi;
+        r.f = mk(kInvPi, kInvPi, kInvPi);
+        return r;
+    }
+    case KZ_CLOSURE_KP_MICROFACET: {  // KpMicrofacet::eval, bsdfs.cpp:300-319
+        const float alpha = l.params[0], kd = l.params[3];
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return r;
+        const f3 wh = normalize(wi + wo);
+        const float D = beckmann_pdf_m(wh, alpha);
+        const float F = fresnel_ext_int(dot(wh, wi), l.params[2], l.params[1]);
+        const float G = beckmann_g1_walter(wh, wi, alpha) * beckmann_g1_walter(wh, wo, alpha);
+        const float ks = 1.f - kd;
+        const float Jh = 1.f / (4.f * dot(wh, wo));
+        r.pdf = ks * D * Jh + kd * co * kInvPi;
+        const float v = kInvPi + ks * D * F * G / (4.f * ci * co * wh.y);
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE: {  // bsdfs.cpp:563-576: only the view factor survives
+        const float ci = wi.y, co = wo.y;
+        if (co <= 0.f || ci <= 0.f) return r;
+        r.pdf = co * kInvPi;
+        const float v = kInvPi * (1.f - 0.5f * pow5(1.f - ci));
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO: {  // bsdfs.cpp:586-605
+        const float ci = wi.y, co = wo.y;
+        if (co <= 0.f || ci <= 0.f) return r;
+        r.pdf = co * kInvPi;
+        const float FL = pow5(1.f - co), FV = pow5(1.f - ci);
+        const f3 wh = normalize(wi + wo);
+        const float RR = 2.f * l.params[3] * sq(dot(wo, wh));
+        const float v = kInvPi * RR * (FL + FV + FL * FV * (RR - 1.f));
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {  // bsdfs.cpp:614-640 (no hemisphere test)
+        const f3 wh = normalize(wi + wo);
+        const float fss90 = sq(dot(wh, wo)) * l.params[0];
+        const float aci = fabsf(wi.y), aco = fabsf(wo.y);
+        const float fi = pow5(1.f - aci), fo = pow5(1.f - aco);
+        const float fss = (1.f + fi * (fss90 - 1.f)) * (1.f + fo * (fss90 - 1.f));
+        const float ss = 1.25f * (fss * (1.f / (aci + aco) - 0.5f) + 0.5f);
+        r.pdf = fmaxf(wo.y, 0.f) * kInvPi;
+        const float v = ss * kInvPi;
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN: {  // bsdfs.cpp:649-666
+        const float ci = wi.y, co = wo.y;
+        if (co <= 0.f || ci <= 0.f) return r;
+        r.pdf = co * kInvPi;
+        const f3 wh = normalize(wi + wo);
+        const float cv = dot(wh, wo);
+        const float v = cv < 1e-6f ? l.params[3] : l.params[3] * pow5(1.f - cv);
+        r.f = mk(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {  // bsdfs.cpp:736-780: D takes cos, G1 takes tan
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return r;
+        const f3 wh = normalize(wi + wo);
+        const float ch = wh.y;
+        const float a2 = sq(l.params[3]);
+        const float D = (a2 - 1.f) / (kPi * logf(a2) * (1.f + (a2 - 1.f) * ch));
+        const float ti = sqrtf(fmaxf(0.f, 1.f - ci * ci)) / ci, to = sqrtf(fmaxf(0.f, 1.f - co * co)) / co;
+        const float G = (2.f / (1.f + sqrtf(1.f + 0.0625f * ti))) * (2.f / (1.f + sqrtf(1.f + 0.0625f * to)));
+        const float F = 0.04f + 0.96f * pow5(1.f - ci);
+        r.pdf = fmaxf(0.f, D * ch / (4.f * dot(wo, wh)));
+        const float v = fminf(fmaxf(D * G * F * 0.25f, 0.f), 0.25f);
+        r.f = mk(v, v, v);
+        return r;
+    }
+    default:  // KpMirror, KpDielectric, Reflection, Refraction (delta: eval 0, pdf 0) and Le-only ids
         return r;
     }
 }
 
 // f*|cos(wo)| and the solid-angle pdf of wo under the lobe's own sampler.
 __device__ inline LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
-    LobeEval r = lobe_eval_reference(l, wi, wo);
+    LobeEval z{mk(0.f, 0.f, 0.f), 0.f};
     switch (l.closure_id) {
     case KZ_CLOSURE_DIFFUSE:
-        return r;
+        return lobe_eval_reference(l, wi, wo);
     case KZ_CLOSURE_KP_GLOSS:
     case KZ_CLOSURE_CONDUCTOR_GGX:
     case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL: {
-        LobeEval z{mk(0.f, 0.f, 0.f), 0.f};
+        LobeEval r = lobe_eval_reference(l, wi, wo);
         if (r.pdf == 0.f || wi.y <= 0.f || wo.y <= 0.f) return z;
         f3 m = normalize(wi + wo);
         float wom = fabsf(dot(wo, m));
@@ -425,8 +598,9 @@ __device__ inline LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
         return r;
     }
     case KZ_CLOSURE_KP_GLASS: {
+        LobeEval r = lobe_eval_reference(l, wi, wo);
         float eta = l.params[9];
-        if (eta == 1.f) return LobeEval{mk(0.f, 0.f, 0.f), 0.f};
+        if (eta == 1.f) return z;
         if (wi.y < 0) eta = 1.f / eta;
         f3 m;
         bool refl = wi.y * wo.y >= 0.f;
@@ -441,21 +615,92 @@ __device__ inline LobeEval lobe_eval(const kz_lobe& l, f3 wi, f3 wo) {
         r.f = r.f * fabsf(wo.y);
         return r;
     }
-    default:
-        return LobeEval{mk(0.f, 0.f, 0.f), 0.f};
+    case KZ_CLOSURE_PHONG: {  // modified Phong, f = (e+2)/(2 pi) cos_r^e, sampled about R
+        const f3 N = mk(l.params[0], l.params[1], l.params[2]);
+        const float e = l.params[3];
+        const float cno = dot(N, wi), cni = dot(N, wo);
+        if (cno <= 0.f || cni <= 0.f) return z;
+        const float cri = dot((2.f * cno) * N - wi, wo);
+        if (cri <= 0.f) return z;
+        const float lobe = powf(cri, e) * (0.5f * kInvPi);
+        const float v = (e + 2.f) * lobe * cni;
+        return LobeEval{mk(v, v, v), (e + 1.f) * lobe};
+    }
+    case KZ_CLOSURE_WARD: {  // Walter, "Notes on the Ward BRDF" (2005), eqs. 3 and 9
+        const float ax = l.params[6], ay = l.params[7];
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return z;
+        const f3 m = normalize(wi + wo);
+        const float k = expf(ward_exponent(m, ax, ay)) / (4.f * kPi * ax * ay);
+        const float v = k * co / sqrtf(ci * co);
+        return LobeEval{mk(v, v, v), k / (dot(m, wi) * (m.y * m.y * m.y))};
+    }
+    case KZ_CLOSURE_TRANSLUCENT: {  // Lambertian transmission: wo on the far side of wi
+        if (wi.y * wo.y >= 0.f) return z;
+        const float v = fabsf(wo.y) * kInvPi;
+        return LobeEval{mk(v, v, v), v};
+    }
+    case KZ_CLOSURE_KP_MICROFACET: {  // Cook-Torrance (Beckmann) + kd/pi, sampled by ks : kd
+        const float alpha = l.params[0], kd = l.params[3];
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return z;
+        const f3 wh = normalize(wi + wo);
+        const float D = beckmann_pdf_m(wh, alpha);
+        const float F = fresnel_ext_int(dot(wh, wi), l.params[2], l.params[1]);
+        const float G = beckmann_g1_walter(wh, wi, alpha) * beckmann_g1_walter(wh, wo, alpha);
+        const float ks = 1.f - kd;
+        const float v = (kd * kInvPi + ks * D * F * G / (4.f * ci * co * wh.y)) * co;
+        return LobeEval{mk(v, v, v), ks * D / (4.f * dot(wh, wo)) + kd * co * kInvPi};
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE: {  // Burley 2015: (1 - F_L / 2)(1 - F_V / 2) / pi
+        const float ci = wi.y, co = wo.y;
+        if (co <= 0.f || ci <= 0.f) return z;
+        const float v = kInvPi * (1.f - 0.5f * pow5(1.f - co)) * (1.f - 0.5f * pow5(1.f - ci)) * co;
+        return LobeEval{mk(v, v, v), co * kInvPi};
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO:
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN: {  // reference f times cos, cosine-sampled
+        if (wi.y <= 0.f || wo.y <= 0.f) return z;
+        LobeEval r = lobe_eval_reference(l, wi, wo);
+        r.f = r.f * wo.y;
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {  // reflection only
+        if (wi.y <= 0.f || wo.y <= 0.f) return z;
+        LobeEval r = lobe_eval_reference(l, wi, wo);
+        r.f = r.f * wo.y;
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {  // Disney 2012 clearcoat: GTR1, Smith G (alpha 0.25), F0 0.04
+        const float ci = wi.y, co = wo.y;
+        if (ci <= 0.f || co <= 0.f) return z;
+        const f3 wh = normalize(wi + wo);
+        const float cd = dot(wo, wh);
+        if (cd <= 0.f) return z;
+        const float D = gtr1_D(l.params[3], wh);
+        const float F = 0.04f + 0.96f * pow5(1.f - cd);
+        const float v = 0.25f * D * F * clearcoat_g1(ci) * clearcoat_g1(co) / (4.f * ci);
+        return LobeEval{mk(v, v, v), D * wh.y / (4.f * cd)};
+    }
+    default:  // delta lobes and Le-only ids
+        return z;
     }
 }
 
 __device__ inline LobeSample lobe_sample(const kz_lobe& l, f3 wi, float u0, float u1, float u2) {
     LobeSample s{mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f), 0.f, false, false};
     switch (l.closure_id) {
-    case KZ_CLOSURE_DIFFUSE: {
-        float r = sqrtf(u0);
-        float sp, cp;
-        sincosf(2.f * kPi * u1, &sp, &cp);
-        float x = r * cp, z = r * sp;
-        float y = sqrtf(fmaxf(0.f, 1.f - x * x - z * z));
-        s.wo = mk(x, y, z);
+    case KZ_CLOSURE_DIFFUSE:
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE:
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO:
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS:
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN:
+    case KZ_CLOSURE_TRANSLUCENT: {
+        s.wo = cosine_hemisphere(u0, u1);
+        if (l.closure_id == KZ_CLOSURE_TRANSLUCENT) {
+            if (wi.y == 0.f) return s;
+            if (wi.y > 0.f) s.wo.y = -s.wo.y;
+        }
         LobeEval e = lobe_eval(l, wi, s.wo);
         if (e.pdf <= 0.f) return s;
         s.pdf = e.pdf;
@@ -486,6 +731,91 @@ __device__ inline LobeSample lobe_sample(const kz_lobe& l, f3 wi, float u0, floa
         }
         s.weight = mk(1.f, 1.f, 1.f);
         s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_REFLECTION:  // Reflection::sample, bsdfs.cpp:150-167 (no Fresnel factor)
+        if (wi.y <= 0.f) return s;
+        s.wo = reflect_n(wi, mk(0.f, 1.f, 0.f));
+        s.weight = mk(1.f, 1.f, 1.f);
+        s.valid = s.delta = true;
+        return s;
+    case KZ_CLOSURE_REFRACTION: {  // Snell transmission through the surface, eta = inside / outside
+        f3 n = mk(0.f, 1.f, 0.f);
+        float fac = l.params[3];
+        if (wi.y < 0.f) {
+            fac = 1.f / fac;
+            n = -n;
+        }
+        s.wo = refract_u(-wi, n, fac);
+        if (is_zero(s.wo)) return s;
+        s.weight = mk(1.f, 1.f, 1.f);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_TRANSPARENT:  // Transparent::sample, bsdfs.cpp:211-217: straight through
+        s.wo = -wi;
+        s.weight = mk(1.f, 1.f, 1.f);
+        s.valid = s.delta = true;
+        return s;
+    case KZ_CLOSURE_PHONG:
+    case KZ_CLOSURE_WARD:
+    case KZ_CLOSURE_KP_MICROFACET:
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {
+        if (wi.y <= 0.f) return s;
+        if (l.closure_id == KZ_CLOSURE_PHONG) {
+            // cos^e lobe about the mirror direction R
+            const f3 N = mk(l.params[0], l.params[1], l.params[2]);
+            const float cno = dot(N, wi);
+            if (cno <= 0.f) return s;
+            const f3 R = (2.f * cno) * N - wi;
+            f3 b1, b2;
+            onb(R, b1, b2);
+            const float ct = powf(u1, 1.f / (l.params[3] + 1.f));
+            const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+            float sp, cp;
+            sincosf(2.f * kPi * u0, &sp, &cp);
+            s.wo = b1 * (st * cp) + b2 * (st * sp) + R * ct;
+        } else {
+            f3 m;
+            if (l.closure_id == KZ_CLOSURE_WARD) {
+                // Walter's notes eqs. 6-7: phi from the stretched angle, quadrant kept
+                const float ax = l.params[6], ay = l.params[7];
+                float sp, cp;
+                sincosf(2.f * kPi * u0, &sp, &cp);
+                const float px = ax * cp, pz = ay * sp;
+                const float inv = 1.f / sqrtf(px * px + pz * pz);
+                const float cphi = px * inv, sphi = pz * inv;
+                const float A = sq(cphi / ax) + sq(sphi / ay);
+                const float t = sqrtf(-logf(1.f - u1) / A);
+                const float ct = 1.f / sqrtf(1.f + t * t);
+                m = mk(t * ct * cphi, ct, t * ct * sphi);
+            } else if (l.closure_id == KZ_CLOSURE_KP_MICROFACET) {
+                if (u2 >= 1.f - l.params[3]) {  // diffuse part, probability kd
+                    s.wo = cosine_hemisphere(u0, u1);
+                    m = mk(0.f, 0.f, 0.f);
+                } else {  // Beckmann normal, BeckmannMDF (microfacet.cpp:3-8)
+                    const float t = sqrtf(-sq(l.params[0]) * logf(1.f - u1));
+                    const float ct = 1.f / sqrtf(1.f + t * t);
+                    float sp, cp;
+                    sincosf(2.f * kPi * u0, &sp, &cp);
+                    m = mk(t * ct * cp, ct, t * ct * sp);
+                }
+            } else {  // GTR1 half vector, Burley 2012 appendix B
+                const float a2 = sq(l.params[3]);
+                const float ct = sqrtf(fmaxf(0.f, (1.f - powf(a2, 1.f - u1)) / (1.f - a2)));
+                const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+                float sp, cp;
+                sincosf(2.f * kPi * u0, &sp, &cp);
+                m = mk(st * cp, ct, st * sp);
+            }
+            if (!is_zero(m)) s.wo = reflect_n(wi, m);
+        }
+        if (s.wo.y <= 0.f) return s;
+        LobeEval e = lobe_eval(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
         return s;
     }
     case KZ_CLOSURE_KP_GLOSS:

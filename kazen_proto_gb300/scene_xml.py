@@ -13,11 +13,11 @@ the GPU path renders:
   camera makes them);
 * <Materials> of <ShaderGroupBegin name> / <Shader name layer> /
   <Parameter ...> / <ShaderGroupEnd>: each group's shader is lowered from
-  its OSL source (name.osl next to the scene file) by reading the
-  `Ci = ...` statement: a sum of terms, each a product of numbers and shader
-  parameters times one closure among diffuse(N), kp_mirror(),
-  kp_dielectric(int_ior, ext_ior), microfacet(dist, N, alpha, eta, refract),
-  kp_emitter(a) and emission() (the last two add their weight to Le);
+  its OSL source (name.osl next to the scene file) by evaluating its body
+  over constant inputs (kazen_proto_gb300.osl_lower): the closures the
+  reference registers (diffuse, ward, reflection, refraction, microfacet,
+  kp_mirror, kp_dielectric, kp_microfacet, the kp_principle_* family) become
+  lobes; kp_emitter and emission add their weight to Le;
 * <Objects>: <Mesh filename shader_name [is_light] [translate] [rotate]
   [scale]> from OBJ files (positions and faces; polygons fan-triangulated,
   negative indices resolved), <Triangle verta vertb vertc>, <Quad center dir
@@ -43,7 +43,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import api
+from . import api, osl_lower
 from .scenes import SceneDesc, icosphere
 
 
@@ -143,91 +143,13 @@ def apply_transform(M, v):
 
 
 # ---------------------------------------------------------------- OSL lowering
-_DECL = re.compile(r"\b(color|float|int|normal|vector|point)\s+(\w+)\s*=\s*([-+0-9.eE]+)")
-_CLOSURE = re.compile(r"^(\w+)\s*\((.*)\)$")
-
-
-def _osl_source_params(src: str):
-    """Parameter defaults declared in the shader's signature."""
-    head = src.split("{", 1)[0]
-    out = {}
-    for kind, name, val in _DECL.findall(head):
-        v = float(val)
-        out[name] = np.array([v, v, v]) if kind == "color" else v
-    return out
-
-
-def _ci_expression(src: str) -> str:
-    body = "\n".join(l.split("//", 1)[0] for l in src.split("{", 1)[1].splitlines())
-    m = re.search(r"\bCi\s*=\s*([^;]+);", body)
-    if not m:
-        raise ValueError("no `Ci = ...;` statement")
-    return " ".join(m.group(1).split())
-
-
-def _split_top(expr: str, sep: str):
-    out, depth, cur = [], 0, ""
-    for ch in expr:
-        if ch == "(":
-            depth += 1
-        elif ch == ")":
-            depth -= 1
-        if ch == sep and depth == 0:
-            out.append(cur.strip())
-            cur = ""
-        else:
-            cur += ch
-    out.append(cur.strip())
-    return out
-
-
-def lower_shader(src: str, params: dict):
-    """kz_material record of a surface shader: OSL source + group parameters."""
-    env = _osl_source_params(src)
-    env.update(params)
-
-    def value(tok: str):
-        tok = tok.strip()
-        if tok.startswith('"'):
-            return tok.strip('"')
-        if tok == "N":
-            return None
-        try:
-            return float(tok)
-        except ValueError:
-            pass
-        if tok not in env:
-            raise ValueError(f"unknown parameter {tok!r}")
-        return env[tok]
-
-    lobes, Le = [], np.zeros(3)
-    for term in _split_top(_ci_expression(src), "+"):
-        weight = np.ones(3)
-        closure = None
-        for fac in _split_top(term, "*"):
-            m = _CLOSURE.match(fac)
-            if m and m.group(1) not in ("color",):
-                closure = (m.group(1), [value(a) for a in _split_top(m.group(2), ",")] if m.group(2).strip() else [])
-            else:
-                weight = weight * np.asarray(value(fac), np.float64)
-        if closure is None:
-            raise ValueError(f"term without a closure: {term!r}")
-        name, args = closure
-        w = tuple(float(x) for x in weight)
-        if name == "diffuse":
-            lobes.append(api.diffuse(w))
-        elif name == "kp_mirror":
-            lobes.append(api.mirror(w))
-        elif name == "kp_dielectric":
-            lobes.append(api.dielectric(float(args[0]), float(args[1]), w))
-        elif name == "microfacet":
-            dist, _, alpha, eta, refract = args[:5]
-            lobes.append(api.microfacet(dist, float(alpha), eta=float(eta), refract=int(refract), weight=w))
-        elif name in ("kp_emitter", "emission"):
-            Le = Le + weight
-        else:
-            raise ValueError(f"closure {name!r} is not lowered")
-    return api.material(lobes, Le=tuple(float(x) for x in Le))
+def lower_shader(src: str, params: dict, warnings: list | None = None):
+    """kz_material record of a surface shader: OSL source + group parameters
+    (evaluated by osl_lower over constant inputs)."""
+    r = osl_lower.lower(src, params)
+    if warnings is not None:
+        warnings.extend(r.warnings)
+    return api.material(r.lobes, Le=tuple(float(x) for x in r.Le))
 
 
 # ---------------------------------------------------------------- scene
@@ -303,7 +225,9 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
         sname, params = shaders[0]
         osl = os.path.join(base, sname + ".osl")
         with open(osl) as f:
-            d.materials.append(lower_shader(f.read(), params))
+            w = []
+            d.materials.append(lower_shader(f.read(), params, w))
+        out.warnings.extend(f"shader group {name!r}: {x}" for x in w)
         out.material_names.append(name)
     mat_id = {n: i for i, n in enumerate(out.material_names)}
 

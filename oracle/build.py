@@ -20,7 +20,7 @@ def build(force: bool = False) -> str:
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR)):
         return LIB
     tmp = LIB + ".tmp"
-    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC", "-pthread",
+    cmd = ["g++", "-O3", "-std=c++20", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC", "-pthread",
            SRC, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

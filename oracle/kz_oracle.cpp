@@ -20,7 +20,8 @@
 // Reference files restated (paths within kazen_proto):
 //   ray epsilon ............ src/core/ray.h:10-45, src/base/basic_types.h:9
 //   shading frame .......... src/base/utils.h:83-210
-//   closures ............... src/shading/bsdfs.cpp:27-41, 254-298, 359-554, 688-730
+//   closures ............... src/shading/bsdfs.cpp:27-223, 254-319, 359-554, 563-780
+//                            src/shading/microfacet.cpp:3-38 (Beckmann pdf, Walter G1)
 //   glass helpers .......... src/shading/bsdfs.h:541-599
 //   microfacet ............. src/shading/microfacet.h:60-291
 //   fresnel ................ src/shading/fresnel.h:12-187, src/base/utils.h:153-177
@@ -660,7 +661,57 @@ struct LobeEval {
     float pdf;  // pdf (convention dependent)
 };
 
-bool lobe_is_delta(uint32_t id) { return id == KZ_CLOSURE_KP_MIRROR || id == KZ_CLOSURE_KP_DIELECTRIC; }
+bool lobe_is_delta(uint32_t id) {
+    switch (id) {
+    case KZ_CLOSURE_KP_MIRROR: case KZ_CLOSURE_KP_DIELECTRIC: case KZ_CLOSURE_REFLECTION:
+    case KZ_CLOSURE_REFRACTION: case KZ_CLOSURE_TRANSPARENT:
+        return true;
+    default:
+        return false;
+    }
+}
+
+// ---- helpers of the further closures (src/shading/microfacet.cpp:3-38,
+// src/base/utils.h:83-125, src/shading/bsdfs.cpp:706-733)
+float tan_theta_ref(V3 w) {
+    float tmp = 1 - w.y * w.y;
+    if (tmp < 0.f) return 0.f;
+    return std::sqrt(tmp) / w.y;
+}
+float tan2_theta_ref(V3 w) { return std::max(0.f, 1.f - w.y * w.y) / (w.y * w.y); }
+// BeckmannPDF: D(m) cos(theta_m)
+float beckmann_pdf_ref(V3 m, float alpha) {
+    float c = m.y;
+    if (c <= 0.) return 0.f;
+    float a2 = alpha * alpha;
+    float t = tan_theta_ref(m);
+    double lon = std::exp((-t * t) / a2) / (a2 * std::pow(c, 3));
+    return (float)(kInvPi * lon);
+}
+// G1 of Walter et al. 2007 (rational fit)
+float walter_g1_ref(V3 wh, V3 wv, float alpha) {
+    if (dot(wv, wh) / wv.y <= 0.f) return 0.f;
+    double b = 1. / (alpha * tan_theta_ref(wv));
+    if (b >= 1.6f) return 1.f;
+    double b2 = b * b;
+    return (float)((3.535 * b + 2.181 * b2) / (1. + 2.276 * b + 2.577 * b2));
+}
+float gtr1_ref(float alpha, float c) {
+    float a2 = alpha * alpha;
+    return (float)((a2 - 1.) / (kPi * std::log(a2) * (1. + (a2 - 1.) * c)));
+}
+float clearcoat_g1_ref(float c) {
+    double s = std::sqrt(std::max(0., 1. - (double)(c * c)));
+    double t = s / c;
+    return (float)(2. / (1. + std::sqrt(1. + 0.0625 * t)));
+}
+float schlick5(float c) { return (float)std::pow(1. - c, 5.); }
+V3 cosine_dir(float u0, float u1) {
+    float r = std::sqrt(u0);
+    float phi = 2.f * kPi * u1;
+    float x = r * std::cos(phi), z = r * std::sin(phi);
+    return V3(x, std::sqrt(std::max(0.f, 1.f - x * x - z * z)), z);
+}
 
 Mdf make_mdf(const kz_lobe& l, V3 wi, int& dist, float& eta) {
     Mdf m;
@@ -780,6 +831,114 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         r.pdf = mdf.pdf(m);
         return r;
     }
+    case KZ_CLOSURE_PHONG: {  // bsdfs.cpp:43-59
+        V3 N(l.params[0], l.params[1], l.params[2]);
+        float ex = l.params[3];
+        float cos_ni = wo.y;
+        float cos_no = dot(N, wi);
+        if (cos_ni > 0 && cos_no > 0) {
+            V3 R = (2 * cos_no) * N - wi;
+            float cos_ri = dot(R, wo);
+            if (cos_ri > 0) {
+                r.pdf = (ex + 1) * (1.f / (2.f * kPi)) * std::pow(cos_ri, ex);
+                float v = cos_ni * (ex + 2) / (ex + 1);
+                r.f = V3(v, v, v);
+            }
+        }
+        return r;
+    }
+    case KZ_CLOSURE_WARD: {  // bsdfs.cpp:92-112
+        float ax = l.params[6], ay = l.params[7];
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return r;
+        V3 m = normalize(wi + wo);
+        float sin_v = std::sqrt(std::max(0.f, 1.f - ci * ci));
+        float A = stretched_roughness(m, sin_v, ax, ay);
+        float tmp = std::exp(-tan2_theta_ref(m) * A) / (4.f * kPi * ax * ay);
+        r.pdf = (float)std::max(tmp / (dot(m, wi) * std::pow(m.y, 3)), 0.);
+        float v = tmp / std::sqrt(ci * co);
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_TRANSPARENT:  // bsdfs.cpp:205-209
+        r.f = V3(1, 1, 1);
+        r.pdf = 1.f;
+        return r;
+    case KZ_CLOSURE_TRANSLUCENT:  // bsdfs.cpp:219-223
+        r.pdf = std::max(wo.y, 0.f) * kInvPi;
+        r.f = V3(kInvPi, kInvPi, kInvPi);
+        return r;
+    case KZ_CLOSURE_KP_MICROFACET: {  // bsdfs.cpp:300-319
+        float alpha = l.params[0], int_ior = l.params[1], ext_ior = l.params[2], kd = l.params[3];
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return r;
+        V3 wh = normalize(wi + wo);
+        float D = beckmann_pdf_ref(wh, alpha);
+        float F = fresnel_utils(dot(wh, wi), ext_ior, int_ior);
+        float G = walter_g1_ref(wh, wi, alpha) * walter_g1_ref(wh, wo, alpha);
+        double ks = 1. - kd;
+        double Jh = 1. / (4. * dot(wh, wo));
+        r.pdf = (float)(ks * D * Jh + kd * co * kInvPi);
+        float v = (float)(kInvPi + ks * D * F * G / (4. * ci * co * wh.y));
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE: {  // bsdfs.cpp:563-576
+        float ci = wi.y, co = wo.y;
+        if (co <= 0 || ci <= 0) return r;
+        r.pdf = std::max(co, 0.f) * kInvPi;
+        float v = (float)(kInvPi * (1.f - 0.5f * std::pow(1 - ci, 5)));
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO: {  // bsdfs.cpp:586-605
+        float ci = wi.y, co = wo.y;
+        if (co <= 0 || ci <= 0) return r;
+        r.pdf = std::max(co, 0.f) * kInvPi;
+        double FL = std::pow(1. - co, 5.), FV = std::pow(1. - ci, 5.);
+        V3 wh = normalize(wi + wo);
+        float d = dot(wo, wh);
+        float RR = 2.f * l.params[3] * (d * d);
+        float v = (float)(kInvPi * RR * (FL + FV + FL * FV * (RR - 1.)));
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {  // bsdfs.cpp:614-640
+        V3 wh = normalize(wi + wo);
+        float ch = dot(wh, wo);
+        float fss90 = ch * ch * l.params[0];
+        float aco = std::fabs(wo.y), aci = std::fabs(wi.y);
+        float fi = schlick5(aci), fo = schlick5(aco);
+        float fss = std::lerp(1.f, fss90, fi) * std::lerp(1.f, fss90, fo);
+        double ss = 1.25f * (fss * (1. / (aci + aco) - .5f) + .5f);
+        r.pdf = std::max(wo.y, 0.f) * kInvPi;
+        float v = (float)(ss * kInvPi);
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN: {  // bsdfs.cpp:649-666
+        float ci = wi.y, co = wo.y;
+        if (co <= 0 || ci <= 0) return r;
+        r.pdf = std::max(co, 0.f) * kInvPi;
+        V3 wh = normalize(wi + wo);
+        float cv = dot(wh, wo);
+        float v = cv < 1e-6 ? l.params[3] : (float)(l.params[3] * std::pow(1. - cv, 5.));
+        r.f = V3(v, v, v);
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {  // bsdfs.cpp:736-780
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return r;
+        V3 wh = normalize(wi + wo);
+        float ch = wh.y;
+        float D = gtr1_ref(l.params[3], ch);
+        float G = clearcoat_g1_ref(ci) * clearcoat_g1_ref(co);
+        double F = 0.04 + 0.96 * std::pow(1. - ci, 5.);
+        r.pdf = (float)std::max(0., D * ch / (4. * dot(wo, wh)));
+        float v = (float)std::clamp(D * G * F * 0.25, 0., 0.25);
+        r.f = V3(v, v, v);
+        return r;
+    }
     default:
         return r;
     }
@@ -821,6 +980,75 @@ LobeEval eval_integrator(const kz_lobe& l, V3 wi, V3 wo) {
         r.f = r.f * std::fabs(wo.y);
         return r;
     }
+    case KZ_CLOSURE_PHONG: {
+        // modified Phong: f = (e+2)/(2 pi) cos_r^e; pdf (e+1)/(2 pi) cos_r^e
+        V3 N(l.params[0], l.params[1], l.params[2]);
+        float ex = l.params[3];
+        float cos_no = dot(N, wi), cos_ni = dot(N, wo);
+        if (cos_no <= 0 || cos_ni <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        float cos_ri = dot((2 * cos_no) * N - wi, wo);
+        if (cos_ri <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        float lobe = std::pow(cos_ri, ex) / (2.f * kPi);
+        float v = (ex + 2) * lobe * cos_ni;
+        return LobeEval{V3(v, v, v), (ex + 1) * lobe};
+    }
+    case KZ_CLOSURE_WARD: {
+        // Walter, "Notes on the Ward BRDF": the exponent uses phi of m
+        float ax = l.params[6], ay = l.params[7];
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        V3 m = normalize(wi + wo);
+        float ex = -((m.x / ax) * (m.x / ax) + (m.z / ay) * (m.z / ay)) / (m.y * m.y);
+        float k = std::exp(ex) / (4.f * kPi * ax * ay);
+        float v = k / std::sqrt(ci * co) * co;
+        return LobeEval{V3(v, v, v), k / (dot(m, wi) * m.y * m.y * m.y)};
+    }
+    case KZ_CLOSURE_TRANSLUCENT: {
+        if (wi.y * wo.y >= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        float v = std::fabs(wo.y) * kInvPi;
+        return LobeEval{V3(v, v, v), v};
+    }
+    case KZ_CLOSURE_KP_MICROFACET: {
+        // Nori's microfacet: kd / pi + ks D F G / (4 ci co cos_h)
+        float alpha = l.params[0], kd = l.params[3];
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        V3 wh = normalize(wi + wo);
+        float D = beckmann_pdf_ref(wh, alpha);
+        float F = fresnel_utils(dot(wh, wi), l.params[2], l.params[1]);
+        float G = walter_g1_ref(wh, wi, alpha) * walter_g1_ref(wh, wo, alpha);
+        float ks = 1.f - kd;
+        float v = (kd * kInvPi + ks * D * F * G / (4.f * ci * co * wh.y)) * co;
+        return LobeEval{V3(v, v, v), ks * D / (4.f * dot(wh, wo)) + kd * co * kInvPi};
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE: {
+        float ci = wi.y, co = wo.y;
+        if (co <= 0 || ci <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        float v = kInvPi * (1.f - 0.5f * schlick5(co)) * (1.f - 0.5f * schlick5(ci)) * co;
+        return LobeEval{V3(v, v, v), co * kInvPi};
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO:
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN:
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {
+        if (wi.y <= 0 || wo.y <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        r.f = r.f * wo.y;
+        return r;
+    }
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {
+        // Burley 2012 clearcoat: GTR1(cos^2), Smith GGX G1 (alpha 0.25, tan^2), F0 0.04 at cos_d
+        float ci = wi.y, co = wo.y;
+        if (ci <= 0 || co <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        V3 wh = normalize(wi + wo);
+        float cd = dot(wo, wh);
+        if (cd <= 0) return LobeEval{V3(0, 0, 0), 0.f};
+        float a2 = l.params[3] * l.params[3];
+        // 1 + (a2 - 1) cos^2 = a2 cos^2 + sin^2, without cancellation at small alpha
+        float D = (a2 - 1.f) / (kPi * std::log(a2) * (a2 * wh.y * wh.y + (wh.x * wh.x + wh.z * wh.z)));
+        auto g1 = [](float c) { return 2.f / (1.f + std::sqrt(1.f + 0.0625f * ((1.f - c * c) / (c * c)))); };
+        float F = 0.04f + 0.96f * schlick5(cd);
+        float v = 0.25f * D * F * g1(ci) * g1(co) / (4.f * ci);
+        return LobeEval{V3(v, v, v), D * wh.y / (4.f * cd)};
+    }
     default:
         return LobeEval{V3(0, 0, 0), 0.f};
     }
@@ -836,13 +1064,19 @@ struct LobeSample {
 LobeSample sample_lobe(const kz_lobe& l, V3 wi, float u0, float u1, float u2) {
     LobeSample s{V3(0, 0, 0), V3(0, 0, 0), 0.f, false, false};
     switch (l.closure_id) {
-    case KZ_CLOSURE_DIFFUSE: {
-        // cosine-weighted hemisphere about +y (the pdf the reference declares)
-        float r = std::sqrt(u0);
-        float phi = 2.f * kPi * u1;
-        float x = r * std::cos(phi), z = r * std::sin(phi);
-        float y = std::sqrt(std::max(0.f, 1.f - x * x - z * z));
-        s.wo = V3(x, y, z);
+    case KZ_CLOSURE_DIFFUSE:
+    case KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE:
+    case KZ_CLOSURE_KP_PRINCIPLE_RETRO:
+    case KZ_CLOSURE_KP_PRINCIPLE_FAKESS:
+    case KZ_CLOSURE_KP_PRINCIPLE_SHEEN:
+    case KZ_CLOSURE_TRANSLUCENT: {
+        // cosine-weighted hemisphere about +y (the pdf the reference declares);
+        // the translucent lobe mirrors it to the side away from wi
+        s.wo = cosine_dir(u0, u1);
+        if (l.closure_id == KZ_CLOSURE_TRANSLUCENT) {
+            if (wi.y == 0.f) return s;
+            if (wi.y > 0.f) s.wo.y = -s.wo.y;
+        }
         LobeEval e = eval_integrator(l, wi, s.wo);
         if (e.pdf <= 0.f) return s;
         s.pdf = e.pdf;
@@ -874,6 +1108,97 @@ LobeSample sample_lobe(const kz_lobe& l, V3 wi, float u0, float u1, float u2) {
         }
         s.weight = V3(1, 1, 1);
         s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_REFLECTION: {  // bsdfs.cpp:150-167
+        if (wi.y <= 0.f) return s;
+        s.wo = reflect_n(wi, V3(0, 1, 0));
+        s.weight = V3(1, 1, 1);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_REFRACTION: {
+        // Snell transmission, eta = inside / outside (the OSL refraction()
+        // convention); bsdfs.cpp:178-203 refracts with the normal on wi's side
+        V3 n(0, 1, 0);
+        float fac = l.params[3];
+        if (wi.y < 0.f) {
+            fac = 1.f / fac;
+            n = -n;
+        }
+        s.wo = refract_u(-wi, n, fac);
+        if (is_zero(s.wo)) return s;
+        s.weight = V3(1, 1, 1);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_TRANSPARENT: {  // bsdfs.cpp:211-217
+        s.wo = -wi;
+        s.weight = V3(1, 1, 1);
+        s.valid = s.delta = true;
+        return s;
+    }
+    case KZ_CLOSURE_PHONG: {
+        if (wi.y <= 0.f) return s;
+        V3 N(l.params[0], l.params[1], l.params[2]);
+        float cos_no = dot(N, wi);
+        if (cos_no <= 0.f) return s;
+        V3 R = (2 * cos_no) * N - wi;
+        // frame about R (Duff et al. 2017)
+        float sg = R.z >= 0.f ? 1.f : -1.f;
+        float a = -1.f / (sg + R.z);
+        float b = R.x * R.y * a;
+        V3 t1(1.f + sg * R.x * R.x * a, sg * b, -sg * R.x);
+        V3 t2(b, sg + R.y * R.y * a, -R.y);
+        float ct = std::pow(u1, 1.f / (l.params[3] + 1.f));
+        float st = std::sqrt(std::max(0.f, 1.f - ct * ct));
+        float phi = 2.f * kPi * u0;
+        s.wo = t1 * (st * std::cos(phi)) + t2 * (st * std::sin(phi)) + R * ct;
+        if (s.wo.y <= 0.f) return s;
+        LobeEval e = eval_integrator(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
+        return s;
+    }
+    case KZ_CLOSURE_WARD:
+    case KZ_CLOSURE_KP_MICROFACET:
+    case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {
+        if (wi.y <= 0.f) return s;
+        V3 m(0, 0, 0);
+        if (l.closure_id == KZ_CLOSURE_WARD) {
+            // Walter's notes eqs. 6-7 with the quadrant of 2 pi u0 kept
+            float ax = l.params[6], ay = l.params[7];
+            float px = ax * std::cos(2.f * kPi * u0), pz = ay * std::sin(2.f * kPi * u0);
+            float len = std::sqrt(px * px + pz * pz);
+            float cphi = px / len, sphi = pz / len;
+            float A = (cphi / ax) * (cphi / ax) + (sphi / ay) * (sphi / ay);
+            float theta = std::atan(std::sqrt(-std::log(1.f - u1) / A));
+            m = V3(std::sin(theta) * cphi, std::cos(theta), std::sin(theta) * sphi);
+        } else if (l.closure_id == KZ_CLOSURE_KP_MICROFACET) {
+            if (u2 >= 1.f - l.params[3]) {
+                s.wo = cosine_dir(u0, u1);
+            } else {
+                float theta = std::atan(std::sqrt(-l.params[0] * l.params[0] * std::log(1.f - u1)));
+                float phi = 2.f * kPi * u0;
+                m = V3(std::sin(theta) * std::cos(phi), std::cos(theta), std::sin(theta) * std::sin(phi));
+            }
+        } else {
+            // GTR1 half vector (Burley 2012, appendix B)
+            float a2 = l.params[3] * l.params[3];
+            float ct = std::sqrt(std::max(0.f, (1.f - std::pow(a2, 1.f - u1)) / (1.f - a2)));
+            float st = std::sqrt(std::max(0.f, 1.f - ct * ct));
+            float phi = 2.f * kPi * u0;
+            m = V3(st * std::cos(phi), ct, st * std::sin(phi));
+        }
+        if (!is_zero(m)) s.wo = reflect_n(wi, m);
+        if (s.wo.y <= 0.f) return s;
+        LobeEval e = eval_integrator(l, wi, s.wo);
+        if (e.pdf <= 0.f) return s;
+        s.pdf = e.pdf;
+        s.weight = e.f * (1.f / e.pdf);
+        s.valid = true;
         return s;
     }
     case KZ_CLOSURE_KP_GLOSS:

@@ -17,11 +17,14 @@ RTOL = 1e-5
 ATOL = 1e-7
 
 
+N_KINDS = 21
+
+
 def lobe_grid(rng, n):
     """Random lobes of every supported closure with random parameters."""
     out = []
     for k in range(n):
-        kind = k % 9
+        kind = k % N_KINDS
         a = float(rng.uniform(0.02, 1.0))
         b = float(rng.uniform(0.02, 1.0))
         eta = float(rng.uniform(0.3, 2.5))
@@ -41,8 +44,35 @@ def lobe_grid(rng, n):
             out.append(api.microfacet("beckmann", a, a, eta, 2))
         elif kind == 7:
             out.append(api.conductor_ggx(tuple(rng.uniform(0.0, 1.0, 3)), a))
-        else:
+        elif kind == 8:
             out.append(api.principle_specular(tuple(rng.uniform(0.0, 1.0, 3)), a, eta, float(rng.uniform())))
+        elif kind == 9:
+            out.append(api.phong(float(rng.uniform(0.5, 100.0))))
+        elif kind == 10:
+            out.append(api.ward(a, a))
+        elif kind == 11:
+            out.append(api.ward(a, b))
+        elif kind == 12:
+            out.append(api.reflection(eta))
+        elif kind == 13:
+            out.append(api.refraction(eta))
+        elif kind == 14:
+            out.append(api.transparent())
+        elif kind == 15:
+            out.append(api.translucent())
+        elif kind == 16:
+            out.append(api.kp_microfacet(a, float(rng.uniform(1.1, 2.0)), float(rng.uniform(1.0, 1.1)),
+                                         float(rng.uniform())))
+        elif kind == 17:
+            out.append(api.principle_diffuse())
+        elif kind == 18:
+            out.append(api.principle_retro(float(rng.uniform())))
+        elif kind == 19:
+            out.append(api.principle_fakess(float(rng.uniform())) if k % 2 else api.principle_sheen(float(rng.uniform())))
+        else:
+            # GTR1 at alpha -> 0 is a spike whose value at the peak turns on the
+            # last bit of cos(theta_h); the grid stays at alpha >= 0.05
+            out.append(api.principle_clearcoat(float(rng.uniform(0.05, 0.9))))
     return np.array(out, dtype=N.LOBE_DTYPE)
 
 

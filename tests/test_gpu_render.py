@@ -108,6 +108,56 @@ def test_mixture_and_delta_materials(gpu, oracle_mod):
     assert rel_mse(img, ref) <= REL_MSE_TOL
 
 
+def test_further_closures_render(gpu, oracle_mod):
+    """Phong, Ward, KpMicrofacet, the principled lobes (diffuse, retro,
+    fake subsurface, sheen, clearcoat), translucent, reflection, refraction
+    and transparent materials in one scene, against the restatement."""
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    d.materials[0] = api.material([api.principle_diffuse((0.5, 0.06, 0.05)), api.principle_retro(0.6, (0.5, 0.06, 0.05)),
+                                   api.principle_sheen(1.0, (0.2, 0.2, 0.2))])
+    d.materials[1] = api.material([api.principle_fakess(0.4, (0.1, 0.4, 0.08)),
+                                   api.principle_clearcoat(0.2, (0.8, 0.8, 0.8))])
+    d.materials[2] = api.material([api.ward(0.1, 0.35, (0.4, 0.4, 0.38)), api.phong(30.0, (0.2, 0.2, 0.2))])
+    d.materials[3] = api.material([api.kp_microfacet(0.25, 1.5, 1.0, 0.5, (0.8, 0.6, 0.3))])
+    extra = [api.material([api.reflection(1.5, (0.9, 0.9, 0.9))]),
+             api.material([api.refraction(1.5)]),
+             api.material([api.transparent((0.5, 0.5, 0.5)), api.translucent((0.4, 0.4, 0.4))])]
+    boxes = [((0.1, 0.0, 0.1), (0.25, 0.15, 0.25)), ((0.6, 0.35, 0.3), (0.75, 0.5, 0.45)),
+             ((0.3, 0.65, 0.4), (0.45, 0.8, 0.55))]
+    for m, (lo, hi) in zip(extra, boxes):
+        d.materials.append(m)
+        v, i = scenes.box(lo, hi)
+        d.add(v, i, len(d.materials) - 1)
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=6, seed=5).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=5)
+    assert np.isfinite(img).all() and img.mean() > 0
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+
+
+def test_reference_shader_library_render(gpu, oracle_mod):
+    """The reference's own principle.osl, disney_brdf.osl and ward.osl, as
+    lowered at their defaults (tests/golden/reference_shaders_lowered.json),
+    on the walls and boxes of the box scene, against the restatement."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_shaders_lowered.json")) as f:
+        g = json.load(f)
+
+    def mat(key):
+        return api.material([api.lobe(l["closure_id"], l["weight"], l["params"]) for l in g[key]["lobes"]])
+
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    d.materials[0] = mat("resource/shader/src/principle.osl")
+    d.materials[1] = mat("resource/shader/src/ward.osl")
+    d.materials[3] = mat("resource/shader/src/disney_brdf.osl")
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=6, seed=6).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=6)
+    assert np.isfinite(img).all() and img.mean() > 0
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+
+
 def test_terrain_scene_small(gpu, oracle_mod):
     d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
     s = d.build()

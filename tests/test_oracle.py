@@ -88,12 +88,27 @@ def _grid_dirs(rng, n, upper=True):
     return d.astype(np.float32)
 
 
+FURTHER_LOBES = [
+    (lambda: api.phong(20.0), "phong"),
+    (lambda: api.ward(0.2), "ward_iso"),
+    (lambda: api.ward(0.1, 0.4), "ward_aniso"),
+    (lambda: api.translucent(), "translucent"),
+    (lambda: api.kp_microfacet(0.3, 1.5, 1.0, 0.4), "kp_microfacet"),
+    (lambda: api.principle_diffuse(), "principle_diffuse"),
+    (lambda: api.principle_retro(0.7), "principle_retro"),
+    (lambda: api.principle_fakess(0.5), "principle_fakess"),
+    (lambda: api.principle_sheen(1.0), "principle_sheen"),
+    (lambda: api.principle_clearcoat(0.3), "principle_clearcoat"),
+]
+
+
 @pytest.mark.parametrize("lobe_fn", [
     lambda: api.diffuse((1, 1, 1)),
     lambda: api.conductor_ggx((1, 1, 1), 0.3),
     lambda: api.microfacet("ggx", 0.4, eta=1.0 / 1.5),
     lambda: api.microfacet("beckmann", 0.4, eta=1.0 / 1.5),
-], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"])
+] + [f for f, _ in FURTHER_LOBES], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"]
+    + [i for _, i in FURTHER_LOBES])
 def test_sampling_matches_pdf(oracle_mod, lobe_fn):
     """E[f*cos/pdf] by sampling equals the quadrature of f*cos (importance
     sampling is consistent with the pdf the integrator divides by)."""
@@ -106,9 +121,10 @@ def test_sampling_matches_pdf(oracle_mod, lobe_fn):
     est = np.where((fl & 1)[:, None] > 0, w, 0).mean(0)
     # quadrature of f*cos over the hemisphere (uniform directions / (1/2pi))
     m = 400000
-    d = _grid_dirs(rng, m)
+    # the whole sphere: the translucent lobe transmits
+    d = _grid_dirs(rng, m, upper=False)
     f, _ = oracle_mod.closure_eval(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), d, 1)
-    quad = f.mean(0) * 2 * math.pi
+    quad = f.mean(0) * 4 * math.pi
     assert np.allclose(est, quad, rtol=0.03, atol=2e-3), (est, quad)
 
 
@@ -117,7 +133,8 @@ def test_sampling_matches_pdf(oracle_mod, lobe_fn):
     lambda: api.conductor_ggx((1, 1, 1), 0.3),
     lambda: api.microfacet("ggx", 0.25, eta=1.0 / 1.5),
     lambda: api.microfacet("beckmann", 0.25, eta=1.0 / 1.5),
-], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"])
+] + [f for f, _ in FURTHER_LOBES], ids=["diffuse", "conductor_ggx", "gloss_ggx", "gloss_beckmann"]
+    + [i for _, i in FURTHER_LOBES])
 def test_integrator_pdf_normalised(oracle_mod, lobe_fn):
     """The solid-angle pdf integrates, over the directions the sampler can
     return, to the fraction of samples that are valid (microfacet samples that
@@ -125,14 +142,15 @@ def test_integrator_pdf_normalised(oracle_mod, lobe_fn):
     rng = np.random.default_rng(6)
     wi = np.array([[math.sin(0.9), math.cos(0.9), 0.0]], np.float32)
     m = 600000
-    d = _grid_dirs(rng, m)
+    d = _grid_dirs(rng, m, upper=False)
     _, pdf = oracle_mod.closure_eval(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), d, 1)
-    integral = pdf.mean() * 2 * math.pi
+    integral = pdf.mean() * 4 * math.pi
     u = rng.random((m, 3), dtype=np.float32)
     _, _, _, fl = oracle_mod.closure_sample(np.repeat(lobe_fn()[None], m), np.repeat(wi, m, 0), u)
     valid = (fl & 1).mean()
     assert abs(integral - valid) < 0.02, (integral, valid)
-    assert valid > 0.85
+    # GTR1's long tail sends a third of the clearcoat half vectors below the horizon at this angle
+    assert valid > 0.6
 
 
 def test_dielectric_energy_and_reciprocal_fresnel(oracle_mod):
