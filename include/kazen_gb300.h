@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define KZ_ABI_VERSION 2
+#define KZ_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 typedef int32_t kz_status;
@@ -109,7 +109,12 @@ typedef int32_t kz_status;
  *   KP_MIRROR, TRANSPARENT, TRANSLUCENT  none
  * Delta lobes (KP_MIRROR, KP_DIELECTRIC, REFLECTION, REFRACTION,
  * TRANSPARENT) are sampled only; their eval is zero.
+ * params[KZ_LOBE_TEXTURE_PARAM] (the last slot, used by no lobe) is a texture
+ * reference: 0 = none, k = the weight is multiplied by texture k-1 of the
+ * scene (kz_scene_set_textures) at the hit's uv. All textured lobes of one
+ * material name the same texture.
  */
+#define KZ_LOBE_TEXTURE_PARAM 11
 typedef struct kz_lobe {
     uint32_t closure_id;
     float    weight[3];
@@ -208,6 +213,20 @@ typedef struct kz_scene_info {
 
 typedef struct kz_scene kz_scene;
 
+/* Texture for lobe weights and the environment, the GPU form of the OSL
+ * lookups the reference's shaders make (texture(filename, u, v),
+ * environment(filename, I); OIIO, src/shading/renderservices.cpp) and of the
+ * OSL checkerboard shader network (resource/scene/textured_cornell_box). */
+#define KZ_TEX_CHECKER 0  /* Ca where int(fmod(s*scale_s, 2)) ^ int(fmod(t*scale_t, 2)) == 0, else Cb */
+#define KZ_TEX_IMAGE   1  /* RGB float image, bilinear, periodic wrap; t = 0 at row 0 (the top) */
+typedef struct kz_texture {
+    int32_t      kind;
+    uint32_t     width, height;   /* IMAGE */
+    const float* rgb;             /* IMAGE: width*height*3 floats, host memory, row-major from the top */
+    float        scale_s, scale_t;  /* CHECKER */
+    float        Ca[3], Cb[3];      /* CHECKER */
+} kz_texture;
+
 /* ---- library --------------------------------------------------------- */
 int32_t     kz_abi_version(void);
 const char* kz_last_error_string(void);
@@ -228,7 +247,20 @@ kz_status kz_scene_add_mesh(kz_scene* scene, const float* xyz, uint32_t nverts,
                             int32_t is_light, int32_t* out_geom_id);
 kz_status kz_scene_set_materials(kz_scene* scene, const kz_material* materials,
                                  uint32_t n_materials);
-/* Builds the BVH and uploads geometry, materials and the light table. */
+/* Textures referenced by lobes and the environment; copied (images too).
+ * Replaces the set. Call before kz_scene_build. */
+kz_status kz_scene_set_textures(kz_scene* scene, const kz_texture* textures, uint32_t n_textures);
+/* Per-vertex texture coordinates (nverts*2 floats, host) of a mesh added
+ * with kz_scene_add_mesh. A mesh without them has uv = the barycentrics of
+ * vertices 1 and 2, as the reference's meshes without texcoords do
+ * (TriangleMesh::post_hit, src/core/shape.cpp:615-683). */
+kz_status kz_scene_set_mesh_uvs(kz_scene* scene, int32_t geom_id, const float* uv, uint32_t nverts);
+/* Radiance of a ray that leaves the scene (the background shader of
+ * PathIntegrator::Li, src/core/integrator.cpp:381-388, 545-552): rgb times
+ * texture `texture` (-1: none) looked up in latitude-longitude form,
+ * s = 0.5 + atan2(d.x, -d.z) / (2 pi), t = acos(d.y) / pi. Default black. */
+kz_status kz_scene_set_environment(kz_scene* scene, const float rgb[3], int32_t texture);
+/* Builds the BVH and uploads geometry, materials, textures and the light table. */
 kz_status kz_scene_build(kz_scene* scene);
 kz_status kz_scene_get_info(kz_scene* scene, kz_scene_info* out_info);
 /* Use an external cudaStream_t (NULL = the library-created stream). */

@@ -58,6 +58,16 @@ class KzLobe(C.Structure):
     _fields_ = [("closure_id", C.c_uint32), ("weight", C.c_float * 3), ("params", C.c_float * 12)]
 
 
+KZ_TEX_CHECKER = 0
+KZ_TEX_IMAGE = 1
+KZ_LOBE_TEXTURE_PARAM = 11
+
+
+class KzTexture(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.c_void_p),
+                ("scale_s", C.c_float), ("scale_t", C.c_float), ("Ca", C.c_float * 3), ("Cb", C.c_float * 3)]
+
+
 class KzMaterial(C.Structure):
     _fields_ = [("Le", C.c_float * 3), ("n_lobes", C.c_uint32), ("lobes", KzLobe * KZ_MAX_LOBES)]
 
@@ -155,6 +165,9 @@ SIGNATURES = {
     "kz_scene_add_mesh": (C.c_int32, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_int32)]),
     "kz_scene_set_materials": (C.c_int32, [_P, _P, C.c_uint32]),
+    "kz_scene_set_textures": (C.c_int32, [_P, _P, C.c_uint32]),
+    "kz_scene_set_mesh_uvs": (C.c_int32, [_P, C.c_int32, _P, C.c_uint32]),
+    "kz_scene_set_environment": (C.c_int32, [_P, _P, C.c_int32]),
     "kz_scene_build": (C.c_int32, [_P]),
     "kz_scene_get_info": (C.c_int32, [_P, C.POINTER(KzSceneInfo)]),
     "kz_scene_set_stream": (C.c_int32, [_P, _P]),

@@ -153,6 +153,50 @@ def principle_clearcoat(roughness=0.1, weight=(1.0, 1.0, 1.0), N_local=(0.0, 1.0
     return lobe(N.KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT, weight, (*N_local, roughness))
 
 
+@dataclass
+class Texture:
+    """A lobe-weight or environment texture (kz_texture): the OSL checkerboard
+    shader's pattern, or an (H, W, 3) float image (row 0 at t = 0)."""
+    kind: int = N.KZ_TEX_CHECKER
+    image: np.ndarray = None
+    scale_s: float = 4.0
+    scale_t: float = 4.0
+    Ca: tuple = (1.0, 1.0, 1.0)
+    Cb: tuple = (0.0, 0.0, 0.0)
+
+    def to_c(self):
+        t = N.KzTexture()
+        t.kind = self.kind
+        keep = None
+        if self.kind == N.KZ_TEX_IMAGE:
+            keep = np.ascontiguousarray(self.image, np.float32)
+            if keep.ndim != 3 or keep.shape[2] != 3:
+                raise ValueError(f"image texture must be (H, W, 3), got {keep.shape}")
+            t.height, t.width = keep.shape[0], keep.shape[1]
+            t.rgb = keep.ctypes.data_as(C.c_void_p)
+        t.scale_s, t.scale_t = self.scale_s, self.scale_t
+        t.Ca[:] = [float(x) for x in self.Ca]
+        t.Cb[:] = [float(x) for x in self.Cb]
+        return t, keep
+
+
+def checker_texture(scale_s=4.0, scale_t=4.0, Ca=(1.0, 1.0, 1.0), Cb=(0.0, 0.0, 0.0)) -> Texture:
+    """The OSL checkerboard shader (resource/scene/textured_cornell_box/checkerboard.osl)."""
+    return Texture(N.KZ_TEX_CHECKER, None, scale_s, scale_t, tuple(Ca), tuple(Cb))
+
+
+def image_texture(rgb) -> Texture:
+    """An (H, W, 3) float image, bilinear with periodic wrap (OSL texture(filename, s, t))."""
+    return Texture(N.KZ_TEX_IMAGE, np.ascontiguousarray(rgb, np.float32))
+
+
+def textured(lobe_rec, texture_index: int) -> np.ndarray:
+    """The lobe with its weight multiplied by texture `texture_index` of the scene."""
+    rec = np.array(lobe_rec, dtype=N.LOBE_DTYPE)
+    rec["params"][N.KZ_LOBE_TEXTURE_PARAM] = texture_index + 1
+    return rec
+
+
 def material(lobes=(), Le=(0.0, 0.0, 0.0)) -> np.ndarray:
     """A lowered surface shader: Le plus up to 8 lobes (ShadingResult, bsdf.h:217-229).
     An emitter shader `Cs * kp_emitter(a)` lowers to Le = Cs with no lobe."""
@@ -259,6 +303,22 @@ class Scene:
         m = np.ascontiguousarray(np.asarray(materials, dtype=N.MATERIAL_DTYPE).reshape(-1))
         self._materials = m
         check(lib().kz_scene_set_materials(self._h, _ptr(m), len(m)))
+
+    def set_textures(self, textures) -> None:
+        """Textures that lobes (params[11] = index + 1) and the environment reference."""
+        recs = [t.to_c() for t in textures]
+        arr = (N.KzTexture * max(1, len(recs)))(*[r for r, _ in recs])
+        check(lib().kz_scene_set_textures(self._h, C.cast(arr, C.c_void_p), len(recs)))
+
+    def set_mesh_uvs(self, geom_id: int, uv) -> None:
+        """Per-vertex texture coordinates (nverts, 2) of a mesh."""
+        a = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        check(lib().kz_scene_set_mesh_uvs(self._h, int(geom_id), _ptr(a), len(a)))
+
+    def set_environment(self, rgb=(0.0, 0.0, 0.0), texture: int = -1) -> None:
+        """Radiance of rays that leave the scene: rgb times a lat-long texture (-1: none)."""
+        a = np.ascontiguousarray(rgb, np.float32).reshape(3)
+        check(lib().kz_scene_set_environment(self._h, _ptr(a), int(texture)))
 
     def build_bvh(self) -> None:
         """Scene::build_bvh / Accelerator::build (accel.h:22-32)."""

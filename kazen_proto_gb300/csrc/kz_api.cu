@@ -75,6 +75,7 @@ struct DevBuf {
 
 struct HostMesh {
     std::vector<float> verts;  // world space, nverts * 3
+    std::vector<float> uv;     // nverts * 2 texture coordinates, or empty
     std::vector<uint32_t> idx;
     int32_t material;
     int32_t is_light;
@@ -172,6 +173,12 @@ struct kz_scene {
 
     // device scene
     DevBuf nodes, tris, geom_offset, geom_light, mats, lights, light_cdf, light_tris;
+    // textures and environment
+    std::vector<kz::DevTexture> textures;  // offsets into tex_texels
+    std::vector<float> tex_texels;
+    float env_rgb[3] = {0.f, 0.f, 0.f};
+    int32_t env_tex = -1;
+    DevBuf d_tri_uv, d_mat_tex, d_textures, d_texels;
     kz::DevScene dev;
     DevBuf status;        // uint32 device status word for batch calls
     uint32_t* status_host = nullptr;  // pinned
@@ -508,6 +515,73 @@ kz_status kz_scene_set_materials(kz_scene* s, const kz_material* materials, uint
     return KZ_OK;
 }
 
+kz_status kz_scene_set_textures(kz_scene* s, const kz_texture* tex, uint32_t n) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    if (n && !tex) return fail(KZ_ERR_INVALID_ARG, "textures is NULL");
+    std::vector<kz::DevTexture> out(n);
+    std::vector<float> texels;
+    for (uint32_t k = 0; k < n; ++k) {
+        const kz_texture& t = tex[k];
+        kz::DevTexture& d = out[k];
+        d.kind = t.kind;
+        if (t.kind == KZ_TEX_CHECKER) {
+            if (!std::isfinite(t.scale_s) || !std::isfinite(t.scale_t) || !finite3(t.Ca) || !finite3(t.Cb))
+                return fail(KZ_ERR_INVALID_ARG, "texture %u: checker parameters must be finite", k);
+            d.scale_s = t.scale_s;
+            d.scale_t = t.scale_t;
+            for (int c = 0; c < 3; ++c) {
+                d.Ca[c] = t.Ca[c];
+                d.Cb[c] = t.Cb[c];
+            }
+        } else if (t.kind == KZ_TEX_IMAGE) {
+            if (!t.rgb || t.width == 0 || t.height == 0 || t.width > (1u << 16) || t.height > (1u << 16))
+                return fail(KZ_ERR_INVALID_ARG, "texture %u: image needs pixels and 1..65536 columns and rows", k);
+            const size_t nf = (size_t)t.width * t.height * 3;
+            for (size_t i = 0; i < nf; ++i)
+                if (!std::isfinite(t.rgb[i])) return fail(KZ_ERR_INVALID_ARG, "texture %u: texel %zu is not finite", k, i / 3);
+            d.w = t.width;
+            d.h = t.height;
+            d.offset = texels.size();
+            texels.insert(texels.end(), t.rgb, t.rgb + nf);
+        } else {
+            return fail(KZ_ERR_INVALID_ARG, "texture %u: unknown kind %d", k, t.kind);
+        }
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->textures = std::move(out);
+    s->tex_texels = std::move(texels);
+    s->built = false;
+    return KZ_OK;
+}
+
+kz_status kz_scene_set_mesh_uvs(kz_scene* s, int32_t geom_id, const float* uv, uint32_t nverts) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (geom_id < 0 || (size_t)geom_id >= s->meshes.size())
+        return fail(KZ_ERR_INVALID_ARG, "geom_id %d is not a mesh of this scene", geom_id);
+    HostMesh& m = s->meshes[(size_t)geom_id];
+    if ((size_t)nverts * 3 != m.verts.size())
+        return fail(KZ_ERR_INVALID_ARG, "mesh %d has %zu vertices, got %u uvs", geom_id, m.verts.size() / 3, nverts);
+    if (nverts && !uv) return fail(KZ_ERR_INVALID_ARG, "uv is NULL");
+    for (size_t i = 0; i < (size_t)nverts * 2; ++i)
+        if (!std::isfinite(uv[i])) return fail(KZ_ERR_INVALID_ARG, "uv %zu is not finite", i / 2);
+    m.uv.assign(uv, uv + (size_t)nverts * 2);
+    s->built = false;
+    return KZ_OK;
+}
+
+kz_status kz_scene_set_environment(kz_scene* s, const float rgb[3], int32_t texture) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    if (!rgb || !finite3(rgb) || rgb[0] < 0.f || rgb[1] < 0.f || rgb[2] < 0.f)
+        return fail(KZ_ERR_INVALID_ARG, "environment radiance must be finite and >= 0");
+    if (texture < -1) return fail(KZ_ERR_INVALID_ARG, "environment texture must be -1 or a texture index");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (int c = 0; c < 3; ++c) s->env_rgb[c] = rgb[c];
+    s->env_tex = texture;
+    s->built = false;
+    return KZ_OK;
+}
+
 kz_status kz_scene_build(kz_scene* s) {
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -516,6 +590,28 @@ kz_status kz_scene_build(kz_scene* s) {
         if ((size_t)s->meshes[g].material >= s->materials.size())
             return fail(KZ_ERR_INVALID_ARG, "mesh %zu uses material %d but only %zu are set", g,
                         s->meshes[g].material, s->materials.size());
+    // texture references: params[KZ_LOBE_TEXTURE_PARAM] = texture + 1, one texture per material
+    const uint32_t ntex = (uint32_t)s->textures.size();
+    std::vector<int32_t> mat_tex(s->materials.size(), -1);
+    bool any_tex = false;
+    for (size_t m = 0; m < s->materials.size(); ++m) {
+        const kz_material& mt = s->materials[m];
+        for (uint32_t k = 0; k < mt.n_lobes; ++k) {
+            const float r = mt.lobes[k].params[KZ_LOBE_TEXTURE_PARAM];
+            if (r == 0.f) continue;
+            if (!(r >= 1.f && r <= (float)ntex && r == std::floor(r)))
+                return fail(KZ_ERR_INVALID_ARG, "material %zu lobe %u: texture reference %g with %u textures set", m,
+                            k, (double)r, ntex);
+            const int32_t t = (int32_t)r - 1;
+            if (mat_tex[m] >= 0 && mat_tex[m] != t)
+                return fail(KZ_ERR_INVALID_ARG, "material %zu: lobes reference textures %d and %d (one per material)",
+                            m, mat_tex[m], t);
+            mat_tex[m] = t;
+            any_tex = true;
+        }
+    }
+    if (s->env_tex >= (int32_t)ntex)
+        return fail(KZ_ERR_INVALID_ARG, "environment texture %d with %u textures set", s->env_tex, ntex);
     KZ_TRY(init_cuda(s));
     KZ_CUDA(cudaSetDevice(s->device));
     // global triangle order = mesh order
@@ -600,6 +696,26 @@ kz_status kz_scene_build(kz_scene* s) {
         lights.push_back(L);
     }
 
+    // vertex uvs per triangle record (leaf order) for textured materials
+    std::vector<float2> tri_uv;
+    if (any_tex) {
+        tri_uv.resize((size_t)total * 3);
+        for (size_t r = 0; r < (size_t)total; ++r) {
+            const uint32_t gid = out.order[r];
+            const uint32_t g = tgeom[gid];
+            const HostMesh& m = s->meshes[g];
+            const size_t k = gid - goff[g];
+            for (int c = 0; c < 3; ++c) {
+                if (m.uv.empty()) {
+                    tri_uv[r * 3 + c] = make_float2(c == 1 ? 1.f : 0.f, c == 2 ? 1.f : 0.f);
+                } else {
+                    const uint32_t vi = m.idx[k * 3 + c];
+                    tri_uv[r * 3 + c] = make_float2(m.uv[(size_t)vi * 2], m.uv[(size_t)vi * 2 + 1]);
+                }
+            }
+        }
+    }
+
     cudaStream_t st = s->stream;
     KZ_TRY(upload(s->nodes, out.nodes, st));
     KZ_TRY(upload(s->tris, out.tris, st));
@@ -609,6 +725,14 @@ kz_status kz_scene_build(kz_scene* s) {
     KZ_TRY(upload(s->lights, lights, st));
     KZ_TRY(upload(s->light_cdf, cdf, st));
     KZ_TRY(upload(s->light_tris, ltris, st));
+    if (any_tex) {
+        KZ_TRY(upload(s->d_tri_uv, tri_uv, st));
+        KZ_TRY(upload(s->d_mat_tex, mat_tex, st));
+    }
+    if (ntex) {
+        KZ_TRY(upload(s->d_textures, s->textures, st));
+        KZ_TRY(upload(s->d_texels, s->tex_texels, st));
+    }
     KZ_CUDA(cudaStreamSynchronize(st));
 
     kz::DevScene& d = s->dev;
@@ -639,6 +763,14 @@ kz_status kz_scene_build(kz_scene* s) {
     d.light_cdf = s->light_cdf.as<float>();
     d.light_tris = s->light_tris.as<float4>();
     d.n_lights = (uint32_t)lights.size();
+    d.tri_uv = any_tex ? s->d_tri_uv.as<float2>() : nullptr;
+    d.mat_tex = any_tex ? s->d_mat_tex.as<int32_t>() : nullptr;
+    d.textures = ntex ? s->d_textures.as<kz::DevTexture>() : nullptr;
+    d.tex_data = ntex ? s->d_texels.as<float>() : nullptr;
+    d.n_textures = ntex;
+    d.env = make_float3(s->env_rgb[0], s->env_rgb[1], s->env_rgb[2]);
+    d.env_tex = s->env_tex;
+    d.has_env = (s->env_rgb[0] > 0.f || s->env_rgb[1] > 0.f || s->env_rgb[2] > 0.f) ? 1u : 0u;
 
     s->info.n_meshes = s->meshes.size();
     s->info.n_triangles = total;
@@ -1373,13 +1505,15 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
     // they started and a captured batch can be replayed as is
     uint32_t iters = std::max<uint32_t>(4, max_depth + 1);
     iters += iters & 1u;
+    bool textured = false;  // the texture tint is compiled out unless a job needs it
+    for (uint32_t j = 0; j < n_jobs; ++j) textured |= jobs[j].scene->dev.mat_tex != nullptr;
     auto enqueue = [&]() {
         kz::PathSoA a = A, b = B;
         for (uint32_t it = 0; it < iters; ++it) {
             kz::launch_plan(ctr, cap, strm);
             kz::launch_generate_batch_dev(djobs, n_jobs, a, ctr, cap, block, strm);
             kz::launch_trace_paths_batch(djobs, a, cap, ctr, strm);
-            kz::launch_shade_batch(djobs, a, cap, b, sq, ctr, block, strm);
+            kz::launch_shade_batch(djobs, a, cap, b, sq, ctr, block, textured, strm);
             kz::launch_trace_shadow_batch(djobs, sq, cap, ctr, strm);
             kz::launch_finish(ctr, strm);
             std::swap(a, b);

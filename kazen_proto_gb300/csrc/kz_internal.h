@@ -21,6 +21,17 @@ struct DevLight {
     float Le[3];
 };
 
+// A texture as the kernels read it (kz_texture with the image moved into
+// the scene's texel array).
+struct DevTexture {
+    int32_t kind = 0;
+    uint32_t w = 0, h = 0;
+    uint32_t pad = 0;
+    uint64_t offset = 0;  // first float of the RGB image in DevScene::tex_data
+    float scale_s = 1.f, scale_t = 1.f;
+    float Ca[3] = {1.f, 1.f, 1.f}, Cb[3] = {0.f, 0.f, 0.f};
+};
+
 struct DevScene {
     const uint4* nodes = nullptr;       // n_nodes * 5 (80-byte 8-wide nodes)
     const float4* tris = nullptr;       // n_tris * 3, leaf order
@@ -35,6 +46,15 @@ struct DevScene {
     uint32_t n_lights = 0;
     float3 box_lo = {0.f, 0.f, 0.f};   // scene bounds (guiding input encoding)
     float3 box_inv = {1.f, 1.f, 1.f};  // 1 / extent per axis
+    // textures: NULL / 0 when the scene has none
+    const float2* tri_uv = nullptr;     // n_tris * 3 vertex uvs, leaf order
+    const int32_t* mat_tex = nullptr;   // texture of each material or -1
+    const DevTexture* textures = nullptr;
+    const float* tex_data = nullptr;
+    uint32_t n_textures = 0;
+    int32_t env_tex = -1;               // environment texture or -1
+    float3 env = {0.f, 0.f, 0.f};       // environment radiance (times env_tex)
+    uint32_t has_env = 0;
 };
 
 // Guiding network parameters as the kernels read them.
@@ -223,7 +243,7 @@ void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst,
                                uint32_t block, cudaStream_t st);
 void launch_trace_paths_batch(const DevJob* jobs, PathSoA p, uint32_t cap, DevCounters* ctr, cudaStream_t st);
 void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
-                        uint32_t block, cudaStream_t st);
+                        uint32_t block, bool textured, cudaStream_t st);
 void launch_trace_shadow_batch(const DevJob* jobs, ShadowSoA sq, uint32_t cap, DevCounters* ctr, cudaStream_t st);
 // Queries the persistent stages' grid sizes (call before a stream capture).
 void prepare_batch_wavefront();

@@ -133,14 +133,22 @@ void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint3
         launch_shade_guided_dev(s, pp, in, cap, out, sq, ctr, film, film64, *gs, block, st);
         return;
     }
-    k_shade<false><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64, GuideShade{},
-                                                           &ctr->n_active);
+    if (s.mat_tex)
+        k_shade<false, true><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64,
+                                                                     GuideShade{}, &ctr->n_active);
+    else
+        k_shade<false, false><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64,
+                                                                      GuideShade{}, &ctr->n_active);
 }
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
                   DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
     if (!n_in) return;
-    k_shade<false><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
-                                                            GuideShade{}, nullptr);
+    if (s.mat_tex)
+        k_shade<false, true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
+                                                                      GuideShade{}, nullptr);
+    else
+        k_shade<false, false><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
+                                                                       GuideShade{}, nullptr);
 }
 void launch_guide_collect(const VRec* recs, const NRec* nee, uint64_t n_recs, float4* samples, uint32_t cap,
                           uint32_t* count, float* wsum, cudaStream_t st) {

@@ -202,6 +202,49 @@ __device__ __forceinline__ void propagate(VRec* recs, uint64_t rbase, uint32_t d
     }
 }
 
+// ------------------------------------------------------------------ textures
+// OSL checkerboard (int() truncates, as the shader's int(fmod(..)) does) or
+// a bilinear lookup with periodic wrap, texel centres at (i + 0.5) / w.
+__device__ __noinline__ f3 tex_eval(const DevScene& s, int32_t k, float u, float v) {
+    const DevTexture& tx = s.textures[k];
+    if (!isfinite(u)) u = 0.f;
+    if (!isfinite(v)) v = 0.f;
+    if (tx.kind == KZ_TEX_CHECKER) {
+        const float cs = fmodf(u * tx.scale_s, 2.f), ct = fmodf(v * tx.scale_t, 2.f);
+        const int a = isfinite(cs) ? (int)cs : 0, b = isfinite(ct) ? (int)ct : 0;
+        return (a ^ b) == 0 ? mk(tx.Ca[0], tx.Ca[1], tx.Ca[2]) : mk(tx.Cb[0], tx.Cb[1], tx.Cb[2]);
+    }
+    u -= floorf(u);
+    v -= floorf(v);
+    const float x = u * (float)tx.w - 0.5f, y = v * (float)tx.h - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = x - fx, ay = y - fy;
+    const uint32_t x0 = fx < 0.f ? tx.w - 1 : min((uint32_t)fx, tx.w - 1), x1 = x0 + 1 == tx.w ? 0 : x0 + 1;
+    const uint32_t y0 = fy < 0.f ? tx.h - 1 : min((uint32_t)fy, tx.h - 1), y1 = y0 + 1 == tx.h ? 0 : y0 + 1;
+    const float* d = s.tex_data + tx.offset;
+    const f3 c00 = ld3(d + ((size_t)y0 * tx.w + x0) * 3), c10 = ld3(d + ((size_t)y0 * tx.w + x1) * 3);
+    const f3 c01 = ld3(d + ((size_t)y1 * tx.w + x0) * 3), c11 = ld3(d + ((size_t)y1 * tx.w + x1) * 3);
+    return (c00 * (1.f - ax) + c10 * ax) * (1.f - ay) + (c01 * (1.f - ax) + c11 * ax) * ay;
+}
+
+// Radiance of a ray leaving the scene: the environment in latitude-longitude form.
+__device__ __noinline__ f3 env_radiance(const DevScene& s, f3 d) {
+    f3 e = mk(s.env.x, s.env.y, s.env.z);
+    if (s.env_tex >= 0) {
+        const float u = 0.5f + atan2f(d.x, -d.z) * (0.5f * kInvPi);
+        const float v = acosf(fminf(fmaxf(d.y, -1.f), 1.f)) * kInvPi;
+        e = hmul(e, tex_eval(s, s.env_tex, u, v));
+    }
+    return e;
+}
+
+// Weight of lobe k at this vertex: the texture tint applies to the lobes
+// that reference the material's texture.
+__device__ __forceinline__ f3 lobe_weight(const kz_lobe& lb, bool textured, f3 tint) {
+    const f3 w = ld3(lb.weight);
+    return textured && lb.params[KZ_LOBE_TEXTURE_PARAM] != 0.f ? hmul(w, tint) : w;
+}
+
 struct ShadeOut {
     bool cont = false, shadow = false;
     float4 o_next, d_next, b_next, s_o, s_d, s_c;
@@ -212,8 +255,9 @@ struct ShadeOut {
 
 // One shaded path vertex: emission, next-event estimation (the shadow ray is
 // returned, not traced), roulette and direction sampling. `raw` holds the
-// guiding network's outputs for this path (guided mode only).
-template <bool kGuided>
+// guiding network's outputs for this path (guided mode only). kTex = false
+// compiles the texture tint out (scenes without textured materials).
+template <bool kGuided, bool kTex = true>
 __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams& pp, const float4 hit,
                                              const float4 o4, const float4 d4, const float4 b4,
                                              unsigned long long rng_state, const GuideShade& gs, const float* raw,
@@ -241,6 +285,17 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
         const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
         const f3 d = xyz(d4);
         const f3 P = xyz(o4) + d * hit.x;
+        // texture tint of the material at the hit's uv (interpolated vertex
+        // uvs; the barycentrics of vertices 1, 2 when the mesh has none)
+        const int32_t mtex = kTex && s.mat_tex ? __ldg(s.mat_tex + __float_as_uint(tc.w)) : -1;
+        const bool textured = mtex >= 0;
+        f3 tint = mk(1.f, 1.f, 1.f);
+        if (textured) {
+            const float2 q0 = s.tri_uv[(size_t)rec * 3], q1 = s.tri_uv[(size_t)rec * 3 + 1],
+                         q2 = s.tri_uv[(size_t)rec * 3 + 2];
+            const float b0 = 1.f - hit.y - hit.z;
+            tint = tex_eval(s, mtex, b0 * q0.x + hit.y * q1.x + hit.z * q2.x, b0 * q0.y + hit.y * q1.y + hit.z * q2.y);
+        }
         const Frame fr(Ng);
         const f3 wi = -fr.to_local(d);
         f3 beta = xyz(b4);
@@ -273,7 +328,8 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
         bool any_smooth = false, any_delta = false;
         for (uint32_t k = 0; k < nlobes; ++k) {
             const kz_lobe& lb = mat.lobes[k];
-            lp[k] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
+            const f3 lw = lobe_weight(lb, textured, tint);
+            lp[k] = (lw.x * beta.x + lw.y * beta.y + lw.z * beta.z) * winv;
             wsum += lp[k];
             const bool dl = lobe_is_delta(lb.closure_id);
             any_smooth |= !dl;
@@ -315,7 +371,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     const kz_lobe& lb = mat.lobes[k];
                     if (lobe_is_delta(lb.closure_id)) continue;
                     const LobeEval e = lobe_eval(lb, wi, wo);
-                    f = f + hmul(ld3(lb.weight), e.f);
+                    f = f + hmul(lobe_weight(lb, textured, tint), e.f);
                     bpdf += lp[k] * e.pdf;
                 }
                 if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
@@ -382,7 +438,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                 for (uint32_t k = 0; k < nlobes; ++k) {
                     const kz_lobe& lb = mat.lobes[k];
                     const LobeEval e = lobe_eval(lb, wi, wo);
-                    f = f + hmul(ld3(lb.weight), e.f);
+                    f = f + hmul(lobe_weight(lb, textured, tint), e.f);
                     pdf += lp[k] * e.pdf;
                 }
                 pdf = alpha * mixture_pdf_shading(mix, wdir) + (1.f - alpha) * pdf;
@@ -430,7 +486,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             float pdf_dir = 0.f;
             if (alive) {
                 if (smp.delta) {
-                    weight = hmul(ld3(ls.weight), smp.weight) * (1.f / lp[sel]);
+                    weight = hmul(lobe_weight(ls, textured, tint), smp.weight) * (1.f / lp[sel]);
                 } else {
                     f3 f = mk(0.f, 0.f, 0.f);
                     float pdf = 0.f;
@@ -438,7 +494,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                         const kz_lobe& lb = mat.lobes[k];
                         if (lobe_is_delta(lb.closure_id)) continue;
                         const LobeEval e = lobe_eval(lb, wi, smp.wo);
-                        f = f + hmul(ld3(lb.weight), e.f);
+                        f = f + hmul(lobe_weight(lb, textured, tint), e.f);
                         pdf += lp[k] * e.pdf;
                     }
                     alive = pdf > 0.f;
@@ -462,7 +518,17 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             }
         }
         out.Lsum = Lsum;
-            out.film_idx = film_idx;
+        out.film_idx = film_idx;
+    } else if (s.has_env) {
+        // a miss: throughput times the environment, without MIS (the
+        // environment is not sampled as a light), integrator.cpp:545-552
+        const uint32_t pid = __float_as_uint(b4.w);
+        out.Lsum = hmul(xyz(b4), env_radiance(s, xyz(d4)));
+        out.film_idx = pid / pp.spp;
+        if (kGuided && gs.recs) {
+            const uint32_t depth = __float_as_uint(d4.w) & 0xffu;
+            propagate(gs.recs, ((uint64_t)pid - gs.pass_first) * pp.max_depth, depth, out.Lsum);
+        }
     }
 }
 
@@ -499,10 +565,10 @@ static unsigned resident_grid(F f, unsigned block) {
 // Plain shading is capped at 64 registers (4 blocks per SM): the occupancy
 // gained outweighs a few spills (measured: 5 % faster); the guided variant
 // keeps its registers (at 64 it spills 728 bytes per thread).
-template <bool kGuided>
 #ifndef KZ_SHADE_MIN_BLOCKS
 #define KZ_SHADE_MIN_BLOCKS 4
 #endif
+template <bool kGuided, bool kTex = true>
 __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
@@ -511,8 +577,8 @@ __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     if (n_dev) n_in = *n_dev;
     ShadeOut so;
     if (i < n_in) {
-        shade_vertex<kGuided>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
-                              kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
+        shade_vertex<kGuided, kTex>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
+                                    kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
         if (!is_zero(so.Lsum)) film_add(film, film64, so.film_idx, so.Lsum);
     }
     const bool cont = so.cont, shadow = so.shadow;

@@ -43,7 +43,7 @@ _TOKEN = re.compile(r"""
   | (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?)
   | (?P<str>"(?:[^"\\]|\\.)*")
   | (?P<id>[A-Za-z_]\w*)
-  | (?P<op>&&|\|\||==|!=|<=|>=|\+=|-=|\*=|/=|\[\[|\]\]|[-+*/<>=!?:(),;{}\[\]])
+  | (?P<op>&&|\|\||==|!=|<=|>=|\+=|-=|\*=|/=|\[\[|\]\]|[-+*/<>=!?:(),;{}\[\]^%&|~.])
 """, re.S | re.X)
 LUMA = np.array([0.2126, 0.7152, 0.0722])
 
@@ -67,13 +67,35 @@ class Normal:
     """The shading normal N (local +y)."""
 
 
+class Global:
+    """A shading-point global the lowering keeps symbolic: u, v (texture
+    coordinates) or I (the ray direction, for environment lookups)."""
+
+    def __init__(self, name):
+        self.name = name
+
+
+@dataclass
+class TexRef:
+    """A colour that varies over the surface: scale times a texture lookup.
+    spec: ("image", filename), ("checker", scale_s, scale_t, Ca, Cb) or
+    ("environment", filename)."""
+    spec: tuple
+    scale: np.ndarray = field(default_factory=lambda: np.ones(3))
+
+
 @dataclass
 class Closure:
-    terms: list = field(default_factory=list)  # (weight np3, name, args)
+    terms: list = field(default_factory=list)  # (weight np3, name, args, TexRef spec or None)
 
-    def scaled(self, w):
+    def scaled(self, w, tex=None):
         w = np.asarray(w, np.float64)
-        return Closure([(t[0] * w, t[1], t[2]) for t in self.terms])
+        out = []
+        for t in self.terms:
+            if tex is not None and t[3] is not None:
+                raise ValueError("OSL: a closure weighted by two textures is not lowered")
+            out.append((t[0] * w, t[1], t[2], t[3] if tex is None else tex))
+        return Closure(out)
 
 
 def _is_num(v):
@@ -85,6 +107,18 @@ def _zero(v):
 
 
 def binop(op, a, b):
+    if isinstance(a, TexRef) or isinstance(b, TexRef):
+        if op == "*":
+            t, o = (a, b) if isinstance(a, TexRef) else (b, a)
+            if isinstance(o, Closure):
+                return o.scaled(t.scale, t.spec)
+            if _is_num(o):
+                return TexRef(t.spec, t.scale * np.asarray(o, np.float64))
+        elif op == "/" and isinstance(a, TexRef) and _is_num(b):
+            return TexRef(a.spec, a.scale / np.asarray(b, np.float64))
+        raise ValueError(f"OSL: operator {op} on a texture lookup is not lowered (only scaling and closure weights)")
+    if isinstance(a, Global) or isinstance(b, Global):
+        raise ValueError("OSL: arithmetic on u, v or I is not lowered (texture coordinates pass through unchanged)")
     if isinstance(a, Closure) or isinstance(b, Closure):
         if op == "+":
             if isinstance(a, Closure) and isinstance(b, Closure):
@@ -137,6 +171,10 @@ def truth(v) -> bool:
 
 def convert(kind: str, v):
     """Assignment conversion to a declared type."""
+    if isinstance(v, Global) and kind in ("float", "vector", "point", "normal"):
+        return v
+    if isinstance(v, TexRef) and kind == "color":
+        return v
     if kind in _VEC_TYPES:
         if isinstance(v, Normal):
             return v
@@ -166,6 +204,8 @@ def convert(kind: str, v):
 
 def _triple(*args):
     if len(args) == 1:
+        if isinstance(args[0], TexRef):
+            return args[0]
         return convert("color", args[0])
     if len(args) == 3:
         return np.array([float(a) for a in args])
@@ -182,14 +222,34 @@ def _mix(a, b, t):
 
 def _elementwise(fn):
     def f(*args):
-        if any(isinstance(a, (Closure, Normal, str)) for a in args):
+        if any(isinstance(a, (Closure, Normal, str, TexRef, Global)) for a in args):
             raise ValueError("OSL: math function on a non-numeric value")
         r = fn(*[np.asarray(a, np.float64) for a in args])
         return r if np.ndim(r) else float(r)
     return f
 
 
+def _texture(filename, s, t, *opts):
+    """texture(filename, u, v): an image lookup at the hit's texture coordinates."""
+    if not (isinstance(s, Global) and s.name == "u" and isinstance(t, Global) and t.name == "v"):
+        raise ValueError("OSL: texture() is lowered at (u, v) only")
+    if not isinstance(filename, str):
+        raise ValueError("OSL: texture() takes a file name")
+    return TexRef(("image", filename))
+
+
+def _environment(filename, d, *opts):
+    """environment(filename, I): a latitude-longitude lookup along the ray; an
+    empty file name looks up nothing (black), as OIIO does."""
+    if not (isinstance(d, Global) and d.name == "I"):
+        raise ValueError("OSL: environment() is lowered along I only")
+    if not filename:
+        return 0.0
+    return TexRef(("environment", filename))
+
+
 FUNCS = {
+    "texture": _texture, "environment": _environment,
     "color": _triple, "vector": _triple, "normal": _triple, "point": _triple,
     "luminance": lambda c: float(np.dot(convert("color", c), LUMA)),
     "clamp": _elementwise(lambda x, lo, hi: np.minimum(np.maximum(x, lo), hi)),
@@ -256,7 +316,7 @@ class Parser:
             return tok[1]
         return None
 
-    def shader(self):
+    def shader(self, body: bool = True):
         kind = self.next()
         if kind[1] not in ("surface", "shader", "displacement", "volume"):
             raise ValueError(f"OSL: expected a shader declaration, found {kind[1]!r}")
@@ -276,8 +336,7 @@ class Parser:
             params.append((ty, pname, self.expr()))
             self.skip_metadata()
             self.accept(",")
-        body = self.block()
-        return name, params, body
+        return name, params, (self.block() if body else None)
 
     def block(self):
         self.expect("{")
@@ -389,9 +448,13 @@ class _Return(Exception):
 
 @dataclass
 class Lowered:
-    lobes: list
+    lobes: list                 # kz_lobe records; params[11] = index into `textures` + 1
     Le: np.ndarray
     warnings: list
+    textures: list = field(default_factory=list)   # TexRef specs the lobes reference
+    background: np.ndarray = field(default_factory=lambda: np.zeros(3))  # background() weight
+    background_texture: tuple = None                # its environment TexRef spec, or None
+    outputs: dict = field(default_factory=dict)     # output parameters after the body ran
 
 
 class Evaluator:
@@ -406,6 +469,8 @@ class Evaluator:
                 return s[name]
         if name == "N" or name == "Ng":
             return Normal()
+        if name in ("u", "v", "I"):
+            return Global(name)
         raise ValueError(f"OSL: `{name}` is not a parameter or local (position-dependent globals are not lowered)")
 
     def declared_type(self, name):
@@ -492,7 +557,7 @@ class Evaluator:
         if kind == "call":
             name, args = e[1], [self.eval(a) for a in e[2]]
             if name in CLOSURES:
-                return Closure([(np.ones(3), name, args)])
+                return Closure([(np.ones(3), name, args, None)])
             if name in FUNCS:
                 return FUNCS[name](*args)
             raise ValueError(f"OSL: function `{name}` is not lowered")
@@ -572,19 +637,32 @@ def _lobe(name, args, w, warnings):
     raise ValueError(f"OSL: closure `{name}` is not lowered")
 
 
-def lower(src: str, overrides: dict | None = None) -> Lowered:
-    """Evaluate a surface shader over constant inputs -> lobes and Le."""
-    name, params, body = Parser(src).shader()
-    ev = Evaluator({})
+def _param_env(params, overrides, ev):
     for ty, pname, default in params:
         ev.types[0][pname] = ty
         if overrides and pname in overrides:
             v = overrides[pname]
-            if not isinstance(v, str):
+            if not isinstance(v, (str, TexRef, Global)):
                 v = np.asarray(v, np.float64) if np.ndim(v) else float(v)
             ev.scopes[0][pname] = convert(ty, v)
         else:
             ev.scopes[0][pname] = convert(ty, ev.eval(default))
+
+
+def shader_params(src: str, overrides: dict | None = None):
+    """(shader name, {parameter: value}) at the defaults, with overrides."""
+    name, params, _ = Parser(src).shader(body=False)
+    ev = Evaluator({})
+    _param_env(params, overrides, ev)
+    return name, dict(ev.scopes[0])
+
+
+def lower(src: str, overrides: dict | None = None) -> Lowered:
+    """Evaluate a surface shader over constant inputs -> lobes, Le, the
+    textures the lobes use, the background() weight and the output parameters."""
+    name, params, body = Parser(src).shader()
+    ev = Evaluator({})
+    _param_env(params, overrides, ev)
     ev.scopes[0]["Ci"] = Closure()
     ev.types[0]["Ci"] = "closure"
     try:
@@ -592,18 +670,53 @@ def lower(src: str, overrides: dict | None = None) -> Lowered:
     except _Return:
         pass
     ci = ev.scopes[0]["Ci"]
-    lobes, Le, warnings = [], np.zeros(3), list(ev.warnings)
-    for w, cname, args in ci.terms:
+    lobes, Le, warnings, textures = [], np.zeros(3), list(ev.warnings), []
+    bg, bg_tex = np.zeros(3), None
+    for w, cname, args, tex in ci.terms:
         w = np.asarray(w, np.float64)
+        if cname == "background":
+            if tex is not None:
+                if bg_tex is not None and bg_tex != tex:
+                    raise ValueError("OSL: a background weighted by two environment maps is not lowered")
+                bg_tex = tex
+            bg = bg + w
+            continue
+        if tex is not None and tex[0] == "environment":
+            raise ValueError("OSL: environment() weights only background()")
         if cname in ("emission", "kp_emitter"):  # process_closure adds the weight to Le
+            if tex is not None:
+                raise ValueError("OSL: textured emission is not lowered")
             Le = Le + w
             continue
-        if cname in ("background", "holdout", "debug"):
+        if cname in ("holdout", "debug"):
             continue
         if np.all(w == 0):
             continue
         lb = _lobe(cname, args, w, warnings)
+        if tex is not None:
+            if tex not in textures:
+                textures.append(tex)
+            if len(textures) > 1:
+                raise ValueError("OSL: lobes of one shader reference two textures (one per material is lowered)")
+            lb = api.textured(lb, textures.index(tex))
         lobes.append(lb)
     if len(lobes) > N.KZ_MAX_LOBES:
         raise ValueError(f"shader yields {len(lobes)} lobes; the reference keeps at most {N.KZ_MAX_LOBES}")
-    return Lowered(lobes, Le, warnings)
+    outputs = {k: ev.scopes[0][k] for _, k, _ in params}
+    return Lowered(lobes, Le, warnings, textures, bg, bg_tex, outputs)
+
+
+def checkerboard_output(params: dict) -> TexRef:
+    """The OSL checkerboard shader (Cout = Ca or Cb by the parity of
+    int(fmod(s * scale_s, 2)) ^ int(fmod(t * scale_t, 2)); the version shipped
+    with OSL and with the reference's textured scenes) at s = u, t = v, as a
+    texture. Its body uses integer operations the evaluator does not lower, so
+    it is recognised by name and parameters."""
+    s, t = params.get("s"), params.get("t")
+    if not (isinstance(s, Global) and s.name == "u" and isinstance(t, Global) and t.name == "v"):
+        raise ValueError("checkerboard is lowered at s = u, t = v only")
+    ca, cb = convert("color", params["Ca"]), convert("color", params["Cb"])
+    if isinstance(ca, TexRef) or isinstance(cb, TexRef):
+        raise ValueError("checkerboard colours must be constant")
+    return TexRef(("checker", float(params["scale_s"]), float(params["scale_t"]), tuple(float(x) for x in ca),
+                   tuple(float(x) for x in cb)))

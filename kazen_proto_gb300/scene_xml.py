@@ -17,21 +17,33 @@ the GPU path renders:
   over constant inputs (kazen_proto_gb300.osl_lower): the closures the
   reference registers (diffuse, ward, reflection, refraction, microfacet,
   kp_mirror, kp_dielectric, kp_microfacet, the kp_principle_* family) become
-  lobes; kp_emitter and emission add their weight to Le;
+  lobes; kp_emitter and emission add their weight to Le; a closure weighted
+  by texture(filename, u, v) or by a connected checkerboard layer
+  (<ConnectShaders>) becomes a textured lobe (kz_texture: image files via
+  texture_io, the checkerboard as a procedural texture);
+* <EnvironmentBegin> / <Shader> / <EnvironmentEnd>: the background shader,
+  `color(environment(filename, I)) * background()`, becomes the scene
+  environment (constant or latitude-longitude image; an empty file name is
+  black, as OIIO returns for it);
 * <Objects>: <Mesh filename shader_name [is_light] [translate] [rotate]
-  [scale]> from OBJ files (positions and faces; polygons fan-triangulated,
-  negative indices resolved), <Triangle verta vertb vertc>, <Quad center dir
-  vertical_vec half_width half_height>; transforms compose as the
-  reference's do, world = T * R * S * local, rotate = (axis xyz, degrees);
+  [scale]> from OBJ files (positions, texture coordinates and faces;
+  polygons fan-triangulated, negative indices resolved), <Triangle verta
+  vertb vertc> (uv = barycentrics), <Quad center dir vertical_vec half_width
+  half_height> (uv over the quad, as Quad::intersect), <Sphere> (tessellated
+  to an icosphere of 5,120 triangles with the reference's parametric uv);
+  transforms compose as the reference's do, world = T * R * S * local,
+  rotate = (axis xyz, degrees);
 * integrator tags are recorded; rendering always uses the path integrator.
 
-Not supported (reported in `LoadedScene.warnings`, never silently changed):
-analytic <Sphere> (tessellated to an icosphere of 5,120 triangles), point
-lights, textures and shader networks (<ConnectShaders>), the environment
-shader (a miss contributes nothing). Shading uses geometric normals (OBJ
-vertex normals are not read). The reference's own parser sets is_light for
-any `is_light` attribute whatever its value (scene.cpp:540); this loader
-honours the value.
+Shader files are looked up next to the scene, then in the reference's shader
+library directory (../../shader/src relative to the scene).
+
+Not supported (reported in `LoadedScene.warnings` or raised, never silently
+changed): point lights, BSSRDF closures, bump mapping and shaders whose
+closure weights depend on the shading point other than through the texture
+lookups above. Shading uses geometric normals (OBJ vertex normals are not
+read). The reference's own parser sets is_light for any `is_light`
+attribute whatever its value (scene.cpp:540); this loader honours the value.
 """
 from __future__ import annotations
 
@@ -43,7 +55,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import api, osl_lower
+from . import _native as N
+from . import api, osl_lower, texture_io
 from .scenes import SceneDesc, icosphere
 
 
@@ -65,7 +78,7 @@ def parse_value(text: str):
     'string x', 'func_translate ...' / 'func_scale ...' -> np.array."""
     parts = text.split()
     if not parts:
-        raise ValueError("empty attribute value")
+        return ""  # an untyped empty value, e.g. filename="" of the environment shader
     kind, vals = parts[0], parts[1:]
     if kind == "bool":
         return vals[0] == "true"
@@ -84,9 +97,11 @@ def parse_value(text: str):
 
 
 # ---------------------------------------------------------------- OBJ
-def load_obj(path: str):
-    """Vertices (n, 3) float32 and triangles (m, 3) uint32 of an OBJ file."""
-    verts, tris = [], []
+def load_obj(path: str, with_uv: bool = False):
+    """Vertices (n, 3) float32 and triangles (m, 3) uint32 of an OBJ file;
+    with_uv also returns (n, 2) texture coordinates (None when the file has
+    no `vt`), vertices split where one position carries several uvs."""
+    verts, uvs, tris, corners = [], [], [], []
     with open(path) as f:
         for line in f:
             line = line.split("#", 1)[0].strip()
@@ -95,20 +110,36 @@ def load_obj(path: str):
             tok = line.split()
             if tok[0] == "v":
                 verts.append([float(tok[1]), float(tok[2]), float(tok[3])])
+            elif tok[0] == "vt":
+                uvs.append([float(tok[1]), float(tok[2]) if len(tok) > 2 else 0.0])
             elif tok[0] == "f":
                 idx = []
                 for t in tok[1:]:
-                    i = int(t.split("/")[0])
-                    idx.append(i - 1 if i > 0 else len(verts) + i)
+                    parts = t.split("/")
+                    i = int(parts[0])
+                    vi = i - 1 if i > 0 else len(verts) + i
+                    ti = -1
+                    if len(parts) > 1 and parts[1]:
+                        j = int(parts[1])
+                        ti = j - 1 if j > 0 else len(uvs) + j
+                    idx.append((vi, ti))
                 if len(idx) < 3:
                     raise ValueError(f"{path}: face with {len(idx)} vertices")
                 for k in range(1, len(idx) - 1):  # fan
-                    tris.append([idx[0], idx[k], idx[k + 1]])
+                    corners.append([idx[0], idx[k], idx[k + 1]])
     v = np.asarray(verts, np.float32).reshape(-1, 3)
-    t = np.asarray(tris, np.int64).reshape(-1, 3)
-    if t.size and (t.min() < 0 or t.max() >= len(v)):
+    c = np.asarray(corners, np.int64).reshape(-1, 3, 2)
+    if c.size and (c[..., 0].min() < 0 or c[..., 0].max() >= len(v)):
         raise ValueError(f"{path}: face index out of range")
-    return v, t.astype(np.uint32)
+    if not with_uv:
+        return v, c[..., 0].astype(np.uint32)
+    if not uvs or (c[..., 1] < 0).all():
+        return v, c[..., 0].astype(np.uint32), None
+    if (c[..., 1] < 0).any() or c[..., 1].max() >= len(uvs):
+        raise ValueError(f"{path}: texture coordinate index missing or out of range")
+    pairs, inv = np.unique(c.reshape(-1, 2), axis=0, return_inverse=True)
+    uv = np.asarray(uvs, np.float32)[pairs[:, 1]]
+    return v[pairs[:, 0]], inv.reshape(-1, 3).astype(np.uint32), uv
 
 
 # ---------------------------------------------------------------- transforms
@@ -150,6 +181,99 @@ def lower_shader(src: str, params: dict, warnings: list | None = None):
     if warnings is not None:
         warnings.extend(r.warnings)
     return api.material(r.lobes, Le=tuple(float(x) for x in r.Le))
+
+
+def _find(paths, what):
+    for p in paths:
+        if os.path.exists(p):
+            return p
+    raise FileNotFoundError(f"{what} not found (looked in: {', '.join(paths)})")
+
+
+def shader_source(base: str, name: str) -> str:
+    """An .osl file next to the scene, else in the shader library two levels
+    up (resource/shader/src beside resource/scene/<name>/ in kazen_proto)."""
+    path = _find([os.path.join(base, name + ".osl"),
+                  os.path.join(base, "..", "..", "shader", "src", name + ".osl")], f"shader {name}.osl")
+    with open(path) as f:
+        return f.read()
+
+
+def lower_group(base: str, shaders, connections):
+    """Evaluate a shader group: each layer in order, <ConnectShaders> feeding
+    an upstream output parameter into a downstream input; the last layer's
+    closures are the group's (OSL's group semantics). Returns osl_lower.Lowered."""
+    outputs, last = {}, None
+    for sname, layer, params in shaders:
+        ov = dict(params)
+        for sl, sp, dl, dp in connections:
+            if dl == layer:
+                if sl not in outputs or sp not in outputs[sl]:
+                    raise ValueError(f"connection from {sl}.{sp}: no such earlier layer output")
+                ov[dp] = outputs[sl][sp]
+        src = shader_source(base, sname)
+        if sname == "checkerboard":
+            _, p = osl_lower.shader_params(src, ov)
+            outputs[layer] = {"Cout": osl_lower.checkerboard_output(p)}
+            last = None
+        else:
+            last = osl_lower.lower(src, ov)
+            outputs[layer] = last.outputs
+    if last is None:
+        raise ValueError("the last layer of a shader group must be a surface shader")
+    return last
+
+
+class TextureTable:
+    """Scene-wide texture list built from the lowered shaders' references."""
+
+    def __init__(self, base: str):
+        self.base = base
+        self.specs, self.textures = [], []
+
+    def index(self, spec) -> int:
+        if spec in self.specs:
+            return self.specs.index(spec)
+        if spec[0] == "checker":
+            _, ss, st, ca, cb = spec
+            tex = api.checker_texture(ss, st, ca, cb)
+        else:
+            fname = spec[1]
+            path = _find([fname if os.path.isabs(fname) else os.path.join(self.base, fname),
+                          os.path.join(self.base, os.path.basename(fname))], f"texture {fname}")
+            tex = api.image_texture(texture_io.read_image(path))
+        self.specs.append(spec)
+        self.textures.append(tex)
+        return len(self.specs) - 1
+
+    def material(self, r):
+        lobes = []
+        for lb in r.lobes:
+            k = int(lb["params"][N.KZ_LOBE_TEXTURE_PARAM])
+            if k:
+                lb = api.textured(lb, self.index(r.textures[k - 1]))
+            lobes.append(lb)
+        return api.material(lobes, Le=tuple(float(x) for x in r.Le))
+
+
+def sphere_mesh(center, radius, level=4):
+    """Icosphere with the reference's parametric uv (Sphere::intersect,
+    src/core/shape.cpp:81-86: u = phi / 2 pi of atan2(z, x), v = theta / pi
+    + 0.5); triangles keep their own vertices so the seam does not wrap."""
+    sv, sf = icosphere(level)
+    v = (sv[sf].reshape(-1, 3)).astype(np.float64)
+    phi = np.arctan2(v[:, 2], v[:, 0])
+    phi = np.where(phi < 0, phi + 2 * np.pi, phi)
+    u = (phi / (2 * np.pi)).reshape(-1, 3)
+    pole = (np.hypot(v[:, 0], v[:, 2]) < 1e-6).reshape(-1, 3)
+    span = np.where(pole, 0.0, u).max(axis=1, keepdims=True) - np.where(pole, 1.0, u).min(axis=1, keepdims=True)
+    u = np.where((span > 0.5) & (u < 0.5), u + 1.0, u)
+    # a pole has no azimuth: give it the mean of its triangle's other corners
+    other = np.where(pole, 0.0, u).sum(axis=1, keepdims=True) / np.maximum(1, (~pole).sum(axis=1, keepdims=True))
+    u = np.where(pole, other, u).reshape(-1)
+    t = np.arccos(np.clip(v[:, 1], -1.0, 1.0)) / np.pi + 0.5
+    uv = np.stack([u, t], -1).astype(np.float32)
+    return (v * radius + center).astype(np.float32), np.arange(len(v), dtype=np.uint32).reshape(-1, 3), uv
 
 
 # ---------------------------------------------------------------- scene
@@ -199,36 +323,59 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             out.integrator = tag
             if tag != "PathIntegrator":
                 out.warnings.append(f"<{tag}> rendered with the path integrator")
-        elif tag in ("PointLight", "ConnectShaders"):
+        elif tag == "PointLight":
             out.warnings.append(f"<{tag}> is not supported and was skipped")
 
-    # materials: a ShaderGroupBegin starts a group, its Shader siblings follow
-    for mats in root.iter("Materials"):
+    # materials: a ShaderGroupBegin starts a group, its Shader and
+    # ConnectShaders siblings follow; the environment is a group between
+    # EnvironmentBegin and EnvironmentEnd at the top level
+    def shader_node(node):
+        params = {}
+        for p in node.iter("Parameter"):
+            for k, v in p.attrib.items():
+                params[k] = parse_value(v)
+        return node.attrib["name"], node.attrib.get("layer", ""), params
+
+    def connection(node):
+        a = node.attrib
+        return a["srclayer"], a["srcparam"], a["dstlayer"], a["dstparam"]
+
+    env_group = None
+    for parent in [root] + list(root.iter("Materials")):
         current = None
-        for node in list(mats):
-            if node.tag == "ShaderGroupBegin":
-                current = node.attrib["name"]
-                groups[current] = []
-            elif node.tag == "ShaderGroupEnd":
+        for node in list(parent):
+            if node.tag in ("ShaderGroupBegin", "EnvironmentBegin"):
+                current = node.attrib.get("name", "env") if node.tag == "ShaderGroupBegin" else "<environment>"
+                if node.tag == "EnvironmentBegin":
+                    env_group = ([], [])
+                else:
+                    groups[current] = ([], [])
+            elif node.tag in ("ShaderGroupEnd", "EnvironmentEnd"):
                 current = None
-            elif node.tag == "Shader":
+            elif node.tag in ("Shader", "ConnectShaders"):
                 if current is None:
-                    raise ValueError("<Shader> outside a shader group")
-                params = {}
-                for p in node.iter("Parameter"):
-                    for k, v in p.attrib.items():
-                        params[k] = parse_value(v)
-                groups[current].append((node.attrib["name"], params))
-    for name, shaders in groups.items():
-        if len(shaders) != 1:
-            raise ValueError(f"shader group {name!r} has {len(shaders)} shaders; networks are not lowered")
-        sname, params = shaders[0]
-        osl = os.path.join(base, sname + ".osl")
-        with open(osl) as f:
-            w = []
-            d.materials.append(lower_shader(f.read(), params, w))
-        out.warnings.extend(f"shader group {name!r}: {x}" for x in w)
+                    raise ValueError(f"<{node.tag}> outside a shader group")
+                g = env_group if current == "<environment>" else groups[current]
+                if node.tag == "Shader":
+                    g[0].append(shader_node(node))
+                else:
+                    g[1].append(connection(node))
+    tex = TextureTable(base)
+    for name, (shaders, conns) in groups.items():
+        r = lower_group(base, shaders, conns)
+        d.materials.append(tex.material(r))
+        out.warnings.extend(f"shader group {name!r}: {x}" for x in r.warnings)
         out.material_names.append(name)
+    if env_group is not None and env_group[0]:
+        try:
+            r = lower_group(base, *env_group)
+        except FileNotFoundError as e:
+            out.warnings.append(f"environment: {e}; the background stays black")
+        else:
+            d.env = tuple(float(x) for x in r.background)
+            if r.background_texture is not None:
+                d.env_texture = tex.index(("image", r.background_texture[1]))
+    d.textures = tex.textures
     mat_id = {n: i for i, n in enumerate(out.material_names)}
 
     def shader_of(node):
@@ -246,8 +393,8 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             light = bool(a.get("is_light", False))
             M = mesh_transform(a.get("translate"), a.get("rotate"), a.get("scale"))
             if node.tag == "Mesh":
-                v, t = load_obj(os.path.join(base, a["filename"]))
-                d.add(apply_transform(M, v), t, shader_of(node), light)
+                v, t, uv = load_obj(os.path.join(base, a["filename"]), with_uv=True)
+                d.add(apply_transform(M, v), t, shader_of(node), light, uv=uv)
             elif node.tag == "Triangle":
                 v = np.stack([a["verta"], a["vertb"], a["vertc"]])
                 d.add(apply_transform(M, v), np.array([[0, 1, 2]], np.uint32), shader_of(node), light)
@@ -258,12 +405,13 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
                 h /= np.linalg.norm(h)
                 c, hw, hh = np.asarray(a["center"]), float(a["half_width"]), float(a["half_height"])
                 q = np.stack([c - h * hw - up * hh, c + h * hw - up * hh, c + h * hw + up * hh, c - h * hw + up * hh])
-                d.add(apply_transform(M, q), np.array([[0, 1, 2], [0, 2, 3]], np.uint32), shader_of(node), light)
+                # uv of Quad::intersect (shape.cpp:335-345): P = c + h hw (u - 1/2) + up hh (v - 1/2)
+                d.add(apply_transform(M, q), np.array([[0, 1, 2], [0, 2, 3]], np.uint32), shader_of(node), light,
+                      uv=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
             elif node.tag == "Sphere":
                 cr = a["center_n_radius"]
-                sv, sf = icosphere(4)
-                v = sv * cr[3] + cr[:3]
-                d.add(apply_transform(M, v), sf, shader_of(node), light)
+                v, sf, uv = sphere_mesh(cr[:3], cr[3])
+                d.add(apply_transform(M, v), sf, shader_of(node), light, uv=uv)
                 out.warnings.append("<Sphere> tessellated to an icosphere of %d triangles" % len(sf))
             elif node.tag != "PointLight":  # reported with the other unsupported tags
                 out.warnings.append(f"<{node.tag}> in <Objects> is not supported and was skipped")

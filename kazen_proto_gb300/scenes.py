@@ -34,10 +34,17 @@ class SceneDesc:
     height: int = 256
     spp: int = 16
     max_depth: int = 5
+    textures: list = field(default_factory=list)   # api.Texture
+    uvs: dict = field(default_factory=dict)         # mesh index -> (nverts, 2) f32
+    env: tuple = (0.0, 0.0, 0.0)
+    env_texture: int = -1
 
-    def add(self, verts, idx, material_id, is_light=False):
+    def add(self, verts, idx, material_id, is_light=False, uv=None) -> int:
         self.meshes.append((np.asarray(verts, np.float32).reshape(-1, 3), np.asarray(idx, np.uint32).reshape(-1, 3),
                             int(material_id), bool(is_light)))
+        if uv is not None:
+            self.uvs[len(self.meshes) - 1] = np.asarray(uv, np.float32).reshape(-1, 2)
+        return len(self.meshes) - 1
 
     def material_array(self):
         arr = np.zeros(len(self.materials), dtype=api.N.MATERIAL_DTYPE)
@@ -50,11 +57,29 @@ class SceneDesc:
 
     def build(self) -> api.Scene:
         s = api.Scene()
-        for v, i, mat, light in self.meshes:
+        for g, (v, i, mat, light) in enumerate(self.meshes):
             s.add_mesh(v, i, mat, light)
+            if g in self.uvs:
+                s.set_mesh_uvs(g, self.uvs[g])
         s.set_materials(self.material_array())
+        if self.textures:
+            s.set_textures(self.textures)
+        if any(self.env) or self.env_texture >= 0:
+            s.set_environment(self.env, self.env_texture)
         s.build_bvh()
         return s
+
+    def tri_uvs(self):
+        """(N, 6) per-triangle vertex uvs in global order (barycentric defaults), or None."""
+        if not self.uvs:
+            return None
+        out = []
+        for g, (v, i, _, _) in enumerate(self.meshes):
+            if g in self.uvs:
+                out.append(self.uvs[g][i].reshape(-1, 6))
+            else:
+                out.append(np.tile(np.array([0, 0, 1, 0, 0, 1], np.float32), (len(i), 1)))
+        return np.concatenate(out).astype(np.float32)
 
     def flatten(self):
         """World-space triangle soup in global (mesh) order for the CPU restatement:

@@ -1256,6 +1256,14 @@ struct OLight {
     V3 Le;
 };
 
+struct OTexture {
+    int kind = KZ_TEX_CHECKER;
+    uint32_t w = 0, h = 0;
+    std::vector<float> rgb;
+    float scale_s = 1.f, scale_t = 1.f;
+    V3 Ca{1, 1, 1}, Cb{0, 0, 0};
+};
+
 struct OScene {
     OBvh bvh;
     std::vector<uint32_t> tri_geom;
@@ -1263,7 +1271,60 @@ struct OScene {
     std::vector<int32_t> geom_light;  // light index or -1
     std::vector<kz_material> materials;
     std::vector<OLight> lights;
+    std::vector<float> tri_uv;        // 6 floats per triangle (global order), or empty
+    std::vector<OTexture> textures;
+    V3 env{0, 0, 0};
+    int env_tex = -1;
 };
+
+// Texture lookup: the OSL checkerboard shader's rule, or bilinear filtering
+// with periodic wrap and texel centres at (i + 0.5) / w.
+V3 texture_lookup(const OTexture& t, float s, float u) {
+    if (!std::isfinite(s)) s = 0.f;
+    if (!std::isfinite(u)) u = 0.f;
+    if (t.kind == KZ_TEX_CHECKER) {
+        float cs = std::fmod(s * t.scale_s, 2.f), ct = std::fmod(u * t.scale_t, 2.f);
+        int a = std::isfinite(cs) ? (int)cs : 0, b = std::isfinite(ct) ? (int)ct : 0;
+        return (a ^ b) == 0 ? t.Ca : t.Cb;
+    }
+    s -= std::floor(s);
+    u -= std::floor(u);
+    float x = s * (float)t.w - 0.5f, y = u * (float)t.h - 0.5f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy;
+    uint32_t x0 = fx < 0.f ? t.w - 1 : std::min((uint32_t)fx, t.w - 1);
+    uint32_t y0 = fy < 0.f ? t.h - 1 : std::min((uint32_t)fy, t.h - 1);
+    uint32_t x1 = (x0 + 1) % t.w, y1 = (y0 + 1) % t.h;
+    auto px = [&](uint32_t xx, uint32_t yy) {
+        const float* p = &t.rgb[((size_t)yy * t.w + xx) * 3];
+        return V3(p[0], p[1], p[2]);
+    };
+    return (px(x0, y0) * (1.f - ax) + px(x1, y0) * ax) * (1.f - ay) + (px(x0, y1) * (1.f - ax) + px(x1, y1) * ax) * ay;
+}
+
+// The environment seen along d (latitude-longitude, +y up).
+V3 environment(const OScene& sc, V3 d) {
+    V3 e = sc.env;
+    if (sc.env_tex >= 0) {
+        float s = 0.5f + std::atan2(d.x, -d.z) * (0.5f * kInvPi);
+        float t = std::acos(std::min(std::max(d.y, -1.f), 1.f)) * kInvPi;
+        e = mul(e, texture_lookup(sc.textures[(size_t)sc.env_tex], s, t));
+    }
+    return e;
+}
+
+// Texture of a material: the one its lobes reference through
+// params[KZ_LOBE_TEXTURE_PARAM] = index + 1, or -1.
+int material_texture(const kz_material& m) {
+    for (uint32_t k = 0; k < std::min<uint32_t>(m.n_lobes, KZ_MAX_LOBES); ++k)
+        if (m.lobes[k].params[KZ_LOBE_TEXTURE_PARAM] != 0.f) return (int)m.lobes[k].params[KZ_LOBE_TEXTURE_PARAM] - 1;
+    return -1;
+}
+
+V3 weight_of(const kz_lobe& lb, int mtex, V3 tint) {
+    V3 w(lb.weight[0], lb.weight[1], lb.weight[2]);
+    return (mtex >= 0 && lb.params[KZ_LOBE_TEXTURE_PARAM] != 0.f) ? mul(w, tint) : w;
+}
 
 float tri_area(const OBvh& b, uint32_t tri) {
     V3 p0 = b.v(tri, 0), p1 = b.v(tri, 1), p2 = b.v(tri, 2);
@@ -1334,7 +1395,11 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         float t, bu, bv;
         uint32_t prim;
         pc.bounces++;
-        if (!sc.bvh.closest(o, d, kRayEps, std::numeric_limits<float>::infinity(), t, prim, bu, bv)) break;
+        if (!sc.bvh.closest(o, d, kRayEps, std::numeric_limits<float>::infinity(), t, prim, bu, bv)) {
+            // background shader on a miss, no MIS (integrator.cpp:545-552)
+            if (sc.env.x > 0.f || sc.env.y > 0.f || sc.env.z > 0.f) L = L + mul(beta, environment(sc, d));
+            break;
+        }
         float u[9];
         for (int k = 0; k < 9; ++k) u[k] = rng.nextf();
         const uint32_t geom = sc.tri_geom[prim];
@@ -1342,6 +1407,19 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         V3 v0 = sc.bvh.v(prim, 0), v1 = sc.bvh.v(prim, 1), v2 = sc.bvh.v(prim, 2);
         V3 Ng = normalize(cross(v1 - v0, v2 - v0));
         V3 P = o + d * t;
+        // texture tint at the hit's uv (vertex uvs interpolated by the hit's
+        // barycentrics; the barycentrics themselves for meshes without uvs)
+        const int mtex = sc.textures.empty() ? -1 : material_texture(mat);
+        V3 tint(1, 1, 1);
+        if (mtex >= 0) {
+            float b0 = 1.f - bu - bv;
+            float s0 = 0.f, t0 = 0.f, s1 = 1.f, t1 = 0.f, s2 = 0.f, t2 = 1.f;
+            if (!sc.tri_uv.empty()) {
+                const float* q = &sc.tri_uv[(size_t)prim * 6];
+                s0 = q[0]; t0 = q[1]; s1 = q[2]; t1 = q[3]; s2 = q[4]; t2 = q[5];
+            }
+            tint = texture_lookup(sc.textures[(size_t)mtex], b0 * s0 + bu * s1 + bv * s2, b0 * t0 + bu * t1 + bv * t2);
+        }
         Frame fr(Ng);
         V3 wi = -fr.to_local(d);
         // 1. emission on hit (front side only, single_emissive_surface)
@@ -1367,7 +1445,8 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         bool any_smooth = false;
         for (uint32_t i = 0; i < nlobes; ++i) {
             const kz_lobe& lb = mat.lobes[i];
-            lp[i] = (lb.weight[0] * beta.x + lb.weight[1] * beta.y + lb.weight[2] * beta.z) * winv;
+            V3 lw = weight_of(lb, mtex, tint);
+            lp[i] = (lw.x * beta.x + lw.y * beta.y + lw.z * beta.z) * winv;
             wsum += lp[i];
             if (!lobe_is_delta(lb.closure_id)) any_smooth = true;
         }
@@ -1400,7 +1479,7 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
                     const kz_lobe& lb = mat.lobes[i];
                     if (lobe_is_delta(lb.closure_id)) continue;
                     LobeEval e = eval_integrator(lb, wi, wo);
-                    f = f + mul(V3(lb.weight[0], lb.weight[1], lb.weight[2]), e.f);
+                    f = f + mul(weight_of(lb, mtex, tint), e.f);
                     bpdf += lp[i] * e.pdf;
                 }
                 if (!is_zero(f)) {
@@ -1438,7 +1517,7 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         V3 weight;
         float pdf_dir;
         if (smp.delta) {
-            weight = mul(V3(ls.weight[0], ls.weight[1], ls.weight[2]), smp.weight) * (1.f / lp[sel]);
+            weight = mul(weight_of(ls, mtex, tint), smp.weight) * (1.f / lp[sel]);
             pdf_dir = 0.f;
         } else {
             V3 f(0, 0, 0);
@@ -1447,7 +1526,7 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
                 const kz_lobe& lb = mat.lobes[i];
                 if (lobe_is_delta(lb.closure_id)) continue;
                 LobeEval e = eval_integrator(lb, wi, smp.wo);
-                f = f + mul(V3(lb.weight[0], lb.weight[1], lb.weight[2]), e.f);
+                f = f + mul(weight_of(lb, mtex, tint), e.f);
                 pdf += lp[i] * e.pdf;
             }
             if (!(pdf > 0.f)) break;
@@ -1630,6 +1709,30 @@ void* kzo_scene_create(const float* tri_verts, uint32_t ntris, const uint32_t* t
 }
 
 void kzo_scene_free(void* h) { delete static_cast<OScene*>(h); }
+
+// Textures, per-triangle vertex uvs (6 floats per triangle in global order,
+// NULL = barycentrics) and the environment of a restatement scene.
+void kzo_scene_set_textures(void* h, const kz_texture* tex, uint32_t n, const float* tri_uv, const float* env_rgb,
+                            int32_t env_tex) {
+    OScene* s = static_cast<OScene*>(h);
+    s->textures.clear();
+    for (uint32_t k = 0; k < n; ++k) {
+        OTexture t;
+        t.kind = tex[k].kind;
+        t.w = tex[k].width;
+        t.h = tex[k].height;
+        if (t.kind == KZ_TEX_IMAGE) t.rgb.assign(tex[k].rgb, tex[k].rgb + (size_t)t.w * t.h * 3);
+        t.scale_s = tex[k].scale_s;
+        t.scale_t = tex[k].scale_t;
+        t.Ca = V3(tex[k].Ca[0], tex[k].Ca[1], tex[k].Ca[2]);
+        t.Cb = V3(tex[k].Cb[0], tex[k].Cb[1], tex[k].Cb[2]);
+        s->textures.push_back(std::move(t));
+    }
+    if (tri_uv) s->tri_uv.assign(tri_uv, tri_uv + (size_t)s->bvh.ntris * 6);
+    else s->tri_uv.clear();
+    s->env = env_rgb ? V3(env_rgb[0], env_rgb[1], env_rgb[2]) : V3(0, 0, 0);
+    s->env_tex = env_tex;
+}
 
 // Renders rows [row_begin, row_end) of a W x H frame; out: W*H*3 doubles
 // (spp average, FP64 accumulation); stats[0] = path bounces, stats[1] = shadow rays.

@@ -48,6 +48,7 @@ def lib():
             "kzo_furnace_fixed_beckmann": (C.c_double, [C.c_float, C.c_float]),
             "kzo_scene_create": (_P, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, _P, C.c_uint32]),
             "kzo_scene_free": (None, [_P]),
+            "kzo_scene_set_textures": (None, [_P, _P, C.c_uint32, _P, _P, C.c_int32]),
             "kzo_render": (None, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(RenderConfig), C.c_int,
                                   C.c_uint32, C.c_uint32, _P, _P]),
             "kzo_camera_rays": (None, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P]),
@@ -177,7 +178,19 @@ class Scene:
     @classmethod
     def from_desc(cls, desc):
         tv, tg, gm, gl = desc.flatten()
-        return cls(tv, tg, gm, gl, desc.material_array())
+        sc = cls(tv, tg, gm, gl, desc.material_array())
+        textures = getattr(desc, "textures", [])
+        env = np.ascontiguousarray(getattr(desc, "env", (0, 0, 0)), np.float32)
+        if textures or env.any():
+            recs = [t.to_c() for t in textures]
+            sc._keep = [k for _, k in recs]
+            arr = (type(recs[0][0]) * len(recs))(*[r for r, _ in recs]) if recs else None
+            uv = desc.tri_uvs()
+            sc._uv = None if uv is None else np.ascontiguousarray(uv, np.float32)
+            sc._env = env
+            lib().kzo_scene_set_textures(sc.h, C.cast(arr, C.c_void_p) if arr is not None else None, len(recs),
+                                         _p(sc._uv), _p(env), int(getattr(desc, "env_texture", -1)))
+        return sc
 
     def __del__(self):
         if getattr(self, "h", None):

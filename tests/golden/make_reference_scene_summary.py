@@ -38,10 +38,16 @@ def main():
         for name, m in zip(L.material_names, d.materials):
             mats[name] = {"Le": [round(float(x), 6) for x in m["Le"]],
                           "lobes": [CLOSURES.get(int(l["closure_id"]), int(l["closure_id"]))
+                                    + (f"@texture{int(l['params'][N.KZ_LOBE_TEXTURE_PARAM]) - 1}"
+                                       if l["params"][N.KZ_LOBE_TEXTURE_PARAM] else "")
                                     for l in m["lobes"][:int(m["n_lobes"])]]}
         out[rel] = {"loaded": True, "film": [d.width, d.height], "mirror_x": L.mirror_x,
                     "integrator": L.integrator, "meshes": len(d.meshes), "triangles": int(d.n_triangles()),
-                    "lights": int(sum(1 for m in d.meshes if m[3])), "materials": mats, "warnings": L.warnings}
+                    "lights": int(sum(1 for m in d.meshes if m[3])), "materials": mats, "warnings": L.warnings,
+                    "textures": [("checker" if t.kind == N.KZ_TEX_CHECKER else "image %dx%d" % t.image.shape[1::-1])
+                                 for t in d.textures],
+                    "environment": {"rgb": [round(float(x), 6) for x in d.env], "texture": d.env_texture},
+                    "meshes_with_uv": len(d.uvs)}
     dst = os.path.join(HERE, "reference_scenes_summary.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)

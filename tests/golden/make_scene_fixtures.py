@@ -4,7 +4,9 @@ written here from scratch (the reference's own scene files are not copied).
 They exercise what kazen_proto_gb300.scene_xml reads: Film, Camera with a
 mirroring scale, shader groups with parameters, Mesh with translate / rotate
 / scale, Triangle and Quad elements, an area light, and the lowering of
-diffuse, mirror, dielectric, microfacet mixture and emitter shaders.
+diffuse, mirror, dielectric, microfacet mixture and emitter shaders
+(box_room); a shader network, image textures, OBJ texture coordinates, a
+Sphere and an environment map (textured_room).
 
 Run: python tests/golden/make_scene_fixtures.py
 """
@@ -16,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
+from kazen_proto_gb300 import film_io  # noqa: E402
 from kazen_proto_gb300.scenes import icosphere  # noqa: E402
 
 OUT = os.path.join(HERE, "scenes", "box_room")
@@ -118,6 +121,76 @@ SCENE = '''<Scene>
 '''
 
 
+TEX_SHADERS = {
+    "checkerboard": """shader checkerboard (
+    float s = u, float t = v, float scale_s = 4, float scale_t = 4,
+    color Ca = color(1, 1, 1), color Cb = color(0, 0, 0),
+    output color Cout = 0)
+{
+    // alternate Ca and Cb over the (s, t) grid
+    float cs = fmod(s * scale_s, 2);
+    float ct = fmod(t * scale_t, 2);
+    if ((int(cs) ^ int(ct)) == 0) Cout = Ca; else Cout = Cb;
+}
+""",
+    "matte": """surface matte ( color Cs = 0.5 )
+{
+    Ci = Cs * diffuse(N);
+}
+""",
+    "painted": """surface painted ( string filename = "paint.png", float gloss = 0.2 )
+{
+    color c = texture(filename, u, v);
+    Ci = 0.8 * c * kp_principle_diffuse(N) + gloss * kp_principle_clearcoat(N, 0.1);
+}
+""",
+    "lamp": SHADERS["lamp"],
+    "env": """shader env ( string filename = "" )
+{
+    Ci = color(environment(filename, I)) * background();
+}
+""",
+}
+
+TEX_SCENE = '''<Scene>
+    <Film width="int 64" height="int 48"/>
+    <Camera position="float3 0.5 0.45 2.2" lookat="float3 0.5 0.3 0.5" up="float3 0 1 0" fov="float 45"/>
+    <EnvironmentBegin/>
+        <Shader name="env" layer="e0">
+            <Parameter filename="string sky.pfm"/>
+        </Shader>
+    <EnvironmentEnd/>
+    <Materials>
+        <ShaderGroupBegin name="checker_floor"/>
+            <Shader name="checkerboard" layer="l0">
+                <Parameter scale_s="float 8"/>
+                <Parameter scale_t="float 8"/>
+                <Parameter Ca="float3 0.8 0.8 0.75"/>
+                <Parameter Cb="float3 0.15 0.15 0.2"/>
+            </Shader>
+            <Shader name="matte" layer="l1"/>
+            <ConnectShaders srclayer="l0" srcparam="Cout" dstlayer="l1" dstparam="Cs"/>
+        <ShaderGroupEnd/>
+        <ShaderGroupBegin name="painted"/>
+            <Shader name="painted" layer="l2"/>
+        <ShaderGroupEnd/>
+        <ShaderGroupBegin name="light"/>
+            <Shader name="lamp" layer="l3">
+                <Parameter Cs="float3 6 5 4"/>
+            </Shader>
+        <ShaderGroupEnd/>
+    </Materials>
+    <Objects>
+        <Quad center="float3 0.5 0 0.5" dir="float3 0 1 0" vertical_vec="float3 0 0 1" half_width="float 0.8" half_height="float 0.8" shader_name="string checker_floor"/>
+        <Sphere center_n_radius="float4 0.5 0.25 0.5 0.25" shader_name="string painted"/>
+        <Mesh filename="string meshes/panel.obj" shader_name="painted" translate="func_translate 0.1 0 0.2"/>
+        <Quad center="float3 0.5 1.2 0.5" dir="float3 0 -1 0" vertical_vec="float3 0 0 1" half_width="float 0.2" half_height="float 0.2" shader_name="string light" is_light="bool true"/>
+    </Objects>
+    <PathIntegrator/>
+</Scene>
+'''
+
+
 def write_obj(path, verts, faces, comment):
     with open(path, "w") as f:
         f.write(f"# {comment}\n")
@@ -153,6 +226,35 @@ def main():
     sv, sf = icosphere(2)
     write_obj(os.path.join(OUT, "meshes", "ball.obj"), sv, (np.asarray(sf) + 1).tolist(), "icosphere, 320 faces")
     print("wrote", OUT)
+    write_textured_room()
+
+
+def write_textured_room():
+    """A textured room: a checkerboard shader network on the floor, an image
+    texture on a sphere and on an OBJ panel with its own texture coordinates,
+    and an environment map seen where the room is open."""
+    out = os.path.join(HERE, "scenes", "textured_room")
+    os.makedirs(os.path.join(out, "meshes"), exist_ok=True)
+    for name, src in TEX_SHADERS.items():
+        with open(os.path.join(out, name + ".osl"), "w") as f:
+            f.write(src)
+    with open(os.path.join(out, "scene.xml"), "w") as f:
+        f.write(TEX_SCENE)
+    # paint.png: 32 x 24 stripes and a gradient; sky.pfm: 16 x 8 sky with a bright band
+    y, x = np.mgrid[0:24, 0:32]
+    paint = np.stack([(x % 8 < 4) * 0.8 + 0.1, y / 23.0, 0.5 + 0.4 * np.sin(x / 5.0)], -1)
+    film_io.write_png(os.path.join(out, "paint.png"), paint)
+    sy, sx = np.mgrid[0:8, 0:16]
+    sky = np.stack([0.3 + 0.1 * sx / 15, 0.4 + 0.05 * sy, 1.2 - 0.1 * sy], -1) * (1 + 4 * (sy == 2))[:, :, None]
+    film_io.write_pfm(os.path.join(out, "sky.pfm"), sky.astype(np.float32))
+    with open(os.path.join(out, "meshes", "panel.obj"), "w") as f:
+        f.write("# upright panel with texture coordinates (vertex 2 carries two)\n")
+        for v in [(0, 0, 0), (0.3, 0, 0), (0.3, 0.5, 0), (0, 0.5, 0)]:
+            f.write("v %g %g %g\n" % v)
+        for t in [(0, 0), (2, 0), (2, 3), (0, 3), (1, 1)]:
+            f.write("vt %g %g\n" % t)
+        f.write("f 1/1 2/2 3/3\nf 1/1 3/5 4/4\n")
+    print("wrote", out)
 
 
 if __name__ == "__main__":

@@ -158,6 +158,38 @@ def test_reference_shader_library_render(gpu, oracle_mod):
     assert rel_mse(img, ref) <= REL_MSE_TOL
 
 
+def test_textures_and_environment_render(gpu, oracle_mod):
+    """Checkerboard-textured walls (uv = barycentrics), an image-textured box
+    with explicit uvs, a lobe pair sharing one texture next to an untextured
+    lobe, and a latitude-longitude environment seen through the open side of
+    the box, against the restatement."""
+    rng = np.random.default_rng(8)
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    img = rng.random((13, 17, 3)).astype(np.float32)
+    sky = (rng.random((8, 16, 3)) * 3).astype(np.float32)
+    d.textures = [api.checker_texture(4, 3, (0.9, 0.9, 0.9), (0.1, 0.2, 0.3)), api.image_texture(img),
+                  api.image_texture(sky)]
+    d.materials[2] = api.material([api.textured(api.diffuse((0.8, 0.8, 0.8)), 0)])
+    d.materials[3] = api.material([api.textured(api.principle_diffuse((0.7, 0.7, 0.7)), 1),
+                                   api.textured(api.principle_retro(0.5, (0.2, 0.2, 0.2)), 1),
+                                   api.conductor_ggx((0.9, 0.6, 0.5), 0.3, weight=(0.3, 0.3, 0.3))])
+    d.env, d.env_texture = (0.5, 0.6, 0.7), 2
+    # explicit uvs on the metal box (mesh 6): its vertex positions, scaled
+    v = d.meshes[6][0]
+    d.uvs[6] = (v[:, [0, 2]] * 3.0 - 0.5).astype(np.float32)
+    d.camera = api.Camera(eye=(0.5, 0.5, -1.0), lookat=(0.5, 0.4, 0.5), up=(0, 1, 0), fov=70.0)
+    s = d.build()
+    img_g = api.Renderer(spp=8, max_depth=6, seed=7).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=7)
+    assert np.isfinite(img_g).all()
+    assert rel_mse(img_g, ref) <= REL_MSE_TOL
+    # the environment and the textures change the image
+    d2 = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    d2.camera = d.camera
+    plain = api.Renderer(spp=8, max_depth=6, seed=7).render(d2.build(), d.camera, 40, 40)
+    assert rel_mse(img_g, plain) > 1e-2
+
+
 def test_terrain_scene_small(gpu, oracle_mod):
     d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
     s = d.build()

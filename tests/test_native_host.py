@@ -46,10 +46,11 @@ def test_struct_layouts_match_header():
     assert C.sizeof(N.KzMaterial) == 16 + 8 * 64
     assert N.RAY_DTYPE.itemsize == 32
     assert C.sizeof(N.KzBatchConfig) == 24
+    assert C.sizeof(N.KzTexture) == 56
 
 
 def test_abi_version_and_device_query(native_lib):
-    assert native_lib.kz_abi_version() == 2
+    assert native_lib.kz_abi_version() == 3
     assert native_lib.kz_device_count() >= 0
 
 
@@ -118,3 +119,39 @@ def test_material_lowering_of_shipped_shaders():
     assert rough["n_lobes"] == 2 and rough["lobes"][1]["closure_id"] == N.KZ_CLOSURE_KP_GLOSS
     assert rough["lobes"][1]["params"][0] == N.KZ_DIST_BECKMANN
     assert area["n_lobes"] == 0 and area["Le"][0] == 1.0
+
+
+def test_texture_validation_on_host(native_lib):
+    s = api.Scene()
+    g = s.add_mesh(np.eye(3, dtype=np.float32), [[0, 1, 2]], material_id=0)
+    with pytest.raises(N.KazenError):  # uv count must match the vertices
+        s.set_mesh_uvs(g, np.zeros((2, 2), np.float32))
+    with pytest.raises(N.KazenError):  # non-finite uv
+        s.set_mesh_uvs(g, np.array([[0, 0], [1, np.nan], [0, 1]], np.float32))
+    with pytest.raises(N.KazenError):  # no such mesh
+        s.set_mesh_uvs(5, np.zeros((3, 2), np.float32))
+    s.set_mesh_uvs(g, np.zeros((3, 2), np.float32))
+    with pytest.raises(N.KazenError):  # image without pixels
+        s.set_textures([api.Texture(N.KZ_TEX_IMAGE, np.zeros((0, 4, 3), np.float32))])
+    with pytest.raises(N.KazenError):  # non-finite texel
+        s.set_textures([api.image_texture(np.full((2, 2, 3), np.inf, np.float32))])
+    with pytest.raises(N.KazenError):  # unknown kind
+        s.set_textures([api.Texture(7)])
+    with pytest.raises(N.KazenError):
+        s.set_environment((-1, 0, 0))
+    s.set_textures([api.checker_texture()])
+    # a lobe naming texture 2 of 1, and two textures in one material, fail at build
+    s.set_materials([api.material([api.textured(api.diffuse(), 1)])])
+    with pytest.raises(N.KazenError) as e:
+        s.build_bvh()
+    assert e.value.code == N.KZ_ERR_INVALID_ARG and "texture" in str(e.value)
+    s.set_textures([api.checker_texture(), api.checker_texture(2, 2)])
+    s.set_materials([api.material([api.textured(api.diffuse(), 0), api.textured(api.phong(), 1)])])
+    with pytest.raises(N.KazenError) as e:
+        s.build_bvh()
+    assert "one per material" in str(e.value)
+    s.set_materials([api.material([api.diffuse()])])
+    s.set_environment((1, 1, 1), 5)
+    with pytest.raises(N.KazenError) as e:
+        s.build_bvh()
+    assert "environment texture" in str(e.value)

@@ -88,7 +88,8 @@ def test_emission_and_rejections():
     r = L.lower("surface e ( color c = 2, float k = 3 ) { Ci = c * k * kp_emitter(0.5) + emission(); }")
     assert not r.lobes and np.allclose(r.Le, 7.0)
     for bad in ("surface b () { Ci = diffuse(N) * P; }",                     # position-dependent global
-                "surface b () { Ci = texture(\"x.png\", u, v) * diffuse(N); }",  # texture lookup
+                "surface b () { Ci = texture(\"x.png\", u * 2, v) * diffuse(N); }",  # texture at moved uvs
+                "surface b () { Ci = (texture(\"x.png\", u, v) + 0.1) * diffuse(N); }",  # texture arithmetic
                 "surface b () { for (int i = 0; i < 2; i += 1) Ci = diffuse(N); }",
                 "surface b () { Ci = diffuse(N) + 1; }",                       # closure + non-zero number
                 "surface b () { Ci = kp_standard_dipole(N, color(1), color(1)); }",  # BSSRDF

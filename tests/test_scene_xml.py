@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from kazen_proto_gb300 import _native as N
+from kazen_proto_gb300 import film_io
 from kazen_proto_gb300 import scene_xml as X
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -122,10 +123,106 @@ def test_loader_errors(tmp_path):
         X.load(scene(cam + group + '<Objects><Mesh filename="string t.obj" shader_name="x"/></Objects>'))
     with pytest.raises(ValueError):  # no camera
         X.load(scene(group + '<Objects><Mesh filename="string t.obj" shader_name="m"/></Objects>'))
-    two = ('<Materials><ShaderGroupBegin name="m"/><Shader name="matte" layer="a"/>'
-           '<Shader name="matte" layer="b"/><ShaderGroupEnd/></Materials>')
-    with pytest.raises(ValueError):  # shader networks are not lowered
-        X.load(scene(cam + two))
+    bad_link = ('<Materials><ShaderGroupBegin name="m"/><Shader name="matte" layer="a"/>'
+                '<ConnectShaders srclayer="z" srcparam="Cout" dstlayer="a" dstparam="Cs"/>'
+                '<ShaderGroupEnd/></Materials>')
+    with pytest.raises(ValueError):  # a connection from a layer that does not exist
+        X.load(scene(cam + bad_link))
     L = X.load(scene(cam + group + '<Objects><Mesh filename="string t.obj" shader_name="m" is_light="bool false"/>'
                      '<PointLight/></Objects><WhittedIntegrator/>'))
     assert L.desc.meshes[0][3] is False and len(L.warnings) == 2
+
+
+CHECKER_OSL = """shader checkerboard (
+    float s = u, float t = v, float scale_s = 4, float scale_t = 4,
+    color Ca = color(1, 1, 1), color Cb = color(0, 0, 0),
+    output color Cout = 0)
+{
+    // the parity rule of OSL's checkerboard example
+    float cs = fmod(s * scale_s, 2);
+    float ct = fmod(t * scale_t, 2);
+    if ((int(cs) ^ int(ct)) == 0) Cout = Ca; else Cout = Cb;
+}
+"""
+
+
+def _scene_dir(tmp_path, shaders, materials, objects, extra=""):
+    for name, src in shaders.items():
+        (tmp_path / (name + ".osl")).write_text(src)
+    (tmp_path / "s.xml").write_text(
+        '<Scene><Camera position="float3 0 0 5" lookat="float3 0 0 0" up="float3 0 1 0" fov="float 30"/>'
+        + extra + "<Materials>" + materials + "</Materials><Objects>" + objects + "</Objects></Scene>")
+    return str(tmp_path / "s.xml")
+
+
+def test_checkerboard_network_becomes_a_texture(tmp_path):
+    mats = ('<ShaderGroupBegin name="c"/><Shader name="checkerboard" layer="l0">'
+            '<Parameter scale_s="float 20"/><Parameter Ca="float3 0.1 0.1 0.1"/></Shader>'
+            '<Shader name="matte" layer="l1"><Parameter Cs="float3 0.6 0.6 0.6"/></Shader>'
+            '<ConnectShaders srclayer="l0" srcparam="Cout" dstlayer="l1" dstparam="Cs"/><ShaderGroupEnd/>')
+    p = _scene_dir(tmp_path, {"checkerboard": CHECKER_OSL,
+                              "matte": "surface matte ( color Cs = 1 ) { Ci = 0.5 * Cs * diffuse(N); }"},
+                   mats, '<Triangle verta="float3 0 0 0" vertb="float3 1 0 0" vertc="float3 0 1 0" shader_name="c"/>')
+    L = X.load(p)
+    t = L.desc.textures
+    assert len(t) == 1 and t[0].kind == N.KZ_TEX_CHECKER and (t[0].scale_s, t[0].scale_t) == (20.0, 4.0)
+    assert np.allclose(t[0].Ca, 0.1) and np.allclose(t[0].Cb, 0.0)
+    lb = L.desc.materials[0]["lobes"][0]
+    assert lb["closure_id"] == N.KZ_CLOSURE_DIFFUSE and np.allclose(lb["weight"], 0.5)
+    assert lb["params"][N.KZ_LOBE_TEXTURE_PARAM] == 1
+
+
+def test_image_texture_uvs_and_environment(tmp_path):
+    rng = np.random.default_rng(3)
+    img = rng.random((5, 7, 3)).astype(np.float32)
+    film_io.write_pfm(str(tmp_path / "tex.pfm"), img)
+    film_io.write_pfm(str(tmp_path / "sky.pfm"), img[::-1])
+    (tmp_path / "m.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nvt 0 0\nvt 1 0\nvt 0 1\nvt 1 1\nvt 0.5 0.5\n"
+                                    "f 1/1 2/2 3/3\nf 2/5 4/4 3/3\n")
+    shaders = {"tm": 'surface tm ( string filename = "tex.pfm" ) { color c = texture(filename, u, v); '
+                     'Ci = c * diffuse(N) + 0.2 * kp_mirror(); }',
+               "env": 'shader env ( string filename = "" ) { Ci = 2 * color(environment(filename, I)) * background(); }'}
+    mats = '<ShaderGroupBegin name="t"/><Shader name="tm" layer="a"/><ShaderGroupEnd/>'
+    env = '<EnvironmentBegin/><Shader name="env" layer="e"><Parameter filename="string sky.pfm"/></Shader><EnvironmentEnd/>'
+    L = X.load(_scene_dir(tmp_path, shaders, mats, '<Mesh filename="string m.obj" shader_name="t"/>'
+                          '<Quad center="float3 0 0 0" dir="float3 0 0 1" vertical_vec="float3 0 1 0" half_width="float 1"'
+                          ' half_height="float 1" shader_name="t"/>', env))
+    d = L.desc
+    assert [t.kind for t in d.textures] == [N.KZ_TEX_IMAGE, N.KZ_TEX_IMAGE]
+    assert np.array_equal(d.textures[0].image, img) and np.array_equal(d.textures[1].image, img[::-1])
+    assert d.env == (2.0, 2.0, 2.0) and d.env_texture == 1
+    m = d.materials[0]["lobes"]
+    assert m[0]["params"][N.KZ_LOBE_TEXTURE_PARAM] == 1 and m[1]["params"][N.KZ_LOBE_TEXTURE_PARAM] == 0
+    # the OBJ vertex 2 carries two uvs, so it is split: 5 (position, uv) pairs
+    v, t = d.meshes[0][0], d.meshes[0][1]
+    uv = d.uvs[0]
+    assert len(v) == 5 and len(uv) == 5
+    corner = {tuple(np.round(v[i], 3)) + tuple(np.round(uv[i], 3)) for i in t.reshape(-1)}
+    assert (1.0, 0.0, 0.0, 0.5, 0.5) in corner and (1.0, 0.0, 0.0, 1.0, 0.0) in corner
+    assert np.allclose(d.uvs[1], [[0, 0], [1, 0], [1, 1], [0, 1]])
+    # an empty environment file name is black
+    env0 = '<EnvironmentBegin/><Shader name="env" layer="e"><Parameter filename=""/></Shader><EnvironmentEnd/>'
+    L0 = X.load(_scene_dir(tmp_path, shaders, mats, '<Mesh filename="string m.obj" shader_name="t"/>', env0))
+    assert L0.desc.env == (0.0, 0.0, 0.0) and L0.desc.env_texture == -1
+
+
+def test_sphere_uv_has_no_wrapped_triangles():
+    v, f, uv = X.sphere_mesh(np.zeros(3), 1.0, level=3)
+    span = uv[f][:, :, 0].max(1) - uv[f][:, :, 0].min(1)
+    assert span.max() < 0.5 and len(v) == 3 * len(f)
+    assert uv[:, 1].min() >= 0.5 and uv[:, 1].max() <= 1.5
+
+
+def test_textured_fixture():
+    L = X.load(os.path.join(os.path.dirname(FIXTURE), "..", "textured_room", "scene.xml"))
+    d = L.desc
+    assert [t.kind for t in d.textures] == [N.KZ_TEX_CHECKER, N.KZ_TEX_IMAGE, N.KZ_TEX_IMAGE]
+    assert d.env_texture == 2 and d.env == (1.0, 1.0, 1.0)
+    assert d.textures[1].image.shape == (24, 32, 3) and d.textures[2].image.shape == (8, 16, 3)
+    ids = [(int(l["closure_id"]), int(l["params"][N.KZ_LOBE_TEXTURE_PARAM]))
+           for m in d.materials for l in m["lobes"][:m["n_lobes"]]]
+    # the painted group's lobes reference paint.png (texture 1 of the scene);
+    # the environment map (sky.pfm) joins the table after the materials'
+    assert ids == [(N.KZ_CLOSURE_DIFFUSE, 1), (N.KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE, 2),
+                   (N.KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT, 0)]
+    assert sorted(d.uvs) == [0, 1, 2, 3]
