@@ -15,9 +15,10 @@ GPU renderer:
     concepts.Film (tiles, generate_tiles, write_tiles, ...), concepts.Tile
 
 Differences, each stated where it happens: shaders are lowered from their
-OSL source (load_oso_shader looks for name.osl, not the compiled .oso) and
-shader networks are not supported; add_point_light and connect_shader raise;
-spheres are tessellated; every integrator type renders with the path
+OSL source (load_oso_shader looks for name.osl, not the compiled .oso; shader
+networks and texture lookups lower as scene_xml lowers them, texture files
+relative to the working directory); add_point_light raises; spheres are
+tessellated (with the reference's parametric uv); every integrator type renders with the path
 integrator; the frame renders in one GPU call and on_tile_end then runs for
 each tile in tile order; tiles cover the film exactly (the reference's
 generate_tiles, film.cpp:66-78, gives the last row and column the nominal
@@ -36,7 +37,7 @@ import numpy as np
 
 from . import api as _api
 from . import film_io, scene_xml
-from .scenes import SceneDesc, icosphere
+from .scenes import SceneDesc
 
 
 class AcceleratorType(enum.Enum):
@@ -136,7 +137,8 @@ class Scene:
         self.warnings: list[str] = []
         self._search = []
         self._groups: dict[str, int] = {}
-        self._group = None          # (name, shader name, params, shader search dir)
+        self._group = None          # [name, [(shader, layer, params, source path)], connections]
+        self._tex = scene_xml.TextureTable(os.getcwd())
         self._built = None          # the GPU scene after build_bvh
         self._mirror_x = False
 
@@ -177,24 +179,27 @@ class Scene:
         self._search = [p for p in path.split(":") if p]
 
     def begin_shader_group(self, name: str) -> None:
-        self._group = [name, None, {}, None]
+        self._group = [name, [], []]
+        self._pending = {}
 
     def load_oso_shader(self, kind: str, name: str, layer: str, lib_path: str) -> bool:
         if self._group is None:
             raise RuntimeError("load_oso_shader outside a shader group")
-        if self._group[1] is not None:
-            raise NotImplementedError("shader networks (several shaders per group) are not supported")
         for d in [lib_path] + self._search:
             src = os.path.join(d, name + ".osl")
             if os.path.exists(src):
-                self._group[1], self._group[3] = name, src
+                self._group[1].append((name, layer, self._pending, src))
+                self._pending = {}
                 return True
         raise FileNotFoundError(f"no OSL source {name}.osl in {[lib_path] + self._search} (needed to lower it)")
 
     def _param(self, name, value):
+        """A parameter of the next shader loaded in the group, as OSL's
+        Parameter() calls precede their Shader() (scene.cpp:631, 316);
+        parameters set after the group's last shader apply to that shader."""
         if self._group is None:
             raise RuntimeError("shader parameter outside a shader group")
-        self._group[2][name] = value
+        self._pending[name] = value
 
     def set_shader_param_bool(self, name, value): self._param(name, bool(value))
     def set_shader_param_int(self, name, value): self._param(name, int(value))
@@ -205,14 +210,25 @@ class Scene:
     def set_shader_param_ustr(self, name, value): self._param(name, str(value))
 
     def connect_shader(self, src_layer, src_param, dst_layer, dst_param):
-        raise NotImplementedError("shader networks (connect_shader) are not supported")
+        if self._group is None:
+            raise RuntimeError("connect_shader outside a shader group")
+        self._group[2].append((src_layer, src_param, dst_layer, dst_param))
 
     def end_shader_group(self) -> None:
-        name, shader, params, src = self._group
-        if shader is None:
+        name, shaders, conns = self._group
+        if not shaders:
             raise RuntimeError(f"shader group {name!r} has no shader")
-        with open(src) as f:
-            self.desc.materials.append(scene_xml.lower_shader(f.read(), params))
+        shaders[-1][2].update(self._pending)
+        self._pending = {}
+        paths = {sname: src for sname, _, _, src in shaders}
+
+        def source(sname):
+            with open(paths[sname]) as f:
+                return f.read()
+        r = scene_xml.lower_group("", [(a, b, c) for a, b, c, _ in shaders], conns, source)
+        self.warnings += [f"shader group {name!r}: {w}" for w in r.warnings]
+        self.desc.materials.append(self._tex.material(r))
+        self.desc.textures = self._tex.textures
         self._groups[name] = len(self.desc.materials) - 1
         self._group = None
 
@@ -223,8 +239,11 @@ class Scene:
 
     # -- geometry
     def add_mesh(self, world, vs, ns, ts, idx, name: str, shader_name: str, is_light: bool = False) -> None:
+        """ts: per-vertex texture coordinates (or None / empty: uv = barycentrics)."""
         v = scene_xml.apply_transform(_world(world), np.asarray(vs, np.float64).reshape(-1, 3))
-        self.desc.add(v, np.asarray(idx, np.uint32).reshape(-1, 3), self._material(shader_name), bool(is_light))
+        uv = None if ts is None or len(ts) == 0 else np.asarray(ts, np.float32).reshape(-1, 2)
+        self.desc.add(v, np.asarray(idx, np.uint32).reshape(-1, 3), self._material(shader_name), bool(is_light),
+                      uv=uv)
 
     def add_triangle(self, world, a, b, c, name: str, shader_name: str, is_light: bool = False) -> None:
         self.add_mesh(world, [a, b, c], None, None, [[0, 1, 2]], name, shader_name, is_light)
@@ -236,12 +255,13 @@ class Scene:
         hv /= np.linalg.norm(hv)
         c = np.asarray(c, np.float64)
         q = [c - hv * w - up * h, c + hv * w - up * h, c + hv * w + up * h, c - hv * w + up * h]
-        self.add_mesh(world, q, None, None, [[0, 1, 2], [0, 2, 3]], name, shader_name, is_light)
+        self.add_mesh(world, q, None, [[0, 0], [1, 0], [1, 1], [0, 1]], [[0, 1, 2], [0, 2, 3]], name, shader_name,
+                      is_light)
 
     def add_sphere(self, world, p, r: float, name: str, shader_name: str, is_light: bool = False) -> None:
-        sv, sf = icosphere(4)
-        self.add_mesh(world, sv * float(r) + np.asarray(p, np.float64), None, None, sf, name, shader_name, is_light)
-        self.warnings.append(f"sphere {name!r} tessellated to {len(sf)} triangles")
+        v, f, uv = scene_xml.sphere_mesh(np.asarray(p, np.float64), float(r))
+        self.add_mesh(world, v, None, uv, f, name, shader_name, is_light)
+        self.warnings.append(f"sphere {name!r} tessellated to {len(f)} triangles")
 
     def add_point_light(self, radiance, position, shader_name) -> None:
         raise NotImplementedError("point lights are not supported on the GPU path")

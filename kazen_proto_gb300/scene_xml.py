@@ -199,10 +199,13 @@ def shader_source(base: str, name: str) -> str:
         return f.read()
 
 
-def lower_group(base: str, shaders, connections):
-    """Evaluate a shader group: each layer in order, <ConnectShaders> feeding
+def lower_group(base: str, shaders, connections, source=None):
+    """Evaluate a shader group: each layer (shader name, layer name, params)
+    in order, connections (src layer, src param, dst layer, dst param) feeding
     an upstream output parameter into a downstream input; the last layer's
-    closures are the group's (OSL's group semantics). Returns osl_lower.Lowered."""
+    closures are the group's (OSL's group semantics). `source(name)` returns
+    a shader's OSL text (default: shader_source beside `base`). Returns
+    osl_lower.Lowered."""
     outputs, last = {}, None
     for sname, layer, params in shaders:
         ov = dict(params)
@@ -211,7 +214,7 @@ def lower_group(base: str, shaders, connections):
                 if sl not in outputs or sp not in outputs[sl]:
                     raise ValueError(f"connection from {sl}.{sp}: no such earlier layer output")
                 ov[dp] = outputs[sl][sp]
-        src = shader_source(base, sname)
+        src = source(sname) if source else shader_source(base, sname)
         if sname == "checkerboard":
             _, p = osl_lower.shader_params(src, ov)
             outputs[layer] = {"Cout": osl_lower.checkerboard_output(p)}

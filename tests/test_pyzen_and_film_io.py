@@ -86,10 +86,9 @@ def test_unsupported_calls_raise():
     with pytest.raises(FileNotFoundError):
         s.load_oso_shader("surface", "no_such_shader", "l", FIXTURE_DIR)
     s.load_oso_shader("surface", "matte", "l", FIXTURE_DIR)
-    with pytest.raises(NotImplementedError):
-        s.load_oso_shader("surface", "matte", "l2", FIXTURE_DIR)
-    with pytest.raises(NotImplementedError):
-        s.connect_shader("l", "Cout", "l2", "Cs")
+    s.connect_shader("z", "Cout", "l", "Cs")  # from a layer that does not exist
+    with pytest.raises(ValueError):
+        s.end_shader_group()
     with pytest.raises(NotImplementedError):
         s.add_point_light((1, 1, 1), (0, 0, 0), "g")
     with pytest.raises(KeyError):
@@ -147,3 +146,27 @@ def test_image_writers(tmp_path):
 
     with pytest.raises(ValueError):
         film_io.write_image(str(tmp_path / "a.jpg"), img)
+
+
+def test_shader_network_and_uvs(tmp_path):
+    """A checkerboard layer connected into a matte layer (parameters before
+    their shader, as OSL orders them), texcoords on add_mesh, the sphere's
+    parametric uv."""
+    (tmp_path / "checkerboard.osl").write_text(
+        "shader checkerboard ( float s = u, float t = v, float scale_s = 4, float scale_t = 4,"
+        " color Ca = 1, color Cb = 0, output color Cout = 0 ) { Cout = Ca; }")
+    (tmp_path / "matte.osl").write_text("surface matte ( color Cs = 1 ) { Ci = Cs * diffuse(N); }")
+    s = pyzen.api.Scene()
+    s.set_shader_search_path(str(tmp_path))
+    s.begin_shader_group("checker")
+    s.set_shader_param_float("scale_s", 10.0)
+    assert s.load_oso_shader("shader", "checkerboard", "tex", "")
+    assert s.load_oso_shader("surface", "matte", "m", "")
+    s.connect_shader("tex", "Cout", "m", "Cs")
+    s.end_shader_group()
+    d = s.desc
+    assert len(d.textures) == 1 and d.textures[0].kind == N.KZ_TEX_CHECKER and d.textures[0].scale_s == 10.0
+    assert d.materials[0]["lobes"][0]["params"][N.KZ_LOBE_TEXTURE_PARAM] == 1
+    s.add_mesh(None, [(0, 0, 0), (1, 0, 0), (0, 1, 0)], [], [(0, 0), (2, 0), (0, 2)], [(0, 1, 2)], "t", "checker")
+    s.add_sphere(None, (0, 0, 0), 1.0, "ball", "checker")
+    assert np.allclose(d.uvs[0], [[0, 0], [2, 0], [0, 2]]) and len(d.uvs[1]) == len(d.meshes[1][0])
