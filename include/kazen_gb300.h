@@ -260,6 +260,13 @@ kz_status kz_scene_set_mesh_uvs(kz_scene* scene, int32_t geom_id, const float* u
  * texture `texture` (-1: none) looked up in latitude-longitude form,
  * s = 0.5 + atan2(d.x, -d.z) / (2 pi), t = acos(d.y) / pi. Default black. */
 kz_status kz_scene_set_environment(kz_scene* scene, const float rgb[3], int32_t texture);
+/* A point light (PointLight, src/core/light.cpp:18-36): next-event estimation
+ * picks it like any light (uniformly among all lights, area lights first in
+ * mesh order, then point lights in the order added) and it contributes
+ * radiance / (0.1 |d|^2), the falloff PointLight::sample returns, without MIS
+ * (nothing can hit it). Host pointers; call before kz_scene_build. */
+kz_status kz_scene_add_point_light(kz_scene* scene, const float position[3], const float radiance[3],
+                                   int32_t* out_light_id);
 /* Builds the BVH and uploads geometry, materials, textures and the light table. */
 kz_status kz_scene_build(kz_scene* scene);
 kz_status kz_scene_get_info(kz_scene* scene, kz_scene_info* out_info);

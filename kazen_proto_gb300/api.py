@@ -315,6 +315,14 @@ class Scene:
         a = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
         check(lib().kz_scene_set_mesh_uvs(self._h, int(geom_id), _ptr(a), len(a)))
 
+    def add_point_light(self, position, radiance) -> int:
+        """PointLight(position, radiance) (light.cpp:18-36): radiance / (0.1 |d|^2) at distance d."""
+        p = np.ascontiguousarray(position, np.float32).reshape(3)
+        r = np.ascontiguousarray(radiance, np.float32).reshape(3)
+        lid = C.c_int32(-1)
+        check(lib().kz_scene_add_point_light(self._h, _ptr(p), _ptr(r), C.byref(lid)))
+        return lid.value
+
     def set_environment(self, rgb=(0.0, 0.0, 0.0), texture: int = -1) -> None:
         """Radiance of rays that leave the scene: rgb times a lat-long texture (-1: none)."""
         a = np.ascontiguousarray(rgb, np.float32).reshape(3)

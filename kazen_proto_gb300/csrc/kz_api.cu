@@ -178,6 +178,7 @@ struct kz_scene {
     std::vector<float> tex_texels;
     float env_rgb[3] = {0.f, 0.f, 0.f};
     int32_t env_tex = -1;
+    std::vector<float> point_lights;  // 6 floats each: position, radiance
     DevBuf d_tri_uv, d_mat_tex, d_textures, d_texels;
     kz::DevScene dev;
     DevBuf status;        // uint32 device status word for batch calls
@@ -570,6 +571,21 @@ kz_status kz_scene_set_mesh_uvs(kz_scene* s, int32_t geom_id, const float* uv, u
     return KZ_OK;
 }
 
+kz_status kz_scene_add_point_light(kz_scene* s, const float position[3], const float radiance[3],
+                                   int32_t* out_light_id) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    if (!position || !radiance || !finite3(position) || !finite3(radiance))
+        return fail(KZ_ERR_INVALID_ARG, "point light position and radiance must be finite");
+    if (radiance[0] < 0.f || radiance[1] < 0.f || radiance[2] < 0.f)
+        return fail(KZ_ERR_INVALID_ARG, "point light radiance must be >= 0");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->point_lights.insert(s->point_lights.end(), position, position + 3);
+    s->point_lights.insert(s->point_lights.end(), radiance, radiance + 3);
+    s->built = false;
+    if (out_light_id) *out_light_id = (int32_t)(s->point_lights.size() / 6) - 1;
+    return KZ_OK;
+}
+
 kz_status kz_scene_set_environment(kz_scene* s, const float rgb[3], int32_t texture) {
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     if (!rgb || !finite3(rgb) || rgb[0] < 0.f || rgb[1] < 0.f || rgb[2] < 0.f)
@@ -693,6 +709,21 @@ kz_status kz_scene_build(kz_scene* s) {
         L.area = sum;
         cdf.insert(cdf.end(), c.begin(), c.end());
         glight[g] = (int32_t)lights.size();
+        lights.push_back(L);
+    }
+    // point lights after the area lights: no triangles, the position in one light_tris record
+    for (size_t k = 0; k < s->point_lights.size() / 6; ++k) {
+        const float* q = &s->point_lights[k * 6];
+        kz::DevLight L{};
+        L.tri_begin = (uint32_t)(ltris.size() / 12);
+        L.tri_count = 0;
+        L.cdf_begin = 0;
+        L.geom = KZ_INVALID_ID;
+        L.area = 0.f;
+        L.Le[0] = q[3];
+        L.Le[1] = q[4];
+        L.Le[2] = q[5];
+        ltris.insert(ltris.end(), {q[0], q[1], q[2], 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
         lights.push_back(L);
     }
 

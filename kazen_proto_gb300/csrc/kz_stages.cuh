@@ -348,22 +348,30 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
         if (nl > 0 && any_smooth && wsum > 0.f) {
             const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
             const DevLight lt = s.lights[li];
-            const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
-            const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
-            const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
-            const float su0 = sqrtf(u[2]);
-            const float bu0 = 1.f - su0;
-            const float bv0 = u[3] * su0;
-            const f3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
-            const f3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+            // a point light (PointLight, light.cpp:18-31) has no triangles:
+            // its position is the one light_tris record it names
+            const bool point = lt.tri_count == 0;
+            f3 p, nlgt = mk(0.f, 0.f, 0.f);
+            if (point) {
+                p = xyz(__ldg(s.light_tris + (size_t)lt.tri_begin * 3));
+            } else {
+                const uint32_t kk = cdf_sample(s.light_cdf + lt.cdf_begin, lt.tri_count, u[1]);
+                const float4* lq = s.light_tris + (size_t)(lt.tri_begin + kk) * 3;
+                const f3 a0 = xyz(__ldg(lq)), a1 = xyz(__ldg(lq + 1)), a2 = xyz(__ldg(lq + 2));
+                const float su0 = sqrtf(u[2]);
+                const float bu0 = 1.f - su0;
+                const float bv0 = u[3] * su0;
+                p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+                nlgt = normalize(cross(a1 - a0, a2 - a0));
+            }
             const f3 lv = p - P;
             const float dist2 = dot(lv, lv);
             const float dist = sqrtf(dist2);
             const f3 ldir = mk(lv.x / dist, lv.y / dist, lv.z / dist);
-            const float cos_l = -dot(ldir, nlgt);
-            if (cos_l > 0.f) {
-                const float pdf_solid = dist2 / (cos_l * lt.area);
-                const float lpdf = pdf_solid * (1.0f / (float)nl);
+            const float cos_l = point ? 1.f : -dot(ldir, nlgt);
+            if (cos_l > 0.f && dist2 > 0.f) {
+                // a delta light is picked with probability 1/nl and weighs no MIS
+                const float lpdf = point ? 1.0f / (float)nl : dist2 / (cos_l * lt.area) * (1.0f / (float)nl);
                 const f3 wo = fr.to_local(ldir);
                 f3 f = mk(0.f, 0.f, 0.f);
                 float bpdf = 0.f;
@@ -376,8 +384,10 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                 }
                 if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
                 if (!is_zero(f)) {
-                    const float w = power_heuristic(lpdf, bpdf);
-                    const f3 c = hmul(hmul(beta, f), ld3(lt.Le)) * (w / lpdf);
+                    const float w = point ? 1.f : power_heuristic(lpdf, bpdf);
+                    // PointLight::sample's falloff: radiance / (0.1 |d|^2)
+                    const f3 Le_l = point ? ld3(lt.Le) * (1.f / (dist2 * 0.1f)) : ld3(lt.Le);
+                    const f3 c = hmul(hmul(beta, f), Le_l) * (w / lpdf);
                     out.shadow = true;
                     out.s_o = make_float4(P.x, P.y, P.z, dist - kRayEps);
                     out.s_d = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(film_idx));
@@ -387,7 +397,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     if (kGuided && gs.nee && guided) {
                         // training sample: the light direction with its
                         // MIS-weighted share of L*f*cos over the light pdf
-                        const f3 fl = hmul(f, ld3(lt.Le));
+                        const f3 fl = hmul(f, Le_l);
                         const float wt = (0.2126f * fl.x + 0.7152f * fl.y + 0.0722f * fl.z) * (w / lpdf);
                         const f3 p01 = hmul(P - mk(s.box_lo.x, s.box_lo.y, s.box_lo.z),
                                             mk(s.box_inv.x, s.box_inv.y, s.box_inv.z));

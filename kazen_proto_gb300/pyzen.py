@@ -17,7 +17,7 @@ GPU renderer:
 Differences, each stated where it happens: shaders are lowered from their
 OSL source (load_oso_shader looks for name.osl, not the compiled .oso; shader
 networks and texture lookups lower as scene_xml lowers them, texture files
-relative to the working directory); add_point_light raises; spheres are
+relative to the working directory); spheres are
 tessellated (with the reference's parametric uv); every integrator type renders with the path
 integrator; the frame renders in one GPU call and on_tile_end then runs for
 each tile in tile order; tiles cover the film exactly (the reference's
@@ -264,7 +264,8 @@ class Scene:
         self.warnings.append(f"sphere {name!r} tessellated to {len(f)} triangles")
 
     def add_point_light(self, radiance, position, shader_name) -> None:
-        raise NotImplementedError("point lights are not supported on the GPU path")
+        """A PointLight at `position` (shader_name is not used by the reference's point light either)."""
+        self.desc.point_lights.append((tuple(map(float, position)), tuple(map(float, radiance))))
 
     def build_bvh(self, names=None) -> None:
         if self._built is not None:

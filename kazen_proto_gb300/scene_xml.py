@@ -38,8 +38,10 @@ the GPU path renders:
 Shader files are looked up next to the scene, then in the reference's shader
 library directory (../../shader/src relative to the scene).
 
+<PointLight position radiance> becomes a point light (kz_scene_add_point_light).
+
 Not supported (reported in `LoadedScene.warnings` or raised, never silently
-changed): point lights, BSSRDF closures, bump mapping and shaders whose
+changed): BSSRDF closures, bump mapping and shaders whose
 closure weights depend on the shading point other than through the texture
 lookups above. Shading uses geometric normals (OBJ vertex normals are not
 read). The reference's own parser sets is_light for any `is_light`
@@ -327,7 +329,10 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             if tag != "PathIntegrator":
                 out.warnings.append(f"<{tag}> rendered with the path integrator")
         elif tag == "PointLight":
-            out.warnings.append(f"<{tag}> is not supported and was skipped")
+            # PointLight defaults: position (0, 5, 0) (light.h:53-56), radiance 0 unless given
+            a = attrs(node)
+            d.point_lights.append((tuple(float(x) for x in a.get("position", (0.0, 5.0, 0.0))),
+                                   tuple(float(x) for x in a.get("radiance", (0.0, 0.0, 0.0)))))
 
     # materials: a ShaderGroupBegin starts a group, its Shader and
     # ConnectShaders siblings follow; the environment is a group between
@@ -416,7 +421,7 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
                 v, sf, uv = sphere_mesh(cr[:3], cr[3])
                 d.add(apply_transform(M, v), sf, shader_of(node), light, uv=uv)
                 out.warnings.append("<Sphere> tessellated to an icosphere of %d triangles" % len(sf))
-            elif node.tag != "PointLight":  # reported with the other unsupported tags
+            elif node.tag != "PointLight":  # read with the lights above
                 out.warnings.append(f"<{node.tag}> in <Objects> is not supported and was skipped")
     if d.camera is None:
         raise ValueError(f"{path}: no <Camera>")

@@ -38,6 +38,7 @@ class SceneDesc:
     uvs: dict = field(default_factory=dict)         # mesh index -> (nverts, 2) f32
     env: tuple = (0.0, 0.0, 0.0)
     env_texture: int = -1
+    point_lights: list = field(default_factory=list)   # (position, radiance)
 
     def add(self, verts, idx, material_id, is_light=False, uv=None) -> int:
         self.meshes.append((np.asarray(verts, np.float32).reshape(-1, 3), np.asarray(idx, np.uint32).reshape(-1, 3),
@@ -62,6 +63,8 @@ class SceneDesc:
             if g in self.uvs:
                 s.set_mesh_uvs(g, self.uvs[g])
         s.set_materials(self.material_array())
+        for pos, rad in self.point_lights:
+            s.add_point_light(pos, rad)
         if self.textures:
             s.set_textures(self.textures)
         if any(self.env) or self.env_texture >= 0:

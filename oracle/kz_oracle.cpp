@@ -1250,10 +1250,12 @@ LobeSample sample_lobe(const kz_lobe& l, V3 wi, float u0, float u1, float u2) {
 // ---------------------------------------------------------------- scene
 struct OLight {
     uint32_t geom;
-    std::vector<uint32_t> tris;  // global triangle ids
+    std::vector<uint32_t> tris;  // global triangle ids (empty for a point light)
     std::vector<float> cdf;      // normalised running sum of areas, cdf[0] = 0
     float area;
     V3 Le;
+    bool point = false;          // PointLight (src/core/light.cpp:18-31) at `pos`
+    V3 pos{0, 0, 0};
 };
 
 struct OTexture {
@@ -1456,22 +1458,25 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         if (nl > 0 && any_smooth && wsum > 0.f) {
             uint32_t li = std::min((uint32_t)(u[0] * (float)nl), nl - 1);
             const OLight& lt = sc.lights[li];
-            uint32_t k = cdf_sample(lt.cdf, u[1]);
-            uint32_t ltri = lt.tris[k];
-            V3 a0 = sc.bvh.v(ltri, 0), a1 = sc.bvh.v(ltri, 1), a2 = sc.bvh.v(ltri, 2);
-            float su0 = std::sqrt(u[2]);
-            float bu0 = 1.f - su0;
-            float bv0 = u[3] * su0;
-            V3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
-            V3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+            V3 p = lt.pos, nlgt(0, 0, 0);
+            if (!lt.point) {
+                uint32_t k = cdf_sample(lt.cdf, u[1]);
+                uint32_t ltri = lt.tris[k];
+                V3 a0 = sc.bvh.v(ltri, 0), a1 = sc.bvh.v(ltri, 1), a2 = sc.bvh.v(ltri, 2);
+                float su0 = std::sqrt(u[2]);
+                float bu0 = 1.f - su0;
+                float bv0 = u[3] * su0;
+                p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+                nlgt = normalize(cross(a1 - a0, a2 - a0));
+            }
             V3 lv = p - P;
             float dist2 = dot(lv, lv);
             float dist = std::sqrt(dist2);
             V3 ldir(lv.x / dist, lv.y / dist, lv.z / dist);
-            float cos_l = -dot(ldir, nlgt);
-            if (cos_l > 0.f) {
-                float pdf_solid = dist2 / (cos_l * lt.area);
-                float lpdf = pdf_solid * (1.0f / (float)nl);
+            float cos_l = lt.point ? 1.f : -dot(ldir, nlgt);
+            if (cos_l > 0.f && dist2 > 0.f) {
+                // a point light: picked with probability 1/nl, no MIS (a delta light)
+                float lpdf = lt.point ? 1.0f / (float)nl : dist2 / (cos_l * lt.area) * (1.0f / (float)nl);
                 V3 wo = fr.to_local(ldir);
                 V3 f(0, 0, 0);
                 float bpdf = 0.f;
@@ -1485,8 +1490,10 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
                 if (!is_zero(f)) {
                     pc.shadow++;
                     if (!sc.bvh.any(P, ldir, kRayEps, dist - kRayEps)) {
-                        float w = power_heuristic(lpdf, bpdf);
-                        V3 c = mul(mul(beta, f), lt.Le) * (w / lpdf);
+                        float w = lt.point ? 1.f : power_heuristic(lpdf, bpdf);
+                        // PointLight::sample returns radiance / (0.1 |d|^2)
+                        V3 Le = lt.point ? lt.Le * (1.f / (dist2 * 0.1f)) : lt.Le;
+                        V3 c = mul(mul(beta, f), Le) * (w / lpdf);
                         L = L + c;
                     }
                 }
@@ -1709,6 +1716,18 @@ void* kzo_scene_create(const float* tri_verts, uint32_t ntris, const uint32_t* t
 }
 
 void kzo_scene_free(void* h) { delete static_cast<OScene*>(h); }
+
+// Point lights follow the area lights in the light list.
+void kzo_scene_add_point_light(void* h, const float* position, const float* radiance) {
+    OScene* s = static_cast<OScene*>(h);
+    OLight lt;
+    lt.geom = 0xffffffffu;
+    lt.area = 0.f;
+    lt.point = true;
+    lt.pos = V3(position[0], position[1], position[2]);
+    lt.Le = V3(radiance[0], radiance[1], radiance[2]);
+    s->lights.push_back(std::move(lt));
+}
 
 // Textures, per-triangle vertex uvs (6 floats per triangle in global order,
 // NULL = barycentrics) and the environment of a restatement scene.

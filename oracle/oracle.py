@@ -49,6 +49,7 @@ def lib():
             "kzo_scene_create": (_P, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, _P, C.c_uint32]),
             "kzo_scene_free": (None, [_P]),
             "kzo_scene_set_textures": (None, [_P, _P, C.c_uint32, _P, _P, C.c_int32]),
+            "kzo_scene_add_point_light": (None, [_P, _P, _P]),
             "kzo_render": (None, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(RenderConfig), C.c_int,
                                   C.c_uint32, C.c_uint32, _P, _P]),
             "kzo_camera_rays": (None, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P]),
@@ -179,6 +180,9 @@ class Scene:
     def from_desc(cls, desc):
         tv, tg, gm, gl = desc.flatten()
         sc = cls(tv, tg, gm, gl, desc.material_array())
+        for pos, rad in getattr(desc, "point_lights", []):
+            lib().kzo_scene_add_point_light(sc.h, _p(np.ascontiguousarray(pos, np.float32)),
+                                            _p(np.ascontiguousarray(rad, np.float32)))
         textures = getattr(desc, "textures", [])
         env = np.ascontiguousarray(getattr(desc, "env", (0, 0, 0)), np.float32)
         if textures or env.any():

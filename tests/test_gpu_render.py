@@ -190,6 +190,21 @@ def test_textures_and_environment_render(gpu, oracle_mod):
     assert rel_mse(img_g, plain) > 1e-2
 
 
+@pytest.mark.parametrize("with_area", [True, False])
+def test_point_lights_render(gpu, oracle_mod, with_area):
+    """Point lights next to the area light (uniform pick among all lights,
+    MIS only for the area light) and point lights alone."""
+    d = scenes.box_scene(40, 40, spp=8, max_depth=5)
+    d.point_lights = [((0.3, 0.8, 0.4), (0.4, 0.3, 0.2)), ((0.7, 0.5, 0.25), (0.1, 0.2, 0.4))]
+    if not with_area:
+        d.meshes = [m for m in d.meshes if not m[3]]
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=5, seed=9).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 5, seed=9)
+    assert np.isfinite(img).all() and ref.mean() > 1e-3
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+
+
 def test_terrain_scene_small(gpu, oracle_mod):
     d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
     s = d.build()

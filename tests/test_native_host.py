@@ -155,3 +155,13 @@ def test_texture_validation_on_host(native_lib):
     with pytest.raises(N.KazenError) as e:
         s.build_bvh()
     assert "environment texture" in str(e.value)
+
+
+def test_point_light_validation_on_host(native_lib):
+    s = api.Scene()
+    assert s.add_point_light((0, 1, 0), (1, 1, 1)) == 0
+    assert s.add_point_light((0, 2, 0), (0, 0, 0)) == 1
+    with pytest.raises(N.KazenError):
+        s.add_point_light((0, np.nan, 0), (1, 1, 1))
+    with pytest.raises(N.KazenError):
+        s.add_point_light((0, 1, 0), (1, -1, 1))

@@ -89,8 +89,8 @@ def test_unsupported_calls_raise():
     s.connect_shader("z", "Cout", "l", "Cs")  # from a layer that does not exist
     with pytest.raises(ValueError):
         s.end_shader_group()
-    with pytest.raises(NotImplementedError):
-        s.add_point_light((1, 1, 1), (0, 0, 0), "g")
+    s.add_point_light((1, 2, 3), (0, 5, 0), "g")
+    assert s.desc.point_lights == [((0.0, 5.0, 0.0), (1.0, 2.0, 3.0))]
     with pytest.raises(KeyError):
         s.add_mesh(None, [(0, 0, 0), (1, 0, 0), (0, 1, 0)], [], [], [(0, 1, 2)], "m", "unknown")
 

@@ -129,8 +129,10 @@ def test_loader_errors(tmp_path):
     with pytest.raises(ValueError):  # a connection from a layer that does not exist
         X.load(scene(cam + bad_link))
     L = X.load(scene(cam + group + '<Objects><Mesh filename="string t.obj" shader_name="m" is_light="bool false"/>'
-                     '<PointLight/></Objects><WhittedIntegrator/>'))
-    assert L.desc.meshes[0][3] is False and len(L.warnings) == 2
+                     '</Objects><Lights><PointLight radiance="float3 1 2 3" position="float3 0 4 0"/></Lights>'
+                     '<WhittedIntegrator/>'))
+    assert L.desc.meshes[0][3] is False and len(L.warnings) == 1
+    assert L.desc.point_lights == [((0.0, 4.0, 0.0), (1.0, 2.0, 3.0))]
 
 
 CHECKER_OSL = """shader checkerboard (
