@@ -255,6 +255,14 @@ kz_status kz_scene_set_textures(kz_scene* scene, const kz_texture* textures, uin
  * vertices 1 and 2, as the reference's meshes without texcoords do
  * (TriangleMesh::post_hit, src/core/shape.cpp:615-683). */
 kz_status kz_scene_set_mesh_uvs(kz_scene* scene, int32_t geom_id, const float* uv, uint32_t nverts);
+/* Per-vertex normals (nverts*3 floats, host, object space: the mesh's
+ * xform12 is applied as its inverse transpose, then each is normalised) of a
+ * mesh added with kz_scene_add_mesh. Shading then uses the interpolated
+ * normal and the shading point moves off the flat triangle by the
+ * shadow-terminator offset (Hanika 2021), as TriangleMesh::post_hit does
+ * (src/core/shape.cpp:628-656); meshes without normals shade with the
+ * geometric normal. */
+kz_status kz_scene_set_mesh_normals(kz_scene* scene, int32_t geom_id, const float* normals, uint32_t nverts);
 /* Radiance of a ray that leaves the scene (the background shader of
  * PathIntegrator::Li, src/core/integrator.cpp:381-388, 545-552): rgb times
  * texture `texture` (-1: none) looked up in latitude-longitude form,

@@ -167,6 +167,7 @@ SIGNATURES = {
     "kz_scene_set_materials": (C.c_int32, [_P, _P, C.c_uint32]),
     "kz_scene_set_textures": (C.c_int32, [_P, _P, C.c_uint32]),
     "kz_scene_set_mesh_uvs": (C.c_int32, [_P, C.c_int32, _P, C.c_uint32]),
+    "kz_scene_set_mesh_normals": (C.c_int32, [_P, C.c_int32, _P, C.c_uint32]),
     "kz_scene_set_environment": (C.c_int32, [_P, _P, C.c_int32]),
     "kz_scene_add_point_light": (C.c_int32, [_P, _P, _P, C.POINTER(C.c_int32)]),
     "kz_scene_build": (C.c_int32, [_P]),

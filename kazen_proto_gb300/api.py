@@ -323,6 +323,11 @@ class Scene:
         check(lib().kz_scene_add_point_light(self._h, _ptr(p), _ptr(r), C.byref(lid)))
         return lid.value
 
+    def set_mesh_normals(self, geom_id: int, normals) -> None:
+        """Per-vertex normals (nverts, 3) of a mesh, in the space its vertices were given in."""
+        a = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        check(lib().kz_scene_set_mesh_normals(self._h, int(geom_id), _ptr(a), len(a)))
+
     def set_environment(self, rgb=(0.0, 0.0, 0.0), texture: int = -1) -> None:
         """Radiance of rays that leave the scene: rgb times a lat-long texture (-1: none)."""
         a = np.ascontiguousarray(rgb, np.float32).reshape(3)

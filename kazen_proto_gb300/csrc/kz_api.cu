@@ -76,6 +76,8 @@ struct DevBuf {
 struct HostMesh {
     std::vector<float> verts;  // world space, nverts * 3
     std::vector<float> uv;     // nverts * 2 texture coordinates, or empty
+    std::vector<float> nrm;    // nverts * 3 world-space unit normals, or empty
+    float xf[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};  // object-to-world (for normals)
     std::vector<uint32_t> idx;
     int32_t material;
     int32_t is_light;
@@ -179,7 +181,7 @@ struct kz_scene {
     float env_rgb[3] = {0.f, 0.f, 0.f};
     int32_t env_tex = -1;
     std::vector<float> point_lights;  // 6 floats each: position, radiance
-    DevBuf d_tri_uv, d_mat_tex, d_textures, d_texels;
+    DevBuf d_tri_uv, d_mat_tex, d_textures, d_texels, d_tri_nrm;
     kz::DevScene dev;
     DevBuf status;        // uint32 device status word for batch calls
     uint32_t* status_host = nullptr;  // pinned
@@ -473,6 +475,7 @@ kz_status kz_scene_add_mesh(kz_scene* s, const float* xyz, uint32_t nverts, cons
     HostMesh m;
     m.material = material_id;
     m.is_light = is_light ? 1 : 0;
+    if (xform12) std::copy(xform12, xform12 + 12, m.xf);
     m.verts.resize((size_t)nverts * 3);
     for (uint32_t i = 0; i < nverts; ++i) {
         const float* p = xyz + (size_t)i * 3;
@@ -567,6 +570,37 @@ kz_status kz_scene_set_mesh_uvs(kz_scene* s, int32_t geom_id, const float* uv, u
     for (size_t i = 0; i < (size_t)nverts * 2; ++i)
         if (!std::isfinite(uv[i])) return fail(KZ_ERR_INVALID_ARG, "uv %zu is not finite", i / 2);
     m.uv.assign(uv, uv + (size_t)nverts * 2);
+    s->built = false;
+    return KZ_OK;
+}
+
+kz_status kz_scene_set_mesh_normals(kz_scene* s, int32_t geom_id, const float* n, uint32_t nverts) {
+    if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (geom_id < 0 || (size_t)geom_id >= s->meshes.size())
+        return fail(KZ_ERR_INVALID_ARG, "geom_id %d is not a mesh of this scene", geom_id);
+    HostMesh& m = s->meshes[(size_t)geom_id];
+    if ((size_t)nverts * 3 != m.verts.size())
+        return fail(KZ_ERR_INVALID_ARG, "mesh %d has %zu vertices, got %u normals", geom_id, m.verts.size() / 3, nverts);
+    if (nverts && !n) return fail(KZ_ERR_INVALID_ARG, "normals is NULL");
+    // inverse transpose of the 3x3 part: the cofactor matrix (scaled by det, normalised away)
+    const float* a = m.xf;
+    const float c[9] = {a[5] * a[10] - a[6] * a[9], a[6] * a[8] - a[4] * a[10], a[4] * a[9] - a[5] * a[8],
+                        a[2] * a[9] - a[1] * a[10], a[0] * a[10] - a[2] * a[8], a[1] * a[8] - a[0] * a[9],
+                        a[1] * a[6] - a[2] * a[5], a[2] * a[4] - a[0] * a[6], a[0] * a[5] - a[1] * a[4]};
+    // cofactors = det * inverse transpose: a mirroring transform (det < 0) keeps the normals' side
+    const float sgn = a[0] * c[0] + a[1] * c[1] + a[2] * c[2] < 0.f ? -1.f : 1.f;
+    std::vector<float> out((size_t)nverts * 3);
+    for (uint32_t i = 0; i < nverts; ++i) {
+        const float* p = n + (size_t)i * 3;
+        if (!finite3(p)) return fail(KZ_ERR_INVALID_ARG, "normal %u is not finite", i);
+        float q[3];
+        for (int r = 0; r < 3; ++r) q[r] = sgn * (c[r * 3] * p[0] + c[r * 3 + 1] * p[1] + c[r * 3 + 2] * p[2]);
+        const float len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+        if (!(len > 0.f) || !std::isfinite(len)) return fail(KZ_ERR_INVALID_ARG, "normal %u has no direction", i);
+        for (int r = 0; r < 3; ++r) out[(size_t)i * 3 + r] = q[r] / len;
+    }
+    m.nrm = std::move(out);
     s->built = false;
     return KZ_OK;
 }
@@ -727,6 +761,23 @@ kz_status kz_scene_build(kz_scene* s) {
         lights.push_back(L);
     }
 
+    // vertex normals per triangle record (leaf order) when any mesh has them
+    bool any_nrm = false;
+    for (const auto& m : s->meshes) any_nrm |= !m.nrm.empty();
+    std::vector<float4> tri_nrm;
+    if (any_nrm) {
+        tri_nrm.assign((size_t)total * 3, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (size_t r = 0; r < (size_t)total; ++r) {
+            const uint32_t gid = out.order[r];
+            const HostMesh& m = s->meshes[tgeom[gid]];
+            if (m.nrm.empty()) continue;
+            const size_t k = gid - goff[tgeom[gid]];
+            for (int c = 0; c < 3; ++c) {
+                const float* q = &m.nrm[(size_t)m.idx[k * 3 + c] * 3];
+                tri_nrm[r * 3 + c] = make_float4(q[0], q[1], q[2], 1.f);
+            }
+        }
+    }
     // vertex uvs per triangle record (leaf order) for textured materials
     std::vector<float2> tri_uv;
     if (any_tex) {
@@ -756,6 +807,7 @@ kz_status kz_scene_build(kz_scene* s) {
     KZ_TRY(upload(s->lights, lights, st));
     KZ_TRY(upload(s->light_cdf, cdf, st));
     KZ_TRY(upload(s->light_tris, ltris, st));
+    if (any_nrm) KZ_TRY(upload(s->d_tri_nrm, tri_nrm, st));
     if (any_tex) {
         KZ_TRY(upload(s->d_tri_uv, tri_uv, st));
         KZ_TRY(upload(s->d_mat_tex, mat_tex, st));
@@ -795,6 +847,7 @@ kz_status kz_scene_build(kz_scene* s) {
     d.light_tris = s->light_tris.as<float4>();
     d.n_lights = (uint32_t)lights.size();
     d.tri_uv = any_tex ? s->d_tri_uv.as<float2>() : nullptr;
+    d.tri_nrm = any_nrm ? s->d_tri_nrm.as<float4>() : nullptr;
     d.mat_tex = any_tex ? s->d_mat_tex.as<int32_t>() : nullptr;
     d.textures = ntex ? s->d_textures.as<kz::DevTexture>() : nullptr;
     d.tex_data = ntex ? s->d_texels.as<float>() : nullptr;
@@ -1537,7 +1590,8 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
     uint32_t iters = std::max<uint32_t>(4, max_depth + 1);
     iters += iters & 1u;
     bool textured = false;  // the texture tint is compiled out unless a job needs it
-    for (uint32_t j = 0; j < n_jobs; ++j) textured |= jobs[j].scene->dev.mat_tex != nullptr;
+    for (uint32_t j = 0; j < n_jobs; ++j)
+        textured |= jobs[j].scene->dev.mat_tex != nullptr || jobs[j].scene->dev.tri_nrm != nullptr;
     auto enqueue = [&]() {
         kz::PathSoA a = A, b = B;
         for (uint32_t it = 0; it < iters; ++it) {

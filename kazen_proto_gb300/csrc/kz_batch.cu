@@ -25,7 +25,7 @@ __global__ void k_generate_batch_dev(const DevJob* __restrict__ jobs, uint32_t n
     dst.d4[k].w = __uint_as_float(__float_as_uint(dst.d4[k].w) | (job << kJobShift));
 }
 
-template <bool kTex>
+template <bool kAttr>
 __global__ void __launch_bounds__(256, 4) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
                                                      ShadowSoA sq, DevCounters* ctr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256, 4) k_shade_batch(const DevJob* __restrict
     if (i < n_in) {
         const float4 d4 = in.d4[i];
         const DevJob& J = jobs[__float_as_uint(d4.w) >> kJobShift];
-        shade_vertex<false, kTex>(J.scene, J.pp, in.hit[i], in.o4[i], d4, in.b4[i], in.rng[i], GuideShade{}, nullptr,
+        shade_vertex<false, kAttr>(J.scene, J.pp, in.hit[i], in.o4[i], d4, in.b4[i], in.rng[i], GuideShade{}, nullptr,
                                   so);
         if (!is_zero(so.Lsum)) film_add(J.film, nullptr, so.film_idx, so.Lsum);
     }
@@ -62,7 +62,7 @@ void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst,
     k_generate_batch_dev<<<grid_for(cap, block), block, 0, st>>>(jobs, n_jobs, dst, ctr);
 }
 void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
-                        uint32_t block, bool textured, cudaStream_t st) {
+                        uint32_t block, bool textured, cudaStream_t st) {  // textured: textures or normals
     if (!cap) return;
     if (textured)
         k_shade_batch<true><<<grid_for(cap, block), block, 0, st>>>(jobs, in, out, sq, ctr);

@@ -48,6 +48,7 @@ struct DevScene {
     float3 box_inv = {1.f, 1.f, 1.f};  // 1 / extent per axis
     // textures: NULL / 0 when the scene has none
     const float2* tri_uv = nullptr;     // n_tris * 3 vertex uvs, leaf order
+    const float4* tri_nrm = nullptr;    // n_tris * 3 vertex normals (w = 1; 0 for a mesh without), leaf order
     const int32_t* mat_tex = nullptr;   // texture of each material or -1
     const DevTexture* textures = nullptr;
     const float* tex_data = nullptr;

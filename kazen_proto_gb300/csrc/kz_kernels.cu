@@ -133,7 +133,7 @@ void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint3
         launch_shade_guided_dev(s, pp, in, cap, out, sq, ctr, film, film64, *gs, block, st);
         return;
     }
-    if (s.mat_tex)
+    if (s.mat_tex || s.tri_nrm)
         k_shade<false, true><<<grid_for(cap, block), block, 0, st>>>(s, pp, in, cap, out, sq, ctr, film, film64,
                                                                      GuideShade{}, &ctr->n_active);
     else
@@ -143,7 +143,7 @@ void launch_shade_dev(const DevScene& s, const PathParams& pp, PathSoA in, uint3
 void launch_shade(const DevScene& s, const PathParams& pp, PathSoA in, uint32_t n_in, PathSoA out, ShadowSoA sq,
                   DevCounters* ctr, float* film, double* film64, uint32_t block, cudaStream_t st) {
     if (!n_in) return;
-    if (s.mat_tex)
+    if (s.mat_tex || s.tri_nrm)
         k_shade<false, true><<<grid_for(n_in, block), block, 0, st>>>(s, pp, in, n_in, out, sq, ctr, film, film64,
                                                                       GuideShade{}, nullptr);
     else

@@ -255,9 +255,10 @@ struct ShadeOut {
 
 // One shaded path vertex: emission, next-event estimation (the shadow ray is
 // returned, not traced), roulette and direction sampling. `raw` holds the
-// guiding network's outputs for this path (guided mode only). kTex = false
-// compiles the texture tint out (scenes without textured materials).
-template <bool kGuided, bool kTex = true>
+// guiding network's outputs for this path (guided mode only). kAttr = false
+// compiles the vertex attributes out (texture tint, shading normals) for
+// scenes that have neither.
+template <bool kGuided, bool kAttr = true>
 __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams& pp, const float4 hit,
                                              const float4 o4, const float4 d4, const float4 b4,
                                              unsigned long long rng_state, const GuideShade& gs, const float* raw,
@@ -284,10 +285,27 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
         const f3 v0 = xyz(ta), v1 = xyz(tb), v2 = xyz(tc);
         const f3 Ng = normalize(cross(v1 - v0, v2 - v0));
         const f3 d = xyz(d4);
-        const f3 P = xyz(o4) + d * hit.x;
+        f3 P = xyz(o4) + d * hit.x;
+        // shading normal: the interpolated vertex normal, with the shading
+        // point moved off the flat triangle by the shadow-terminator offset
+        // (Hanika 2021), as TriangleMesh::post_hit does (shape.cpp:628-656)
+        f3 Ns = Ng;
+        if (kAttr && s.tri_nrm) {
+            const float4 m0 = __ldg(s.tri_nrm + (size_t)rec * 3);
+            if (m0.w != 0.f) {
+                const f3 n0 = xyz(m0), n1 = xyz(__ldg(s.tri_nrm + (size_t)rec * 3 + 1)),
+                         n2 = xyz(__ldg(s.tri_nrm + (size_t)rec * 3 + 2));
+                const float b0 = 1.f - hit.y - hit.z;
+                Ns = normalize(n0 * b0 + n1 * hit.y + n2 * hit.z);
+                const f3 Pb = v0 * b0 + v1 * hit.y + v2 * hit.z;
+                const float e0 = fminf(0.f, dot(Pb - v0, n0)), e1 = fminf(0.f, dot(Pb - v1, n1)),
+                            e2 = fminf(0.f, dot(Pb - v2, n2));
+                P = Pb - (n0 * (b0 * e0) + n1 * (hit.y * e1) + n2 * (hit.z * e2));
+            }
+        }
         // texture tint of the material at the hit's uv (interpolated vertex
         // uvs; the barycentrics of vertices 1, 2 when the mesh has none)
-        const int32_t mtex = kTex && s.mat_tex ? __ldg(s.mat_tex + __float_as_uint(tc.w)) : -1;
+        const int32_t mtex = kAttr && s.mat_tex ? __ldg(s.mat_tex + __float_as_uint(tc.w)) : -1;
         const bool textured = mtex >= 0;
         f3 tint = mk(1.f, 1.f, 1.f);
         if (textured) {
@@ -296,16 +314,17 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
             const float b0 = 1.f - hit.y - hit.z;
             tint = tex_eval(s, mtex, b0 * q0.x + hit.y * q1.x + hit.z * q2.x, b0 * q0.y + hit.y * q1.y + hit.z * q2.y);
         }
-        const Frame fr(Ng);
+        const Frame fr(Ns);
         const f3 wi = -fr.to_local(d);
         f3 beta = xyz(b4);
         f3 Lsum = mk(0.f, 0.f, 0.f);
         const uint32_t nl = s.n_lights;
         const uint64_t rbase = kGuided ? ((uint64_t)pid - gs.pass_first) * pp.max_depth : 0;
 
-        // 1. emission (front face only: single_emissive_surface)
+        // 1. emission (front face only, against the shading normal:
+        // single_emissive_surface, integrator.cpp:454)
         const f3 Le = ld3(mat.Le);
-        if (!is_zero(Le) && dot(d, Ng) < 0.f) {
+        if (!is_zero(Le) && dot(d, Ns) < 0.f) {
             float w = 1.f;
             if (!prev_spec) {
                 const int li = __ldg(s.geom_light + geom);
@@ -578,7 +597,7 @@ static unsigned resident_grid(F f, unsigned block) {
 #ifndef KZ_SHADE_MIN_BLOCKS
 #define KZ_SHADE_MIN_BLOCKS 4
 #endif
-template <bool kGuided, bool kTex = true>
+template <bool kGuided, bool kAttr = true>
 __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
@@ -587,8 +606,8 @@ __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     if (n_dev) n_in = *n_dev;
     ShadeOut so;
     if (i < n_in) {
-        shade_vertex<kGuided, kTex>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
-                                    kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
+        shade_vertex<kGuided, kAttr>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
+                                     kGuided ? gs.raw + (size_t)i * kGuideOut : nullptr, so);
         if (!is_zero(so.Lsum)) film_add(film, film64, so.film_idx, so.Lsum);
     }
     const bool cont = so.cont, shadow = so.shadow;

@@ -239,11 +239,15 @@ class Scene:
 
     # -- geometry
     def add_mesh(self, world, vs, ns, ts, idx, name: str, shader_name: str, is_light: bool = False) -> None:
-        """ts: per-vertex texture coordinates (or None / empty: uv = barycentrics)."""
-        v = scene_xml.apply_transform(_world(world), np.asarray(vs, np.float64).reshape(-1, 3))
+        """ns: per-vertex normals (shading normals; None / empty: the geometric
+        normal); ts: per-vertex texture coordinates (None / empty: uv = barycentrics)."""
+        M = _world(world)
+        v = scene_xml.apply_transform(M, np.asarray(vs, np.float64).reshape(-1, 3))
         uv = None if ts is None or len(ts) == 0 else np.asarray(ts, np.float32).reshape(-1, 2)
+        nr = None if ns is None or len(ns) == 0 else scene_xml.apply_normal_transform(
+            M, np.asarray(ns, np.float64).reshape(-1, 3))
         self.desc.add(v, np.asarray(idx, np.uint32).reshape(-1, 3), self._material(shader_name), bool(is_light),
-                      uv=uv)
+                      uv=uv, normals=nr)
 
     def add_triangle(self, world, a, b, c, name: str, shader_name: str, is_light: bool = False) -> None:
         self.add_mesh(world, [a, b, c], None, None, [[0, 1, 2]], name, shader_name, is_light)
@@ -260,7 +264,7 @@ class Scene:
 
     def add_sphere(self, world, p, r: float, name: str, shader_name: str, is_light: bool = False) -> None:
         v, f, uv = scene_xml.sphere_mesh(np.asarray(p, np.float64), float(r))
-        self.add_mesh(world, v, None, uv, f, name, shader_name, is_light)
+        self.add_mesh(world, v, v - np.asarray(p, np.float32), uv, f, name, shader_name, is_light)
         self.warnings.append(f"sphere {name!r} tessellated to {len(f)} triangles")
 
     def add_point_light(self, radiance, position, shader_name) -> None:

@@ -40,11 +40,13 @@ library directory (../../shader/src relative to the scene).
 
 <PointLight position radiance> becomes a point light (kz_scene_add_point_light).
 
+OBJ vertex normals (and the tessellated spheres' radial normals) become shading
+normals (kz_scene_set_mesh_normals).
+
 Not supported (reported in `LoadedScene.warnings` or raised, never silently
 changed): BSSRDF closures, bump mapping and shaders whose
 closure weights depend on the shading point other than through the texture
-lookups above. Shading uses geometric normals (OBJ vertex normals are not
-read). The reference's own parser sets is_light for any `is_light`
+lookups above. The reference's own parser sets is_light for any `is_light`
 attribute whatever its value (scene.cpp:540); this loader honours the value.
 """
 from __future__ import annotations
@@ -103,7 +105,15 @@ def load_obj(path: str, with_uv: bool = False):
     """Vertices (n, 3) float32 and triangles (m, 3) uint32 of an OBJ file;
     with_uv also returns (n, 2) texture coordinates (None when the file has
     no `vt`), vertices split where one position carries several uvs."""
-    verts, uvs, tris, corners = [], [], [], []
+    v, t, uv, _ = load_obj_attributes(path, normals=False)
+    return (v, t, uv) if with_uv else (v, t)
+
+
+def load_obj_attributes(path: str, normals: bool = True):
+    """(vertices (n, 3), triangles (m, 3), uvs (n, 2) or None, normals (n, 3)
+    or None) of an OBJ file: a vertex per distinct (position, texcoord,
+    normal) triple the faces use, polygons fan-triangulated."""
+    verts, uvs, nrms, corners = [], [], [], []
     with open(path) as f:
         for line in f:
             line = line.split("#", 1)[0].strip()
@@ -114,34 +124,43 @@ def load_obj(path: str, with_uv: bool = False):
                 verts.append([float(tok[1]), float(tok[2]), float(tok[3])])
             elif tok[0] == "vt":
                 uvs.append([float(tok[1]), float(tok[2]) if len(tok) > 2 else 0.0])
+            elif tok[0] == "vn":
+                nrms.append([float(tok[1]), float(tok[2]), float(tok[3])])
             elif tok[0] == "f":
                 idx = []
                 for t in tok[1:]:
                     parts = t.split("/")
                     i = int(parts[0])
                     vi = i - 1 if i > 0 else len(verts) + i
-                    ti = -1
+                    ti = ni = -1
                     if len(parts) > 1 and parts[1]:
                         j = int(parts[1])
                         ti = j - 1 if j > 0 else len(uvs) + j
-                    idx.append((vi, ti))
+                    if len(parts) > 2 and parts[2]:
+                        j = int(parts[2])
+                        ni = j - 1 if j > 0 else len(nrms) + j
+                    idx.append((vi, ti, ni))
                 if len(idx) < 3:
                     raise ValueError(f"{path}: face with {len(idx)} vertices")
                 for k in range(1, len(idx) - 1):  # fan
                     corners.append([idx[0], idx[k], idx[k + 1]])
     v = np.asarray(verts, np.float32).reshape(-1, 3)
-    c = np.asarray(corners, np.int64).reshape(-1, 3, 2)
+    c = np.asarray(corners, np.int64).reshape(-1, 3, 3)
     if c.size and (c[..., 0].min() < 0 or c[..., 0].max() >= len(v)):
         raise ValueError(f"{path}: face index out of range")
-    if not with_uv:
-        return v, c[..., 0].astype(np.uint32)
-    if not uvs or (c[..., 1] < 0).all():
-        return v, c[..., 0].astype(np.uint32), None
-    if (c[..., 1] < 0).any() or c[..., 1].max() >= len(uvs):
+    use_uv = bool(uvs) and (c[..., 1] >= 0).any()
+    use_n = normals and bool(nrms) and (c[..., 2] >= 0).any()
+    if use_uv and ((c[..., 1] < 0).any() or c[..., 1].max() >= len(uvs)):
         raise ValueError(f"{path}: texture coordinate index missing or out of range")
-    pairs, inv = np.unique(c.reshape(-1, 2), axis=0, return_inverse=True)
-    uv = np.asarray(uvs, np.float32)[pairs[:, 1]]
-    return v[pairs[:, 0]], inv.reshape(-1, 3).astype(np.uint32), uv
+    if use_n and ((c[..., 2] < 0).any() or c[..., 2].max() >= len(nrms)):
+        raise ValueError(f"{path}: normal index missing or out of range")
+    if not use_uv and not use_n:
+        return v, c[..., 0].astype(np.uint32), None, None
+    keys = c[..., [0] + ([1] if use_uv else []) + ([2] if use_n else [])].reshape(len(c) * 3, -1)
+    uniq, inv = np.unique(keys, axis=0, return_inverse=True)
+    uv = np.asarray(uvs, np.float32)[uniq[:, 1]] if use_uv else None
+    nr = np.asarray(nrms, np.float32)[uniq[:, -1]] if use_n else None
+    return v[uniq[:, 0]], inv.reshape(-1, 3).astype(np.uint32), uv, nr
 
 
 # ---------------------------------------------------------------- transforms
@@ -173,6 +192,12 @@ def mesh_transform(translate=None, rotate=None, scale=None):
 def apply_transform(M, v):
     v = np.asarray(v, np.float64)
     return (v @ M[:, :3].T + M[:, 3]).astype(np.float32)
+
+
+def apply_normal_transform(M, n):
+    """Normals under the 3x4 world matrix M: its inverse transpose, renormalised."""
+    n = np.asarray(n, np.float64) @ np.linalg.inv(M[:, :3])
+    return (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
 
 
 # ---------------------------------------------------------------- OSL lowering
@@ -401,8 +426,9 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             light = bool(a.get("is_light", False))
             M = mesh_transform(a.get("translate"), a.get("rotate"), a.get("scale"))
             if node.tag == "Mesh":
-                v, t, uv = load_obj(os.path.join(base, a["filename"]), with_uv=True)
-                d.add(apply_transform(M, v), t, shader_of(node), light, uv=uv)
+                v, t, uv, nr = load_obj_attributes(os.path.join(base, a["filename"]))
+                d.add(apply_transform(M, v), t, shader_of(node), light, uv=uv,
+                      normals=None if nr is None else apply_normal_transform(M, nr))
             elif node.tag == "Triangle":
                 v = np.stack([a["verta"], a["vertb"], a["vertc"]])
                 d.add(apply_transform(M, v), np.array([[0, 1, 2]], np.uint32), shader_of(node), light)
@@ -419,7 +445,8 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             elif node.tag == "Sphere":
                 cr = a["center_n_radius"]
                 v, sf, uv = sphere_mesh(cr[:3], cr[3])
-                d.add(apply_transform(M, v), sf, shader_of(node), light, uv=uv)
+                d.add(apply_transform(M, v), sf, shader_of(node), light, uv=uv,
+                      normals=apply_normal_transform(M, v - np.asarray(cr[:3], np.float32)))
                 out.warnings.append("<Sphere> tessellated to an icosphere of %d triangles" % len(sf))
             elif node.tag != "PointLight":  # read with the lights above
                 out.warnings.append(f"<{node.tag}> in <Objects> is not supported and was skipped")

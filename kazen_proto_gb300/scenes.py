@@ -39,13 +39,18 @@ class SceneDesc:
     env: tuple = (0.0, 0.0, 0.0)
     env_texture: int = -1
     point_lights: list = field(default_factory=list)   # (position, radiance)
+    normals: dict = field(default_factory=dict)        # mesh index -> (nverts, 3) f32 unit normals
 
-    def add(self, verts, idx, material_id, is_light=False, uv=None) -> int:
+    def add(self, verts, idx, material_id, is_light=False, uv=None, normals=None) -> int:
         self.meshes.append((np.asarray(verts, np.float32).reshape(-1, 3), np.asarray(idx, np.uint32).reshape(-1, 3),
                             int(material_id), bool(is_light)))
+        g = len(self.meshes) - 1
         if uv is not None:
-            self.uvs[len(self.meshes) - 1] = np.asarray(uv, np.float32).reshape(-1, 2)
-        return len(self.meshes) - 1
+            self.uvs[g] = np.asarray(uv, np.float32).reshape(-1, 2)
+        if normals is not None:
+            n = np.asarray(normals, np.float64).reshape(-1, 3)
+            self.normals[g] = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+        return g
 
     def material_array(self):
         arr = np.zeros(len(self.materials), dtype=api.N.MATERIAL_DTYPE)
@@ -62,6 +67,8 @@ class SceneDesc:
             s.add_mesh(v, i, mat, light)
             if g in self.uvs:
                 s.set_mesh_uvs(g, self.uvs[g])
+            if g in self.normals:
+                s.set_mesh_normals(g, self.normals[g])
         s.set_materials(self.material_array())
         for pos, rad in self.point_lights:
             s.add_point_light(pos, rad)
@@ -71,6 +78,24 @@ class SceneDesc:
             s.set_environment(self.env, self.env_texture)
         s.build_bvh()
         return s
+
+    def tri_normals(self):
+        """((N, 9) per-triangle vertex normals, (N,) has-normals flags) in global order, or None.
+        The normals are renormalised in FP32 as the library does."""
+        if not self.normals:
+            return None
+        nrm, has = [], []
+        for g, (v, i, _, _) in enumerate(self.meshes):
+            if g in self.normals:
+                n = self.normals[g].astype(np.float32)
+                ln = np.sqrt((n * n).sum(axis=1, dtype=np.float32), dtype=np.float32)
+                n = (n / ln[:, None]).astype(np.float32)
+                nrm.append(n[i].reshape(-1, 9))
+                has.append(np.ones(len(i), np.uint8))
+            else:
+                nrm.append(np.zeros((len(i), 9), np.float32))
+                has.append(np.zeros(len(i), np.uint8))
+        return np.concatenate(nrm).astype(np.float32), np.concatenate(has)
 
     def tri_uvs(self):
         """(N, 6) per-triangle vertex uvs in global order (barycentric defaults), or None."""

@@ -1274,6 +1274,8 @@ struct OScene {
     std::vector<kz_material> materials;
     std::vector<OLight> lights;
     std::vector<float> tri_uv;        // 6 floats per triangle (global order), or empty
+    std::vector<float> tri_nrm;       // 9 floats per triangle (global order), or empty
+    std::vector<uint8_t> tri_has_nrm; // per triangle: its mesh has vertex normals
     std::vector<OTexture> textures;
     V3 env{0, 0, 0};
     int env_tex = -1;
@@ -1409,6 +1411,19 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         V3 v0 = sc.bvh.v(prim, 0), v1 = sc.bvh.v(prim, 1), v2 = sc.bvh.v(prim, 2);
         V3 Ng = normalize(cross(v1 - v0, v2 - v0));
         V3 P = o + d * t;
+        // shading normal and shadow-terminator offset, TriangleMesh::post_hit
+        // (shape.cpp:628-656): P' = P_bary - sum_i b_i min(0, (P_bary - v_i).n_i) n_i
+        V3 Ns = Ng;
+        if (!sc.tri_has_nrm.empty() && sc.tri_has_nrm[prim]) {
+            const float* q = &sc.tri_nrm[(size_t)prim * 9];
+            V3 n0(q[0], q[1], q[2]), n1(q[3], q[4], q[5]), n2(q[6], q[7], q[8]);
+            float b0 = 1.f - bu - bv;
+            Ns = normalize(n0 * b0 + n1 * bu + n2 * bv);
+            V3 Pb = v0 * b0 + v1 * bu + v2 * bv;
+            float e0 = std::min(0.f, dot(Pb - v0, n0)), e1 = std::min(0.f, dot(Pb - v1, n1)),
+                  e2 = std::min(0.f, dot(Pb - v2, n2));
+            P = Pb - (n0 * (b0 * e0) + n1 * (bu * e1) + n2 * (bv * e2));
+        }
         // texture tint at the hit's uv (vertex uvs interpolated by the hit's
         // barycentrics; the barycentrics themselves for meshes without uvs)
         const int mtex = sc.textures.empty() ? -1 : material_texture(mat);
@@ -1422,11 +1437,11 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
             }
             tint = texture_lookup(sc.textures[(size_t)mtex], b0 * s0 + bu * s1 + bv * s2, b0 * t0 + bu * t1 + bv * t2);
         }
-        Frame fr(Ng);
+        Frame fr(Ns);
         V3 wi = -fr.to_local(d);
-        // 1. emission on hit (front side only, single_emissive_surface)
+        // 1. emission on hit (front side of the shading normal, single_emissive_surface)
         V3 Le(mat.Le[0], mat.Le[1], mat.Le[2]);
-        if (!is_zero(Le) && dot(d, Ng) < 0.f) {
+        if (!is_zero(Le) && dot(d, Ns) < 0.f) {
             float w = 1.f;
             if (!prev_specular) {
                 int li = sc.geom_light[geom];
@@ -1716,6 +1731,14 @@ void* kzo_scene_create(const float* tri_verts, uint32_t ntris, const uint32_t* t
 }
 
 void kzo_scene_free(void* h) { delete static_cast<OScene*>(h); }
+
+// Vertex normals per triangle (9 floats, global order) and a per-triangle
+// flag (0: the mesh has none, shade with the geometric normal).
+void kzo_scene_set_normals(void* h, const float* tri_nrm, const uint8_t* has) {
+    OScene* s = static_cast<OScene*>(h);
+    s->tri_nrm.assign(tri_nrm, tri_nrm + (size_t)s->bvh.ntris * 9);
+    s->tri_has_nrm.assign(has, has + s->bvh.ntris);
+}
 
 // Point lights follow the area lights in the light list.
 void kzo_scene_add_point_light(void* h, const float* position, const float* radiance) {

@@ -50,6 +50,7 @@ def lib():
             "kzo_scene_free": (None, [_P]),
             "kzo_scene_set_textures": (None, [_P, _P, C.c_uint32, _P, _P, C.c_int32]),
             "kzo_scene_add_point_light": (None, [_P, _P, _P]),
+            "kzo_scene_set_normals": (None, [_P, _P, _P]),
             "kzo_render": (None, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(RenderConfig), C.c_int,
                                   C.c_uint32, C.c_uint32, _P, _P]),
             "kzo_camera_rays": (None, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P]),
@@ -180,6 +181,11 @@ class Scene:
     def from_desc(cls, desc):
         tv, tg, gm, gl = desc.flatten()
         sc = cls(tv, tg, gm, gl, desc.material_array())
+        nrm = desc.tri_normals() if hasattr(desc, "tri_normals") else None
+        if nrm is not None:
+            sc._nrm = np.ascontiguousarray(nrm[0], np.float32)
+            sc._has = np.ascontiguousarray(nrm[1], np.uint8)
+            lib().kzo_scene_set_normals(sc.h, _p(sc._nrm), _p(sc._has))
         for pos, rad in getattr(desc, "point_lights", []):
             lib().kzo_scene_add_point_light(sc.h, _p(np.ascontiguousarray(pos, np.float32)),
                                             _p(np.ascontiguousarray(rad, np.float32)))

@@ -47,7 +47,8 @@ def main():
                     "textures": [("checker" if t.kind == N.KZ_TEX_CHECKER else "image %dx%d" % t.image.shape[1::-1])
                                  for t in d.textures],
                     "environment": {"rgb": [round(float(x), 6) for x in d.env], "texture": d.env_texture},
-                    "meshes_with_uv": len(d.uvs), "point_lights": len(d.point_lights)}
+                    "meshes_with_uv": len(d.uvs), "meshes_with_normals": len(d.normals),
+                    "point_lights": len(d.point_lights)}
     dst = os.path.join(HERE, "reference_scenes_summary.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)

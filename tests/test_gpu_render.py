@@ -205,6 +205,28 @@ def test_point_lights_render(gpu, oracle_mod, with_area):
     assert rel_mse(img, ref) <= REL_MSE_TOL
 
 
+def test_shading_normals_render(gpu, oracle_mod):
+    """Smooth spheres (icospheres with radial vertex normals: interpolated
+    shading normals and the shadow-terminator offset), one diffuse, one
+    mirror, one glass, next to flat meshes, against the restatement."""
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    d.materials.append(api.material([api.mirror((0.9, 0.9, 0.9))]))
+    d.materials.append(api.material([api.dielectric(1.5, 1.0)]))
+    sv, sf = scenes.icosphere(2)
+    for k, (c, r, m) in enumerate([((0.3, 0.15, 0.3), 0.15, 2), ((0.7, 0.45, 0.35), 0.12, len(d.materials) - 2),
+                                    ((0.5, 0.2, 0.7), 0.14, len(d.materials) - 1)]):
+        d.add(sv * r + np.asarray(c, np.float32), sf, m, normals=sv)
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=6, seed=11).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=11)
+    assert np.isfinite(img).all()
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+    flat = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    flat.materials, flat.meshes = d.materials, d.meshes  # the same meshes without normals
+    img_flat = api.Renderer(spp=8, max_depth=6, seed=11).render(flat.build(), d.camera, 40, 40)
+    assert rel_mse(img, img_flat) > 1e-4
+
+
 def test_terrain_scene_small(gpu, oracle_mod):
     d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
     s = d.build()

@@ -165,3 +165,15 @@ def test_point_light_validation_on_host(native_lib):
         s.add_point_light((0, np.nan, 0), (1, 1, 1))
     with pytest.raises(N.KazenError):
         s.add_point_light((0, 1, 0), (1, -1, 1))
+
+
+def test_normals_validation_on_host(native_lib):
+    s = api.Scene()
+    g = s.add_mesh(np.eye(3, dtype=np.float32), [[0, 1, 2]], material_id=0)
+    with pytest.raises(N.KazenError):  # count must match the vertices
+        s.set_mesh_normals(g, np.ones((2, 3), np.float32))
+    with pytest.raises(N.KazenError):  # a zero normal has no direction
+        s.set_mesh_normals(g, np.array([[0, 0, 1], [0, 0, 0], [0, 0, 1]], np.float32))
+    with pytest.raises(N.KazenError):
+        s.set_mesh_normals(g, np.array([[0, 0, 1], [0, np.inf, 0], [0, 0, 1]], np.float32))
+    s.set_mesh_normals(g, np.array([[0, 0, 2], [0, 1, 1], [1, 0, 0]], np.float32))

@@ -228,3 +228,27 @@ def test_textured_fixture():
     assert ids == [(N.KZ_CLOSURE_DIFFUSE, 1), (N.KZ_CLOSURE_KP_PRINCIPLE_DIFFUSE, 2),
                    (N.KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT, 0)]
     assert sorted(d.uvs) == [0, 1, 2, 3]
+
+
+def test_obj_normals_split_and_transform(tmp_path):
+    (tmp_path / "n.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nvn 0 0 1\nvn 0 0.6 0.8\n"
+                                    "f 1//1 2//1 3//1\nf 2//2 4//2 3//1\n")
+    v, t, uv, n = X.load_obj_attributes(str(tmp_path / "n.obj"))
+    assert uv is None and len(v) == 5 and n.shape == (5, 3)  # vertex 2 carries two normals
+    corners = {tuple(np.round(np.concatenate([v[i], n[i]]).astype(np.float64), 3)) for i in t.reshape(-1)}
+    assert (1.0, 0.0, 0.0, 0.0, 0.6, 0.8) in corners and (1.0, 0.0, 0.0, 0.0, 0.0, 1.0) in corners
+    # a mirroring, non-uniform scale: normals follow the inverse transpose
+    M = X.mesh_transform(scale=np.array([-1.0, 2.0, 1.0]))
+    nn = X.apply_normal_transform(M, np.array([[0.0, 0.6, 0.8]]))
+    want = np.array([0.0, 0.3, 0.8]) / np.linalg.norm([0.0, 0.3, 0.8])
+    assert np.allclose(nn[0], want, atol=1e-6)
+
+
+def test_sphere_objects_carry_normals(tmp_path):
+    mats = '<ShaderGroupBegin name="m"/><Shader name="matte" layer="a"/><ShaderGroupEnd/>'
+    p = _scene_dir(tmp_path, {"matte": "surface matte ( color Cs = 1 ) { Ci = Cs * diffuse(N); }"}, mats,
+                   '<Sphere center_n_radius="float4 1 2 3 0.5" shader_name="m"/>')
+    d = X.load(p).desc
+    v, n = d.meshes[0][0], d.normals[0]
+    assert np.allclose(np.linalg.norm(n, axis=1), 1, atol=1e-6)
+    assert np.allclose((v - [1, 2, 3]) / 0.5, n, atol=1e-5)
