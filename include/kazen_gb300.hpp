@@ -61,6 +61,21 @@ public:
         return gid;
     }
     void set_materials(const std::vector<kz_material>& m) { check(kz_scene_set_materials(h_, m.data(), (uint32_t)m.size())); }
+    // Per-vertex normals / texture coordinates of a mesh (TriangleMesh norms / uvs, src/core/shape.h)
+    void set_mesh_normals(int32_t gid, const std::vector<float>& n) {
+        check(kz_scene_set_mesh_normals(h_, gid, n.data(), (uint32_t)(n.size() / 3)));
+    }
+    void set_mesh_uvs(int32_t gid, const std::vector<float>& uv) {
+        check(kz_scene_set_mesh_uvs(h_, gid, uv.data(), (uint32_t)(uv.size() / 2)));
+    }
+    void set_textures(const std::vector<kz_texture>& t) { check(kz_scene_set_textures(h_, t.data(), (uint32_t)t.size())); }
+    void set_environment(const float rgb[3], int32_t texture = -1) { check(kz_scene_set_environment(h_, rgb, texture)); }
+    // PointLight(position, radiance) (src/core/light.h:51-71); returns its index among the point lights
+    int32_t add_point_light(const float position[3], const float radiance[3]) {
+        int32_t id = -1;
+        check(kz_scene_add_point_light(h_, position, radiance, &id));
+        return id;
+    }
     // Scene::build_bvh / Accelerator::build
     void build_bvh() { check(kz_scene_build(h_)); }
     kz_scene* handle() const { return h_; }

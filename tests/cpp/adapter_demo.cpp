@@ -20,7 +20,14 @@ int main() {
     kz_material light{};
     light.Le[0] = light.Le[1] = light.Le[2] = 3.f;
     scene.add_mesh({-1, 2, -1, -1, 2, 1, 1, 2, 1, 1, 2, -1}, {0, 1, 2, 0, 2, 3}, 1, true);
+    // vertex normals equal to the face normal: the same shading through the attribute path
+    scene.set_mesh_normals(0, {0, 1, 0, 0, 1, 0, 0, 1, 0});
     scene.set_materials({m, light});
+    {
+        kz::Scene other;  // host-side calls of the remaining wrappers
+        const float p[3] = {0, 5, 0}, rad[3] = {1, 1, 1};
+        if (other.add_point_light(p, rad) != 0) return 2;
+    }
     scene.build_bvh();
     kz::GpuAccel accel(scene);
     const float o[3] = {0, 1, 0}, d[3] = {0, -1, 0};
