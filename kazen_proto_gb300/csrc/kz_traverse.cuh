@@ -227,18 +227,9 @@ struct ClosestState {
     uint32_t prim;
     int32_t rec;
     uint32_t gbase, gbits;  // current node group
-    uint32_t tbase, tbits;  // pending triangle group (postponed leaf tests)
     uint32_t visits;
     int sp;
 };
-
-// Postponed leaf tests (Ylitie et al. 2017, sec. 4): after a node visit, a
-// lane whose warp has fewer than 1/KZ_POSTPONE of its active lanes with leaf
-// triangles pushes its triangle group on the stack (marked by bit 31 of the
-// first word) and keeps traversing; the group is tested when popped. 0 = off.
-#ifndef KZ_POSTPONE
-#define KZ_POSTPONE 0
-#endif
 
 __device__ __forceinline__ void closest_begin(ClosestState& c, float tmax) {
     c.t = tmax;
@@ -248,7 +239,6 @@ __device__ __forceinline__ void closest_begin(ClosestState& c, float tmax) {
     c.rec = -1;
     c.gbase = 0;
     c.gbits = 0x80000000u;  // the root as the only child of a virtual node
-    c.tbase = c.tbits = 0;
     c.visits = 0;
     c.sp = 0;
 }
@@ -261,30 +251,17 @@ __device__ __forceinline__ void closest_begin(ClosestState& c, float tmax) {
 template <bool kCount>
 __device__ __forceinline__ int closest_step(const DevScene& s, const TRay& r, uint32_t octp, ClosestState& c,
                                             uint2* stack, uint32_t& nnode, uint32_t& ntri) {
-    uint32_t tri_base = c.tbase, tbits = c.tbits;
-    c.tbits = 0;
-    if (!tbits) {
-        const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
-        if (c.gbits > 0x00FFFFFFu) {
-            if (c.sp >= kWideStack) return -1;
-            stack[c.sp++] = make_uint2(c.gbase, c.gbits);
-        }
-        if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
-        uint32_t imask;
-        const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, c.t, c.gbase, tri_base, imask);
-        if (kCount) ++nnode;
-        c.gbits = (hm & 0xFF000000u) | imask;
-        tbits = hm & 0x00FFFFFFu;
-#if KZ_POSTPONE > 0
-        const uint32_t act = __activemask();
-        const uint32_t want = __ballot_sync(act, tbits != 0u);
-        if (tbits && (uint32_t)__popc(want) * KZ_POSTPONE < (uint32_t)__popc(act)) {
-            if (c.sp >= kWideStack) return -1;
-            stack[c.sp++] = make_uint2(0x80000000u | tri_base, tbits);
-            tbits = 0;
-        }
-#endif
+    const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
+    if (c.gbits > 0x00FFFFFFu) {
+        if (c.sp >= kWideStack) return -1;
+        stack[c.sp++] = make_uint2(c.gbase, c.gbits);
     }
+    if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
+    uint32_t tri_base, imask;
+    const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, c.t, c.gbase, tri_base, imask);
+    if (kCount) ++nnode;
+    c.gbits = (hm & 0xFF000000u) | imask;
+    uint32_t tbits = hm & 0x00FFFFFFu;
     while (tbits) {
         const uint32_t rec = tri_base + (__ffs(tbits) - 1);
         tbits &= tbits - 1u;
@@ -306,13 +283,6 @@ __device__ __forceinline__ int closest_step(const DevScene& s, const TRay& r, ui
     }
     while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
         const uint2 e = stack[--c.sp];
-#if KZ_POSTPONE > 0
-        if (e.x & 0x80000000u) {  // a postponed triangle group: test it next step
-            c.tbase = e.x & 0x7FFFFFFFu;
-            c.tbits = e.y;
-            return 0;
-        }
-#endif
         c.gbase = e.x;
         c.gbits = e.y;
     }
