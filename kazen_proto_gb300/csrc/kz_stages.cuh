@@ -116,7 +116,7 @@ __device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long
 template <bool kCount, typename Ctr, typename Load, typename Store>
 __device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
                                                    Store store, uint32_t& dn, uint32_t& dt) {
-    uint2 stack[kWideStack];
+    KZ_CLOSEST_STACK(stack);
     ClosestState c;
     TRay r;
     float tmax = 0.f;

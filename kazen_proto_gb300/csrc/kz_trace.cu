@@ -125,7 +125,8 @@ __global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, Sha
                                                                  float* film, double* film64, VRec* recs, NRec* nee,
                                                                  uint32_t max_depth) {
     uint32_t dn = 0, dt = 0;
-    uint2 stack[kWideStack];
+    uint2 stack_lm[kWideStack];
+    const LocalStack stack{stack_lm};
     AnyState c;
     TRay r;
     float tmax = 0.f;
@@ -181,7 +182,8 @@ __global__ void __launch_bounds__(256) k_trace_paths_batch(const DevJob* __restr
 __global__ void __launch_bounds__(256) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
                                                             DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
-    uint2 stack[kWideStack];
+    uint2 stack_lm[kWideStack];
+    const LocalStack stack{stack_lm};
     AnyState c;
     TRay r;
     DevScene ls;

@@ -218,6 +218,27 @@ __device__ __forceinline__ uint32_t wide_pop_child(uint32_t base, uint32_t& bits
     return base + __popc(bits & ((1u << slot) - 1u));
 }
 
+// Traversal stack of node groups: a per-thread local array (LocalStack), or
+// its first kSmem entries in shared memory, entry i of thread t at
+// i * blockDim.x + t, and the rest local (SplitStack).
+struct LocalStack {
+    uint2* p;
+    __device__ __forceinline__ uint2 get(int i) const { return p[i]; }
+    __device__ __forceinline__ void put(int i, uint2 e) const { p[i] = e; }
+};
+template <int kSmem>
+struct SplitStack {
+    uint2* sm;
+    uint2* lm;
+    __device__ __forceinline__ uint2 get(int i) const {
+        return i < kSmem ? sm[i * blockDim.x + threadIdx.x] : lm[i - kSmem];
+    }
+    __device__ __forceinline__ void put(int i, uint2 e) const {
+        if (i < kSmem) sm[i * blockDim.x + threadIdx.x] = e;
+        else lm[i - kSmem] = e;
+    }
+};
+
 // Closest-hit traversal state, advanced one node at a time (closest_step) so
 // that persistent kernels can interleave rays; trace_closest runs it to the
 // end. The barycentric divisions are deferred to closest_finish (the same
@@ -248,13 +269,13 @@ __device__ __forceinline__ void closest_begin(ClosestState& c, float tmax) {
 // overflow (the builder bounds the depth by the stack size), more nodes are
 // visited than the tree holds, or a record index is out of range (a corrupt
 // node array).
-template <bool kCount>
+template <bool kCount, typename Stack>
 __device__ __forceinline__ int closest_step(const DevScene& s, const TRay& r, uint32_t octp, ClosestState& c,
-                                            uint2* stack, uint32_t& nnode, uint32_t& ntri) {
+                                            const Stack& stack, uint32_t& nnode, uint32_t& ntri) {
     const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
     if (c.gbits > 0x00FFFFFFu) {
         if (c.sp >= kWideStack) return -1;
-        stack[c.sp++] = make_uint2(c.gbase, c.gbits);
+        stack.put(c.sp++, make_uint2(c.gbase, c.gbits));
     }
     if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
     uint32_t tri_base, imask;
@@ -282,7 +303,7 @@ __device__ __forceinline__ int closest_step(const DevScene& s, const TRay& r, ui
         }
     }
     while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
-        const uint2 e = stack[--c.sp];
+        const uint2 e = stack.get(--c.sp);
         c.gbase = e.x;
         c.gbits = e.y;
     }
@@ -316,7 +337,7 @@ __device__ bool trace_closest(const DevScene& s, const TRay& r, float tmax, HitR
     closest_begin(c, tmax);
     int rc;
     do {
-        rc = closest_step<kCount>(s, r, octp, c, stack, nnode, ntri);
+        rc = closest_step<kCount>(s, r, octp, c, LocalStack{stack}, nnode, ntri);
     } while (rc == 0);
     closest_finish(c, rc > 0, tmax, h);
     return rc > 0;
@@ -338,13 +359,13 @@ __device__ __forceinline__ void any_begin(AnyState& c) {
 
 // One node of an any-hit query in (tmin, tmax]: 0 while nodes remain, 1 no
 // hit (complete), 2 hit, -1 abort (as closest_step).
-template <bool kCount>
+template <bool kCount, typename Stack>
 __device__ __forceinline__ int any_step(const DevScene& s, const TRay& r, uint32_t octp, float tmax, AnyState& c,
-                                        uint2* stack, uint32_t& nnode, uint32_t& ntri) {
+                                        const Stack& stack, uint32_t& nnode, uint32_t& ntri) {
     const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
     if (c.gbits > 0x00FFFFFFu) {
         if (c.sp >= kWideStack) return -1;
-        stack[c.sp++] = make_uint2(c.gbase, c.gbits);
+        stack.put(c.sp++, make_uint2(c.gbase, c.gbits));
     }
     if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
     uint32_t tri_base, imask;
@@ -363,7 +384,7 @@ __device__ __forceinline__ int any_step(const DevScene& s, const TRay& r, uint32
             return 2;
     }
     while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
-        const uint2 e = stack[--c.sp];
+        const uint2 e = stack.get(--c.sp);
         c.gbase = e.x;
         c.gbits = e.y;
     }
@@ -381,7 +402,7 @@ __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& ov
     any_begin(c);
     int rc;
     do {
-        rc = any_step<kCount>(s, r, octp, tmax, c, stack, nnode, ntri);
+        rc = any_step<kCount>(s, r, octp, tmax, c, LocalStack{stack}, nnode, ntri);
     } while (rc == 0);
     overflow = rc < 0;
     return rc == 2;
@@ -395,6 +416,25 @@ __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& ov
 // Every traversal is bounded, so a warp leaves once the queue [0, n) is
 // drained. Refilling only in groups (8 lanes) keeps the set-up code from
 // running for one or two lanes at a time.
+// Stack entries of a persistent closest-hit thread kept in shared memory
+// (16 KB per block of 256 threads at 8). Measured: the terrain frame's trace
+// stage 130.6 -> 129.7 ms, the incoherent-ray microbenchmark 1.190 -> 1.242
+// Grays/s; the any-hit kernels keep the local stack (their frame stage lost
+// 1 % with it).
+#ifndef KZ_SMEM_STACK
+#define KZ_SMEM_STACK 8
+#endif
+#if KZ_SMEM_STACK > 0
+#define KZ_CLOSEST_STACK(name)                       \
+    __shared__ uint2 name##_sm[KZ_SMEM_STACK * 256]; \
+    uint2 name##_lm[kWideStack - KZ_SMEM_STACK];     \
+    const SplitStack<KZ_SMEM_STACK> name{name##_sm, name##_lm}
+#else
+#define KZ_CLOSEST_STACK(name)   \
+    uint2 name##_lm[kWideStack]; \
+    const LocalStack name { name##_lm }
+#endif
+
 #ifndef KZ_TRACE_REFILL
 #define KZ_TRACE_REFILL 8
 #endif
