@@ -275,8 +275,13 @@ __device__ __forceinline__ f3 refract_u(f3 wi, f3 n, float eta) {
 // lobe_eval and lobe_sample stay out of line: one copy of the 21-way lobe
 // switch per kernel instead of one per call site (the shading kernels call
 // them from three loops). Measured on the terrain frame: shading 42.1 ->
-// 40.4 ms, the instruction-cache stalls being the shading kernel's first.
+// 40.4 ms, the instruction-cache stalls being the shading kernel's first. A
+// translation unit that defines KZ_LOBE_INLINE inlines them instead.
+#ifdef KZ_LOBE_INLINE
+#define KZ_LOBE_FN __device__ inline
+#else
 #define KZ_LOBE_FN static __device__ __noinline__
+#endif
 
 struct LobeEval {
     f3 f;
