@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--no-traversal", action="store_true")
     p.add_argument("--no-guiding", action="store_true")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-features", action="store_true")
     p.add_argument("--profile-guide", action="store_true",
                    help="one small guided render with training (slit room 128x128, 32 spp), for ncu captures "
                         "of the guiding network kernels; prints its stats and exits")
@@ -237,6 +238,114 @@ def traversal_bench(steps, warmup):
     res["bvh_nodes"] = info["n_bvh_nodes"]
     res["bvh_depth"] = info["bvh_depth"]
     s.close()
+    return res
+
+
+# ---------------------------------------------------------------- the widened rows
+def features_bench(W=960, H=540, spp=16, max_depth=8, frames=3):
+    """Scene-file loading, the vertex-attribute shading variant and the closure
+    kernels, each measured on its own (not part of the headline):
+    * XML + OBJ + OSL lowering of the two scene fixtures (host seconds);
+    * the terrain frame at 960x540, 16 spp with a checkerboard-textured
+      terrain and smooth (vertex-normal) spheres, against the same frame
+      plain: Mpaths*bounces/s of each, device-resident, L2 flushed;
+    * kz_closure_eval_batch / kz_closure_sample_batch over 21 closure kinds
+      (2^22 random lobes, device buffers): lobes per second."""
+    import time
+
+    import torch
+
+    from kazen_proto_gb300 import _native as N
+    from kazen_proto_gb300 import api, scene_xml, scenes
+    here = os.path.dirname(os.path.abspath(__file__))
+    res = {}
+    for name in ("box_room", "textured_room"):
+        t0 = time.perf_counter()
+        L = scene_xml.load(os.path.join(here, "tests", "golden", "scenes", name, "scene.xml"))
+        res[f"load_{name}_s"] = round(time.perf_counter() - t0, 4)
+        res[f"load_{name}_triangles"] = int(L.desc.n_triangles())
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    rgb = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+
+    def frame_rate(desc):
+        s = desc.build()
+        stream = torch.cuda.Stream()
+        s.set_stream(stream)
+        r = api.Renderer(spp=spp, max_depth=max_depth, seed=5)
+        r.render(s, desc.camera, W, H, device_out=(rgb, None))
+        s.synchronize()
+        ms, bounces = 0.0, 0
+        for _ in range(frames):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r.render(s, desc.camera, W, H, device_out=(rgb, None))
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+            bounces += r.last_stats["path_bounces"]
+        s.close()
+        return bounces / (ms / 1e3) / 1e6
+
+    plain = scenes.terrain_scene(W, H, spp, max_depth)
+    res["terrain_plain_mpaths_bounces_per_s"] = round(frame_rate(plain), 1)
+    feat = scenes.terrain_scene(W, H, spp, max_depth)
+    feat.textures = [api.checker_texture(64, 64, (0.7, 0.7, 0.65), (0.3, 0.3, 0.35))]
+    feat.materials[0] = api.material([api.textured(api.diffuse((0.8, 0.8, 0.8)), 0)])
+    for g in range(1, len(feat.meshes)):
+        v, i, m, light = feat.meshes[g]
+        if not light:  # the icospheres: radial vertex normals about their centroid
+            n = v - v.mean(axis=0)
+            feat.normals[g] = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+    res["terrain_textured_smooth_mpaths_bounces_per_s"] = round(frame_rate(feat), 1)
+    res["terrain_frame"] = f"{W}x{H}, {spp} spp, depth {max_depth}"
+
+    rng = np.random.default_rng(3)
+    n = 1 << 22
+    a, e = 0.3, 1.4
+    kinds = [api.diffuse(), api.mirror(), api.dielectric(1.5, 1.0), api.microfacet("ggx", a, 0.5 * a, e, 0),
+             api.microfacet("beckmann", a, a, e, 0), api.microfacet("ggx", a, a, e, 1),
+             api.microfacet("beckmann", a, a, e, 2), api.conductor_ggx((0.9, 0.6, 0.5), a),
+             api.principle_specular((0.1, 0.1, 0.1), a, e, 0.3), api.phong(30.0), api.ward(a), api.ward(a, 0.5 * a),
+             api.reflection(e), api.refraction(e), api.transparent(), api.translucent(),
+             api.kp_microfacet(a, 1.5, 1.0, 0.4), api.principle_diffuse(), api.principle_retro(0.5),
+             api.principle_fakess(0.5), api.principle_clearcoat(0.1)]
+    rec = np.array([kinds[k % len(kinds)] for k in range(1 << 16)], dtype=N.LOBE_DTYPE)
+    lobes = torch.from_numpy(rec.view(np.uint8).reshape(1 << 16, -1)).cuda().repeat(n >> 16, 1)
+
+    def dirs(m):
+        d = rng.standard_normal((m, 3)).astype(np.float32)
+        return d / np.linalg.norm(d, axis=1, keepdims=True)
+    wi = torch.from_numpy(np.tile(dirs(1 << 16), (n >> 16, 1))).cuda()
+    wo = torch.from_numpy(np.tile(dirs(1 << 16), (n >> 16, 1))).cuda()
+    u = torch.rand((n, 3), device="cuda")
+    f = torch.empty((n, 3), device="cuda")
+    pdf = torch.empty(n, device="cuda")
+    w3 = torch.empty((n, 3), device="cuda")
+    fl = torch.empty(n, dtype=torch.uint8, device="cuda")
+    lib = N.lib()
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    P = lambda t: t.data_ptr()  # noqa: E731
+    ev = timed(lambda: N.check(lib.kz_closure_eval_batch(P(lobes), P(wi), P(wo), n, N.KZ_CONVENTION_INTEGRATOR,
+                                                         P(f), P(pdf), N.KZ_MEM_DEVICE)))
+    sm = timed(lambda: N.check(lib.kz_closure_sample_batch(P(lobes), P(wi), P(u), n, P(wo), P(w3), P(pdf), P(fl),
+                                                           N.KZ_MEM_DEVICE)))
+    res["closure_eval_globes_per_s"] = round(n / (ev / 1e3) / 1e9, 3)
+    res["closure_sample_globes_per_s"] = round(n / (sm / 1e3) / 1e9, 3)
+    res["closure_batch"] = f"{n} lobes of {len(kinds)} closure kinds, device buffers"
     return res
 
 
@@ -458,6 +567,10 @@ def run_ours(args):
     if rank == 0 and not args.no_batch and not args.small and not args.profile:
         batch = batch_bench()
 
+    feats = None
+    if rank == 0 and not args.no_features and not args.small and not args.profile:
+        feats = features_bench()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
@@ -503,6 +616,7 @@ def run_ours(args):
         "traversal": trav,
         "guiding": guide,
         "batch": batch,
+        "features": feats,
     }
     if img is not None:
         line["image_mean"] = float(np.mean(img))
