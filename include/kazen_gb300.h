@@ -186,6 +186,14 @@ typedef struct kz_render_config {
 /* Trace with the fetch-counting traversal variant and report BVH node and
  * triangle fetches (slower; for roofline accounting, not for timing). */
 #define KZ_RENDER_FLAG_COUNT  2u
+/* Estimator of kz_render / kz_li_batch (default: next-event estimation and
+ * BSDF sampling combined by MIS, PathIntegrator, integrator.cpp:362-561).
+ * NEE_ONLY is PathEmsIntegrator (integrator.cpp:264-360): lights found by
+ * BSDF-sampled rays count only after a specular bounce or from the camera.
+ * BSDF_ONLY is PathMatsIntegrator (integrator.cpp:213-262): no next-event
+ * estimation, every emission hit counts in full. At most one of the two. */
+#define KZ_RENDER_FLAG_NEE_ONLY  4u
+#define KZ_RENDER_FLAG_BSDF_ONLY 8u
 
 typedef struct kz_render_stats {
     uint64_t path_bounces;   /* closest-hit extension rays traced (camera rays included) */

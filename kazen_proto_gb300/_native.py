@@ -98,6 +98,8 @@ class KzRenderConfig(C.Structure):
 
 KZ_RENDER_FLAG_TIMING = 1
 KZ_RENDER_FLAG_COUNT = 2
+KZ_RENDER_FLAG_NEE_ONLY = 4
+KZ_RENDER_FLAG_BSDF_ONLY = 8
 
 
 class KzRenderStats(C.Structure):

@@ -317,6 +317,7 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
     pp.rr_min = cfg->rr_min_depth;
     pp.seed = cfg->seed;
     pp.camera = cam ? 1u : 0u;
+    pp.estimator = (cfg->flags & KZ_RENDER_FLAG_NEE_ONLY) ? 1u : (cfg->flags & KZ_RENDER_FLAG_BSDF_ONLY) ? 2u : 0u;
     if (pp_override) pp = *pp_override;
     uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
     const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(want, total), 1u << 30));
@@ -1087,6 +1088,8 @@ static kz_status check_cfg(const kz_render_config* cfg) {
     if (!cfg) return fail(KZ_ERR_INVALID_ARG, "cfg is NULL");
     if (cfg->spp == 0) return fail(KZ_ERR_INVALID_ARG, "spp must be >= 1");
     if (cfg->max_depth == 0 || cfg->max_depth > 255) return fail(KZ_ERR_INVALID_ARG, "max_depth must be in [1, 255]");
+    if ((cfg->flags & KZ_RENDER_FLAG_NEE_ONLY) && (cfg->flags & KZ_RENDER_FLAG_BSDF_ONLY))
+        return fail(KZ_ERR_INVALID_ARG, "KZ_RENDER_FLAG_NEE_ONLY and KZ_RENDER_FLAG_BSDF_ONLY exclude each other");
     return KZ_OK;
 }
 
@@ -1382,6 +1385,8 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     KZ_TRY(check_scene(s));
     KZ_TRY(check_cfg(cfg));
     if (cfg->max_depth > 16) return fail(KZ_ERR_INVALID_ARG, "guided rendering supports max_depth <= 16");
+    if (cfg->flags & (KZ_RENDER_FLAG_NEE_ONLY | KZ_RENDER_FLAG_BSDF_ONLY))
+        return fail(KZ_ERR_INVALID_ARG, "guided rendering combines the guide with the MIS estimator only");
     if (g->device != s->device) return fail(KZ_ERR_INVALID_ARG, "guide and scene live on different devices");
     if (!camera || !fd || !out_rgb) return fail(KZ_ERR_INVALID_ARG, "camera, film and out_rgb are required");
     if (fd->width == 0 || fd->height == 0) return fail(KZ_ERR_INVALID_ARG, "film size must be > 0");
@@ -1899,6 +1904,7 @@ extern "C" kz_status kz_li_batch_noalloc(kz_scene* s, const kz_ray* rays, uint64
     pp.rr_min = cfg->rr_min_depth;
     pp.seed = cfg->seed;
     pp.camera = 0;
+    pp.estimator = (cfg->flags & KZ_RENDER_FLAG_NEE_ONLY) ? 1u : (cfg->flags & KZ_RENDER_FLAG_BSDF_ONLY) ? 2u : 0u;
     const uint32_t cap = (uint32_t)std::min<uint64_t>(cfg->wavefront_size ? cfg->wavefront_size : kNoAllocCap, n);
     const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
     const bool count = (cfg->flags & KZ_RENDER_FLAG_COUNT) != 0;

@@ -131,6 +131,7 @@ struct PathParams {
     uint32_t rr_min;
     uint64_t seed;
     uint32_t camera;  // 1: paths start at the camera, 0: at rays[] (Li batch)
+    uint32_t estimator = 0;  // 0: NEE + BSDF sampling with MIS, 1: NEE only, 2: BSDF sampling only
 };
 
 // Counters the stage kernels update on the device.

@@ -326,12 +326,16 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
         const f3 Le = ld3(mat.Le);
         if (!is_zero(Le) && dot(d, Ns) < 0.f) {
             float w = 1.f;
-            if (!prev_spec) {
+            if (!prev_spec && pp.estimator != 2u) {
                 const int li = __ldg(s.geom_light + geom);
                 if (li >= 0) {
-                    const float cos_l = -dot(d, Ng);
-                    const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
-                    w = power_heuristic(prev_pdf, lpdf);
+                    if (pp.estimator == 1u) {
+                        w = 0.f;  // NEE only: after a non-specular bounce this light was sampled directly
+                    } else {
+                        const float cos_l = -dot(d, Ng);
+                        const float lpdf = (hit.x * hit.x) / (cos_l * s.lights[li].area) * (1.0f / (float)nl);
+                        w = power_heuristic(prev_pdf, lpdf);
+                    }
                 }
             }
             Lsum = Lsum + hmul(beta, Le) * w;
@@ -363,8 +367,8 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                                 mk(1.f / s.box_inv.x, 1.f / s.box_inv.y, 1.f / s.box_inv.z), mix);
         const float alpha = gs.alpha;
 
-        // 2. next-event estimation
-        if (nl > 0 && any_smooth && wsum > 0.f) {
+        // 2. next-event estimation (none when sampling the BSDF only)
+        if (pp.estimator != 2u && nl > 0 && any_smooth && wsum > 0.f) {
             const uint32_t li = min((uint32_t)(u[0] * (float)nl), nl - 1);
             const DevLight lt = s.lights[li];
             // a point light (PointLight, light.cpp:18-31) has no triangles:
@@ -403,7 +407,7 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                 }
                 if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
                 if (!is_zero(f)) {
-                    const float w = point ? 1.f : power_heuristic(lpdf, bpdf);
+                    const float w = point || pp.estimator == 1u ? 1.f : power_heuristic(lpdf, bpdf);
                     // PointLight::sample's falloff: radiance / (0.1 |d|^2)
                     const f3 Le_l = point ? ld3(lt.Le) * (1.f / (dist2 * 0.1f)) : ld3(lt.Le);
                     const f3 c = hmul(hmul(beta, f), Le_l) * (w / lpdf);

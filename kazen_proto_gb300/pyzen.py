@@ -18,8 +18,9 @@ Differences, each stated where it happens: shaders are lowered from their
 OSL source (load_oso_shader looks for name.osl, not the compiled .oso; shader
 networks and texture lookups lower as scene_xml lowers them, texture files
 relative to the working directory); spheres are
-tessellated (with the reference's parametric uv); every integrator type renders with the path
-integrator; the frame renders in one GPU call and on_tile_end then runs for
+tessellated (with the reference's parametric uv); PathEmsIntegrator and
+PathMatIntegrator render with the NEE-only and BSDF-only estimators, every
+other integrator type with the path integrator; the frame renders in one GPU call and on_tile_end then runs for
 each tile in tile order; tiles cover the film exactly (the reference's
 generate_tiles, film.cpp:66-78, gives the last row and column the nominal
 size and the others the remainder, which overlaps tiles and leaves pixels
@@ -52,6 +53,12 @@ class IntegratorType(enum.Enum):
     PathMatIntegrator = 3
     PathEmsIntegrator = 4
     PathIntegrator = 5
+
+
+# the integrators the GPU path renders as such (render-config flags)
+_ESTIMATOR_FLAGS = {IntegratorType.PathIntegrator: 0,
+                    IntegratorType.PathEmsIntegrator: _api.N.KZ_RENDER_FLAG_NEE_ONLY,
+                    IntegratorType.PathMatIntegrator: _api.N.KZ_RENDER_FLAG_BSDF_ONLY}
 
 
 # ---------------------------------------------------------------- concepts
@@ -149,7 +156,9 @@ class Scene:
         self._groups = {n: i for i, n in enumerate(L.material_names)}
         self._mirror_x = L.mirror_x
         self.warnings += L.warnings
-        self.integrator = IntegratorType.PathIntegrator
+        self.integrator = {"PathEmsIntegrator": IntegratorType.PathEmsIntegrator,
+                           "PathMatsIntegrator": IntegratorType.PathMatIntegrator}.get(L.integrator,
+                                                                                       IntegratorType.PathIntegrator)
         self.film = Film(L.desc.width, L.desc.height, 1, 1)
         self.film.generate_tiles()
         self._built = None  # built by build_bvh or the first render, as the reference defers it
@@ -171,7 +180,7 @@ class Scene:
 
     def set_integrator(self, kind: IntegratorType) -> None:
         self.integrator = kind
-        if kind != IntegratorType.PathIntegrator:
+        if kind not in _ESTIMATOR_FLAGS:
             self.warnings.append(f"{kind.name} renders with the path integrator")
 
     # -- shaders
@@ -304,7 +313,8 @@ class Renderer:
         if scene.desc.camera is None:
             raise RuntimeError("camera not set")
         film = scene.film
-        r = _api.Renderer(spp=self.sample_count, max_depth=self.max_depth, seed=self.seed)
+        r = _api.Renderer(spp=self.sample_count, max_depth=self.max_depth, seed=self.seed,
+                          flags=_ESTIMATOR_FLAGS.get(scene.integrator, 0))
         img = r.render(scene._built, scene.desc.camera, film.width, film.height)
         if scene._mirror_x:
             img = img[:, ::-1]

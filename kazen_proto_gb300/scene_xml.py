@@ -33,7 +33,9 @@ the GPU path renders:
   to an icosphere of 5,120 triangles with the reference's parametric uv);
   transforms compose as the reference's do, world = T * R * S * local,
   rotate = (axis xyz, degrees);
-* integrator tags are recorded; rendering always uses the path integrator.
+* integrator tags are recorded: PathEmsIntegrator and PathMatsIntegrator map to
+  the NEE-only and BSDF-only estimators (`LoadedScene.render_flags`), every
+  other integrator renders with the path integrator (with a warning).
 
 Shader files are looked up next to the scene, then in the reference's shader
 library directory (../../shader/src relative to the scene).
@@ -307,6 +309,11 @@ def sphere_mesh(center, radius, level=4):
 
 
 # ---------------------------------------------------------------- scene
+# integrator tags the GPU path renders as such: render-config flags
+ESTIMATOR_FLAGS = {"PathIntegrator": 0, "PathEmsIntegrator": N.KZ_RENDER_FLAG_NEE_ONLY,
+                   "PathMatsIntegrator": N.KZ_RENDER_FLAG_BSDF_ONLY}
+
+
 @dataclass
 class LoadedScene:
     desc: SceneDesc
@@ -314,6 +321,11 @@ class LoadedScene:
     integrator: str = "PathIntegrator"
     material_names: list = field(default_factory=list)
     warnings: list = field(default_factory=list)
+
+    @property
+    def render_flags(self) -> int:
+        """kz_render_config.flags of the scene's integrator (the path integrator's for the others)."""
+        return ESTIMATOR_FLAGS.get(self.integrator, 0)
 
     def postprocess(self, img):
         """Apply the camera's horizontal mirror to a rendered (H, W, 3) image."""
@@ -351,7 +363,7 @@ def load(path: str, spp: int = 16, max_depth: int = 5) -> LoadedScene:
             pass  # handled with its Shader siblings below
         elif tag.endswith("Integrator"):
             out.integrator = tag
-            if tag != "PathIntegrator":
+            if tag not in ESTIMATOR_FLAGS:
                 out.warnings.append(f"<{tag}> rendered with the path integrator")
         elif tag == "PointLight":
             # PointLight defaults: position (0, 5, 0) (light.h:53-56), radiance 0 unless given

@@ -1390,7 +1390,11 @@ struct PathCounters {
 // Random numbers: 9 per shaded vertex, in a fixed order, whatever branches run:
 //   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
 //   [5] lobe pick   [6,7,8] lobe sample
-V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_min, PathCounters& pc) {
+// est: 0 NEE + BSDF sampling with MIS (PathIntegrator), 1 NEE only
+// (PathEmsIntegrator, integrator.cpp:264-360), 2 BSDF sampling only
+// (PathMatsIntegrator, integrator.cpp:213-262).
+V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_min, PathCounters& pc,
+      int est = 0) {
     V3 L(0, 0, 0), beta(1, 1, 1);
     float prev_pdf = 0.f;
     bool prev_specular = true;
@@ -1443,12 +1447,16 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         V3 Le(mat.Le[0], mat.Le[1], mat.Le[2]);
         if (!is_zero(Le) && dot(d, Ns) < 0.f) {
             float w = 1.f;
-            if (!prev_specular) {
+            if (!prev_specular && est != 2) {
                 int li = sc.geom_light[geom];
                 if (li >= 0) {
-                    float cos_l = -dot(d, Ng);
-                    float lpdf = (t * t) / (cos_l * sc.lights[(size_t)li].area) * (1.0f / (float)nl);
-                    w = power_heuristic(prev_pdf, lpdf);
+                    if (est == 1) {
+                        w = 0.f;  // found by next-event estimation instead
+                    } else {
+                        float cos_l = -dot(d, Ng);
+                        float lpdf = (t * t) / (cos_l * sc.lights[(size_t)li].area) * (1.0f / (float)nl);
+                        w = power_heuristic(prev_pdf, lpdf);
+                    }
                 }
             }
             L = L + mul(beta, Le) * w;
@@ -1469,8 +1477,8 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         }
         if (wsum > 0.f)
             for (uint32_t i = 0; i < nlobes; ++i) lp[i] /= wsum;
-        // 2. next-event estimation
-        if (nl > 0 && any_smooth && wsum > 0.f) {
+        // 2. next-event estimation (not when sampling the BSDF only)
+        if (est != 2 && nl > 0 && any_smooth && wsum > 0.f) {
             uint32_t li = std::min((uint32_t)(u[0] * (float)nl), nl - 1);
             const OLight& lt = sc.lights[li];
             V3 p = lt.pos, nlgt(0, 0, 0);
@@ -1505,7 +1513,7 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
                 if (!is_zero(f)) {
                     pc.shadow++;
                     if (!sc.bvh.any(P, ldir, kRayEps, dist - kRayEps)) {
-                        float w = lt.point ? 1.f : power_heuristic(lpdf, bpdf);
+                        float w = lt.point || est == 1 ? 1.f : power_heuristic(lpdf, bpdf);
                         // PointLight::sample returns radiance / (0.1 |d|^2)
                         V3 Le = lt.point ? lt.Le * (1.f / (dist2 * 0.1f)) : lt.Le;
                         V3 c = mul(mul(beta, f), Le) * (w / lpdf);
@@ -1563,6 +1571,10 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         d = normalize(fr.to_world(smp.wo));
     }
     return L;
+}
+
+int estimator_of(const kz_render_config* cfg) {
+    return (cfg->flags & KZ_RENDER_FLAG_NEE_ONLY) ? 1 : (cfg->flags & KZ_RENDER_FLAG_BSDF_ONLY) ? 2 : 0;
 }
 
 }  // namespace
@@ -1796,7 +1808,7 @@ void kzo_render(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_
             rng.seed(cfg->seed, pix * spp + s);
             float jx = rng.nextf(), jy = rng.nextf();
             V3 d = cam_dir(cb, px, py, W, H, jx, jy);
-            V3 L = Li(*sc, cb.eye, d, rng, cfg->max_depth, cfg->rr_min_depth, pc);
+            V3 L = Li(*sc, cb.eye, d, rng, cfg->max_depth, cfg->rr_min_depth, pc, estimator_of(cfg));
             acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
         }
         for (int c = 0; c < 3; ++c) out[pix * 3 + c] = acc[c] / (double)spp;
@@ -1835,7 +1847,8 @@ void kzo_li(void* h, const kz_ray* rays, uint64_t n, const kz_render_config* cfg
         rng.seed(cfg->seed, i);
         PathCounters pc;
         const kz_ray& r = rays[i];
-        V3 L = Li(*sc, V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz), rng, cfg->max_depth, cfg->rr_min_depth, pc);
+        V3 L = Li(*sc, V3(r.ox, r.oy, r.oz), V3(r.dx, r.dy, r.dz), rng, cfg->max_depth, cfg->rr_min_depth, pc,
+                  estimator_of(cfg));
         out[3 * i] = L.x; out[3 * i + 1] = L.y; out[3 * i + 2] = L.z;
         nb += pc.bounces;
         ns += pc.shadow;

@@ -156,12 +156,13 @@ def make_camera(eye, lookat, up, fov, flip=False):
     return c
 
 
-def make_config(spp, max_depth, seed=0, rr_min_depth=3):
+def make_config(spp, max_depth, seed=0, rr_min_depth=3, flags=0):
     c = RenderConfig()
     c.spp = spp
     c.max_depth = max_depth
     c.seed = seed
     c.rr_min_depth = rr_min_depth
+    c.flags = flags
     return c
 
 
@@ -207,8 +208,8 @@ class Scene:
             lib().kzo_scene_free(self.h)
             self.h = None
 
-    def render(self, camera, W, H, spp, max_depth, seed=0, rr_min_depth=3, nthreads=0, rows=None):
-        cfg = make_config(spp, max_depth, seed, rr_min_depth)
+    def render(self, camera, W, H, spp, max_depth, seed=0, rr_min_depth=3, nthreads=0, rows=None, flags=0):
+        cfg = make_config(spp, max_depth, seed, rr_min_depth, flags)
         out = np.zeros((H, W, 3), np.float64)
         stats = np.zeros(2, np.uint64)
         r0, r1 = rows if rows is not None else (0, H)

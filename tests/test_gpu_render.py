@@ -227,6 +227,24 @@ def test_shading_normals_render(gpu, oracle_mod):
     assert rel_mse(img, img_flat) > 1e-4
 
 
+@pytest.mark.parametrize("flags", [0, 4, 8], ids=["mis", "nee_only", "bsdf_only"])
+def test_estimators_match_restatement(gpu, oracle_mod, flags):
+    """PathIntegrator (MIS), PathEmsIntegrator (NEE only) and
+    PathMatsIntegrator (BSDF sampling only) on the mixed-material box."""
+    d = scenes.box_scene(40, 40, spp=8, max_depth=6)
+    d.materials[3] = api.material([api.dielectric(1.5, 1.0)])
+    d.point_lights = [((0.3, 0.8, 0.4), (0.2, 0.2, 0.2))]
+    s = d.build()
+    img = api.Renderer(spp=8, max_depth=6, seed=12, flags=flags).render(s, d.camera, 40, 40)
+    ref, _ = oracle_mod.Scene.from_desc(d).render(oracle_camera(oracle_mod, d.camera), 40, 40, 8, 6, seed=12,
+                                                  flags=flags)
+    assert np.isfinite(img).all() and ref.mean() > 1e-3
+    assert rel_mse(img, ref) <= REL_MSE_TOL
+    if flags == 0:
+        with pytest.raises(Exception):
+            api.Renderer(spp=1, max_depth=2, flags=12).render(s, d.camera, 8, 8)
+
+
 def test_terrain_scene_small(gpu, oracle_mod):
     d = scenes.terrain_scene(width=64, height=36, spp=2, max_depth=8, cells=64, n_spheres=16)
     s = d.build()

@@ -7,6 +7,7 @@ import os
 import numpy as np
 import pytest
 
+from kazen_proto_gb300 import _native as N
 from kazen_proto_gb300 import api, scenes
 
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
@@ -180,3 +181,18 @@ def test_oracle_renders_box_scene(oracle_mod):
     assert st["path_bounces"] >= 32 * 32 * 4
     # the light is visible from the camera: some pixel carries its radiance
     assert img.max() > 3.0
+
+
+def test_estimators_agree(oracle_mod):
+    """NEE only, BSDF sampling only and their MIS combination estimate the
+    same image (PathEmsIntegrator, PathMatsIntegrator, PathIntegrator)."""
+    d = scenes.box_scene(16, 16, spp=256, max_depth=5)
+    sc = oracle_mod.Scene.from_desc(d)
+    c = d.camera
+    cam = oracle_mod.make_camera(c.eye, c.lookat, c.up, c.fov)
+    imgs = [sc.render(cam, 16, 16, 256, 5, seed=3, flags=f)[0] for f in (0, N.KZ_RENDER_FLAG_NEE_ONLY,
+                                                                         N.KZ_RENDER_FLAG_BSDF_ONLY)]
+    means = [float(i.mean()) for i in imgs]
+    assert abs(means[1] - means[0]) < 0.03 * means[0] and abs(means[2] - means[0]) < 0.05 * means[0], means
+    # different estimators of the same integral: not the same samples
+    assert not np.allclose(imgs[0], imgs[1])

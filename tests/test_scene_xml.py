@@ -133,6 +133,13 @@ def test_loader_errors(tmp_path):
                      '<WhittedIntegrator/>'))
     assert L.desc.meshes[0][3] is False and len(L.warnings) == 1
     assert L.desc.point_lights == [((0.0, 4.0, 0.0), (1.0, 2.0, 3.0))]
+    assert L.render_flags == 0  # Whitted renders with the path integrator (the warning)
+    L = X.load(scene(cam + group + '<Objects><Mesh filename="string t.obj" shader_name="m"/></Objects>'
+                     '<PathEmsIntegrator/>'))
+    assert L.render_flags == N.KZ_RENDER_FLAG_NEE_ONLY and not L.warnings
+    L = X.load(scene(cam + group + '<Objects><Mesh filename="string t.obj" shader_name="m"/></Objects>'
+                     '<PathMatsIntegrator/>'))
+    assert L.render_flags == N.KZ_RENDER_FLAG_BSDF_ONLY and not L.warnings
 
 
 CHECKER_OSL = """shader checkerboard (
