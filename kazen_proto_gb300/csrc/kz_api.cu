@@ -339,8 +339,9 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
     }
     const bool timing = (cfg->flags & KZ_RENDER_FLAG_TIMING) != 0;
     const bool count = (cfg->flags & KZ_RENDER_FLAG_COUNT) != 0;
-    // one batch covers the life of one wave of paths
-    const uint32_t batch = std::max<uint32_t>(4, cfg->max_depth + 1);
+    // one batch covers the life of two waves of paths: the host waits for the
+    // device once per batch, and fewer waits leave fewer idle gaps
+    const uint32_t batch = 2 * std::max<uint32_t>(4, cfg->max_depth + 1);
     std::vector<cudaEvent_t> ev;
     if (timing) {
         ev.assign(5 * (size_t)batch, nullptr);
