@@ -15,9 +15,12 @@ emissive.osl and the scene shaders):
 * statements: declarations, `=` `+=` `-=` `*=` `/=`, `if` / `else`,
   blocks, `return`;
 * expressions: float and color arithmetic, comparisons, `&&` `||` `!`,
-  `?:`, casts, color()/vector()/normal()/point(), luminance (Rec. 709
-  weights, OSL's default colour space), clamp, mix, min, max, pow, sqrt,
-  abs, exp, log, floor, ceil, fmod;
+  `?:`, casts, component access (c[i], v.x, c.r), color()/vector()/
+  normal()/point(), luminance (Rec. 709 weights, OSL's default colour
+  space), clamp, mix, min, max, pow, sqrt, inversesqrt, abs, exp, exp2, log,
+  log2, log10, floor, ceil, round, trunc, sign, fmod, mod, step,
+  smoothstep, linearstep, the trigonometric functions, radians, degrees,
+  hypot, dot, cross, length, distance, normalize;
 * closures: sums of closures times colours or floats, mix() of closures.
 
 The global N is the shading normal, (0, 1, 0) in the local frame the lobes
@@ -37,6 +40,7 @@ from . import _native as N
 from . import api
 
 _TYPES = {"float", "int", "color", "vector", "normal", "point", "string", "closure", "matrix", "void"}
+_COMPONENTS = {"x": 0, "y": 1, "z": 2, "r": 0, "g": 1, "b": 2}
 _VEC_TYPES = {"color", "vector", "normal", "point"}
 _TOKEN = re.compile(r"""
     (?P<ws>\s+|//[^\n]*|/\*.*?\*/)
@@ -258,6 +262,23 @@ FUNCS = {
     "pow": _elementwise(np.power), "sqrt": _elementwise(np.sqrt), "abs": _elementwise(np.abs),
     "fabs": _elementwise(np.abs), "exp": _elementwise(np.exp), "log": _elementwise(np.log),
     "floor": _elementwise(np.floor), "ceil": _elementwise(np.ceil), "fmod": _elementwise(np.fmod),
+    "mod": _elementwise(lambda a, b: a - b * np.floor(a / b)),
+    "sin": _elementwise(np.sin), "cos": _elementwise(np.cos), "tan": _elementwise(np.tan),
+    "asin": _elementwise(np.arcsin), "acos": _elementwise(np.arccos), "atan": _elementwise(np.arctan),
+    "atan2": _elementwise(np.arctan2), "radians": _elementwise(np.radians), "degrees": _elementwise(np.degrees),
+    "exp2": _elementwise(np.exp2), "log2": _elementwise(np.log2), "log10": _elementwise(np.log10),
+    "sign": _elementwise(np.sign), "round": _elementwise(np.round), "trunc": _elementwise(np.trunc),
+    "hypot": _elementwise(np.hypot), "inversesqrt": _elementwise(lambda x: 1.0 / np.sqrt(x)),
+    "step": _elementwise(lambda edge, x: (x >= edge).astype(np.float64)),
+    "smoothstep": _elementwise(lambda e0, e1, x: np.where(
+        x <= e0, 0.0, np.where(x >= e1, 1.0, ((x - e0) / np.where(e1 > e0, e1 - e0, 1.0)) ** 2
+                               * (3.0 - 2.0 * (x - e0) / np.where(e1 > e0, e1 - e0, 1.0))))),
+    "linearstep": _elementwise(lambda e0, e1, x: np.clip((x - e0) / np.where(e1 > e0, e1 - e0, 1.0), 0.0, 1.0)),
+    "dot": _elementwise(lambda a, b: np.dot(a, b)),
+    "cross": _elementwise(np.cross),
+    "length": _elementwise(np.linalg.norm),
+    "distance": _elementwise(lambda a, b: np.linalg.norm(a - b)),
+    "normalize": _elementwise(lambda a: a / np.linalg.norm(a) if np.linalg.norm(a) > 0 else a),
 }
 CLOSURES = {
     "diffuse", "phong", "oren_nayar", "ward", "reflection", "refraction", "transparent", "translucent",
@@ -432,13 +453,27 @@ class Parser:
                 while not self.accept(")"):
                     args.append(self.expr())
                     self.accept(",")
-                return ("call", val, args)
-            return ("var", val)
+                return self.postfix(("call", val, args))
+            return self.postfix(("var", val))
         if val == "(":
             e = self.expr()
             self.expect(")")
-            return e
+            return self.postfix(e)
         raise ValueError(f"OSL: unexpected token {val!r}")
+
+    def postfix(self, e):
+        """Component access: c[i], or v.x / v.y / v.z (p.r / p.g / p.b)."""
+        while True:
+            if self.peek()[1] == "[" and self.peek()[0] == "op":
+                self.next()
+                i = self.expr()
+                self.expect("]")
+                e = ("index", e, i)
+            elif self.peek()[1] == "." and self.peek(1)[0] == "id" and self.peek(1)[1] in _COMPONENTS:
+                self.next()
+                e = ("index", e, ("num", float(_COMPONENTS[self.next()[1]])))
+            else:
+                return e
 
 
 # ---------------------------------------------------------------- evaluation
@@ -550,6 +585,11 @@ class Evaluator:
         if kind == "cast":
             v = self.eval(e[2])
             return v if isinstance(v, Normal) else convert(e[1], v)
+        if kind == "index":
+            v, i = self.eval(e[1]), self.eval(e[2])
+            if not isinstance(v, np.ndarray) or not _is_num(i) or isinstance(i, np.ndarray) or not 0 <= int(i) < 3:
+                raise ValueError("OSL: component access needs a triple and an index 0-2")
+            return float(v[int(i)])
         if kind == "&&":
             return float(truth(self.eval(e[1])) and truth(self.eval(e[2])))
         if kind == "||":

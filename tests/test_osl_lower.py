@@ -154,3 +154,22 @@ def test_reference_library_coverage(golden):
     for k, v in golden.items():
         if not v["lowered"]:
             assert v["error"].startswith("ValueError"), (k, v["error"])
+
+
+def test_builtins_and_component_access():
+    src = """surface s ( color base = color(0.2, 0.4, 0.8), float angle = 60 )
+    {
+        float k = smoothstep(0, 1, 0.5) + step(0.5, 0.7) * cos(radians(angle));
+        vector v = normalize(vector(3, 0, 4));
+        float w = base[2] * v.z + base.r + length(vector(0, 3, 4)) / 5 + mod(-1, 3) * 0.1;
+        color c = color(base.b, base.g, base.r);
+        Ci = k * w * c * diffuse(N) + dot(v, vector(0, 0, 1)) * 0.1 * kp_mirror();
+    }"""
+    r = L.lower(src)
+    k = 0.5 + 1.0 * 0.5
+    w = 0.8 * 0.8 + 0.2 + 1.0 + 2.0 * 0.1
+    (d_id, d_w), (m_id, m_w) = ids_weights(r)
+    assert d_id == N.KZ_CLOSURE_DIFFUSE and np.allclose(d_w, k * w * np.array([0.8, 0.4, 0.2]))
+    assert m_id == N.KZ_CLOSURE_KP_MIRROR and np.allclose(m_w, 0.08)
+    with pytest.raises(ValueError):
+        L.lower("surface b ( float f = 1 ) { Ci = f[0] * diffuse(N); }")  # indexing a float
