@@ -148,9 +148,8 @@ def test_reference_disney_shader(golden):
 
 def test_reference_library_coverage(golden):
     lowered = sorted(k.rsplit("/", 1)[1] for k, v in golden.items() if v["lowered"])
-    assert lowered == ["disney_brdf.osl", "emissive.osl", "lambert.osl", "principle.osl", "ward.osl"]
-    # the rest need what the GPU path does not have: bump mapping, the
-    # environment lookup, BSSRDFs
+    assert lowered == ["disney_brdf.osl", "emissive.osl", "env.osl", "lambert.osl", "principle.osl", "ward.osl"]
+    # the rest need what the GPU path does not have: bump mapping, BSSRDFs
     for k, v in golden.items():
         if not v["lowered"]:
             assert v["error"].startswith("ValueError"), (k, v["error"])
