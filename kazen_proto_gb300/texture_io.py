@@ -225,23 +225,29 @@ def read_png(path: str) -> np.ndarray:
         line = np.frombuffer(raw, np.uint8, stride, y * (stride + 1) + 1).astype(np.int32)
         if f == 0:
             cur = line
-        elif f == 2:
+        elif f == 1:  # Sub: a running sum per byte of the pixel
+            cur = (np.cumsum(line.reshape(-1, bpp), axis=0) & 0xFF).reshape(-1)
+        elif f == 2:  # Up
             cur = (line + prev) & 0xFF
-        else:
-            cur = np.zeros(stride, np.int32)
-            for i in range(stride):
-                a = cur[i - bpp] if i >= bpp else 0
-                c = prev[i - bpp] if i >= bpp else 0
-                if f == 1:
-                    p = a
-                elif f == 3:
-                    p = (a + prev[i]) >> 1
-                elif f == 4:
-                    pa, pb, pc = abs(prev[i] - c), abs(a - c), abs(a + prev[i] - 2 * c)
-                    p = a if pa <= pb and pa <= pc else (prev[i] if pb <= pc else c)
+        elif f in (3, 4):  # Average, Paeth: sequential along the row, a pixel at a time
+            ln = line.reshape(-1, bpp)
+            up = prev.reshape(-1, bpp)
+            cur2 = np.zeros_like(ln)
+            a = np.zeros(bpp, np.int32)
+            c = np.zeros(bpp, np.int32)
+            for x in range(ln.shape[0]):
+                b = up[x]
+                if f == 3:
+                    p = (a + b) >> 1
                 else:
-                    raise ValueError(f"{path}: PNG filter {f}")
-                cur[i] = (line[i] + p) & 0xFF
+                    pa, pb, pc = np.abs(b - c), np.abs(a - c), np.abs(a + b - 2 * c)
+                    p = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+                a = (ln[x] + p) & 0xFF
+                cur2[x] = a
+                c = b
+            cur = cur2.reshape(-1)
+        else:
+            raise ValueError(f"{path}: PNG filter {f}")
         out[y] = cur
         prev = cur
     a = out.view(">u2").astype(np.uint16) if depth == 16 else out
