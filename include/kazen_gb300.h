@@ -201,7 +201,7 @@ typedef struct kz_render_stats {
     uint64_t iterations;     /* wavefront iterations                           */
     uint64_t paths;          /* camera paths started                           */
     uint64_t kernel_launches;/* kernels launched by the call                   */
-    /* KZ_RENDER_FLAG_COUNT: fetches of 64-byte nodes / 48-byte triangles */
+    /* KZ_RENDER_FLAG_COUNT: fetches of 80-byte nodes / 48-byte triangles */
     uint64_t closest_node_fetches, closest_tri_fetches;
     uint64_t shadow_node_fetches, shadow_tri_fetches;
     /* KZ_RENDER_FLAG_TIMING: summed device time per stage, milliseconds */
