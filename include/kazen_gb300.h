@@ -176,7 +176,9 @@ typedef struct kz_render_config {
     uint64_t seed;           /* PCG32 seed; stream = pixel * spp + sample      */
     uint32_t wavefront_size; /* paths in flight; 0 = KZ_RENDER_DEFAULT_WAVEFRONT */
     uint32_t rr_min_depth;   /* first vertex index that plays roulette (ref: 3) */
-    uint32_t block_size;     /* threads per block of the stage kernels; 0 = 256 */
+    uint32_t block_size;     /* threads per block of the stage kernels: 0 (= 256)
+                              * or a multiple of 32 up to 256 (the kernels are
+                              * compiled for at most 256 threads per block) */
     uint32_t flags;          /* KZ_RENDER_FLAG_* bits, 0 = none                */
 } kz_render_config;
 
@@ -457,13 +459,20 @@ kz_status kz_scene_release_scratch(kz_scene* scene);
  *     flight; a larger value fails with KZ_ERR_INVALID_ARG. n itself may be
  *     up to 2^32-1: paths stream through the fixed wavefront.
  *   - The first call on a device looks up the array's device address (once
- *     per device, with that device current); make that first call before any
- *     stream capture.
+ *     per device and context, with that device current); make that first
+ *     call before any stream capture. After a cudaDeviceReset the next call
+ *     looks the address up again (the scene must be rebuilt first, as for
+ *     every other entry point).
  *   - All calls share the one array and its previous contents (the counters
  *     are cleared on every call): calls that overlap on the GPU — from two
  *     threads, or on two scenes' streams — race and corrupt each other.
  *   - KZ_RENDER_FLAG_TIMING is ignored (stage times stay 0); the call
- *     returns after the work has finished on the scene stream. */
+ *     returns after the work has finished on the scene stream.
+ *   - The host waits for the stream after every wavefront iteration (it
+ *     reads the queue counts to size the next launches), where kz_li_batch
+ *     lets the device drive the loop and waits once per 2 x (max_depth + 1)
+ *     iterations: for the same rays this call is slower, more so for small
+ *     batches whose iterations are short. */
 #define KZ_LI_NOALLOC_MAX_WAVEFRONT 16384u
 kz_status kz_li_batch_noalloc(kz_scene* scene, const kz_ray* rays, uint64_t n,
                               const kz_render_config* cfg, float* out_rgb,

@@ -322,7 +322,6 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
     uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
     const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(want, total), 1u << 30));
     const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
-    if (block % 32 != 0 || block > 1024) return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
     kz::PathSoA A, B;
     KZ_TRY(alloc_paths(s->pa, cap, A));
     KZ_TRY(alloc_paths(s->pb, cap, B));
@@ -1091,6 +1090,10 @@ static kz_status check_cfg(const kz_render_config* cfg) {
     if (cfg->max_depth == 0 || cfg->max_depth > 255) return fail(KZ_ERR_INVALID_ARG, "max_depth must be in [1, 255]");
     if ((cfg->flags & KZ_RENDER_FLAG_NEE_ONLY) && (cfg->flags & KZ_RENDER_FLAG_BSDF_ONLY))
         return fail(KZ_ERR_INVALID_ARG, "KZ_RENDER_FLAG_NEE_ONLY and KZ_RENDER_FLAG_BSDF_ONLY exclude each other");
+    // the stage kernels are compiled with __launch_bounds__(256): a larger
+    // block would pass here and then fail at every launch
+    if (cfg->block_size % 32 != 0 || cfg->block_size > 256)
+        return fail(KZ_ERR_INVALID_ARG, "block_size must be 0 or a multiple of 32 that is <= 256");
     return KZ_OK;
 }
 
@@ -1099,8 +1102,8 @@ kz_status kz_li_batch(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_rend
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_cfg(cfg));  // before the scene check: needs no device
     KZ_TRY(check_scene(s));
-    KZ_TRY(check_cfg(cfg));
     if (n == 0) return KZ_OK;
     if (n > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "at most 2^32-1 rays per call");
     if (!rays || !out_rgb) return fail(KZ_ERR_INVALID_ARG, "rays and out_rgb are required");
@@ -1130,8 +1133,8 @@ kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_cfg(cfg));  // before the scene check: needs no device
     KZ_TRY(check_scene(s));
-    KZ_TRY(check_cfg(cfg));
     if (!camera || !fd) return fail(KZ_ERR_INVALID_ARG, "camera and film are required");
     if (!out_rgb) return fail(KZ_ERR_INVALID_ARG, "out_rgb is required");
     if (fd->width == 0 || fd->height == 0) return fail(KZ_ERR_INVALID_ARG, "film size must be > 0");
@@ -1383,8 +1386,8 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     if (!s || !g) return fail(KZ_ERR_INVALID_ARG, "scene and guide are required");
     std::lock_guard<std::mutex> lk(s->mu);
     std::lock_guard<std::mutex> lk2(g->mu);
+    KZ_TRY(check_cfg(cfg));  // before the scene check: needs no device
     KZ_TRY(check_scene(s));
-    KZ_TRY(check_cfg(cfg));
     if (cfg->max_depth > 16) return fail(KZ_ERR_INVALID_ARG, "guided rendering supports max_depth <= 16");
     if (cfg->flags & (KZ_RENDER_FLAG_NEE_ONLY | KZ_RENDER_FLAG_BSDF_ONLY))
         return fail(KZ_ERR_INVALID_ARG, "guided rendering combines the guide with the MIS estimator only");
@@ -1422,7 +1425,6 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
     const uint64_t want = cfg->wavefront_size ? cfg->wavefront_size : KZ_RENDER_DEFAULT_WAVEFRONT;
     const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, per_pass));
     const uint32_t block = cfg->block_size ? cfg->block_size : 256u;
-    if (block % 32 != 0 || block > 1024) return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
     const uint64_t n_recs = per_pass * cfg->max_depth;
     KZ_TRY(g->recs.ensure(n_recs * sizeof(kz::VRec)));
     KZ_TRY(g->nee.ensure(n_recs * sizeof(kz::NRec)));
@@ -1842,24 +1844,61 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+struct NoAllocSlot {
+    void* addr = nullptr;
+    unsigned long long ctx_id = 0;  // cuCtxGetId of the context the address belongs to
+};
+NoAllocSlot g_noalloc[kNoAllocMaxDevices];
+
+// Unique id of the calling thread's current context (cuCtxGetId), through the
+// runtime's driver entry-point lookup so the library does not link libcuda.
+// A context that is destroyed and created again (cudaDeviceReset) gets a new
+// id, and the module holding the array is loaded again at a new address.
+kz_status current_context_id(unsigned long long* id) {
+    typedef int (*GetCurrentFn)(void**);
+    typedef int (*GetIdFn)(void*, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        cudaError_t ea = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
+        cudaError_t eb = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+        if (ea != cudaSuccess || eb != cudaSuccess || qa != cudaDriverEntryPointSuccess ||
+            qb != cudaDriverEntryPointSuccess || !a || !b)
+            return fail(KZ_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId are unavailable");
+        get_current = reinterpret_cast<GetCurrentFn>(a);
+        get_id = reinterpret_cast<GetIdFn>(b);
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return fail(KZ_ERR_CUDA, "no current CUDA context");
+    if (get_id(ctx, id) != 0) return fail(KZ_ERR_CUDA, "cuCtxGetId failed");
+    return KZ_OK;
+}
 
 // Device address of g_noalloc_scratch on `device` (which must be current):
-// looked up on the first call per device and cached. In host code the symbol
-// is only a host-side stand-in, never a device address.
+// looked up on the first call per device, and again whenever the device's
+// context has changed since (after a cudaDeviceReset the array lives at a new
+// address). In host code the symbol is only a host-side stand-in, never a
+// device address.
 kz_status noalloc_scratch(int device, unsigned char** out) {
     if (device < 0 || device >= kNoAllocMaxDevices)
         return fail(KZ_ERR_INVALID_ARG, "device %d is beyond the %d devices the scratch table covers", device,
                     kNoAllocMaxDevices);
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[device]) {
+    unsigned long long ctx_id = 0;
+    KZ_TRY(current_context_id(&ctx_id));
+    NoAllocSlot& slot = g_noalloc[device];
+    if (!slot.addr || slot.ctx_id != ctx_id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return fail(KZ_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-        g_noalloc_addr[device] = p;
+        slot.addr = p;
+        slot.ctx_id = ctx_id;
     }
-    *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+    *out = static_cast<unsigned char*>(slot.addr);
     return KZ_OK;
 }
 
@@ -1879,13 +1918,11 @@ extern "C" kz_status kz_li_batch_noalloc(kz_scene* s, const kz_ray* rays, uint64
                                          float* out_rgb, kz_render_stats* out_stats) {
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
+    KZ_TRY(check_cfg(cfg));  // before the scene check: needs no device
     KZ_TRY(check_scene(s));
-    KZ_TRY(check_cfg(cfg));
     if (cfg->wavefront_size > KZ_LI_NOALLOC_MAX_WAVEFRONT)
         return fail(KZ_ERR_INVALID_ARG, "wavefront_size %u exceeds the no-allocation maximum of %u paths",
                     cfg->wavefront_size, KZ_LI_NOALLOC_MAX_WAVEFRONT);
-    if (cfg->block_size && (cfg->block_size % 32 != 0 || cfg->block_size > 1024))
-        return fail(KZ_ERR_INVALID_ARG, "block_size must be a multiple of 32, <= 1024");
     if (n > 0xffffffffull) return fail(KZ_ERR_INVALID_ARG, "at most 2^32-1 rays per call");
     if (out_stats) *out_stats = kz_render_stats{};
     if (n == 0) return KZ_OK;

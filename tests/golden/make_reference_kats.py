@@ -18,6 +18,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+def reference_root():
+    """The kazen_proto checkout to read: the first command-line argument, else
+    the KAZEN_PROTO_ROOT environment variable."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KAZEN_PROTO_ROOT")
+    if not root:
+        sys.exit("usage: %s <kazen_proto checkout>  (or set KAZEN_PROTO_ROOT)" % os.path.basename(sys.argv[0]))
+    return root
+
+
 def main(ref):
     mf = os.path.join(ref, "tests/render_tests/microfacet_tests.cpp")
     em = os.path.join(ref, "tests/libusage_tests/embree_tests.cpp")
@@ -67,4 +76,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -5,7 +5,7 @@ tests/golden/reference_scenes_summary.json. It reads the scenes where the
 reference checkout lies; nothing else reads them.
 
 Run: python tests/golden/make_reference_scene_summary.py [reference root]
-     (default root: /root/reference)
+     (root: first argument or KAZEN_PROTO_ROOT)
 """
 import glob
 import json
@@ -21,8 +21,17 @@ from kazen_proto_gb300 import scene_xml as X  # noqa: E402
 CLOSURES = {v: k[len("KZ_CLOSURE_"):] for k, v in vars(N).items() if k.startswith("KZ_CLOSURE_")}
 
 
+def reference_root():
+    """The kazen_proto checkout to read: the first command-line argument, else
+    the KAZEN_PROTO_ROOT environment variable."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KAZEN_PROTO_ROOT")
+    if not root:
+        sys.exit("usage: %s <kazen_proto checkout>  (or set KAZEN_PROTO_ROOT)" % os.path.basename(sys.argv[0]))
+    return root
+
+
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root()
     scenes = sorted(glob.glob(os.path.join(root, "resource", "scene", "*", "*.xml")))
     out = {}
     for path in scenes:

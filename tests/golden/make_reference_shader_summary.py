@@ -6,7 +6,7 @@ tests/golden/reference_shaders_lowered.json. It reads the shaders where the
 reference checkout lies; nothing else reads them.
 
 Run: python tests/golden/make_reference_shader_summary.py [reference root]
-     (default root: /root/reference)
+     (root: first argument or KAZEN_PROTO_ROOT)
 """
 import glob
 import json
@@ -19,8 +19,17 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from kazen_proto_gb300 import osl_lower  # noqa: E402
 
 
+def reference_root():
+    """The kazen_proto checkout to read: the first command-line argument, else
+    the KAZEN_PROTO_ROOT environment variable."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("KAZEN_PROTO_ROOT")
+    if not root:
+        sys.exit("usage: %s <kazen_proto checkout>  (or set KAZEN_PROTO_ROOT)" % os.path.basename(sys.argv[0]))
+    return root
+
+
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root()
     out = {}
     for path in sorted(glob.glob(os.path.join(root, "resource", "shader", "src", "*.osl"))):
         rel = os.path.relpath(path, root)

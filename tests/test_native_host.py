@@ -177,3 +177,32 @@ def test_normals_validation_on_host(native_lib):
     with pytest.raises(N.KazenError):
         s.set_mesh_normals(g, np.array([[0, 0, 1], [0, np.inf, 0], [0, 0, 1]], np.float32))
     s.set_mesh_normals(g, np.array([[0, 0, 2], [0, 1, 1], [1, 0, 0]], np.float32))
+
+
+@pytest.mark.parametrize("block_size", [512, 1024, 48])
+def test_block_size_above_the_launch_bounds_is_rejected(native_lib, block_size):
+    # the stage kernels are compiled for at most 256 threads per block; the
+    # render-config check runs before any scene or device work, so an unbuilt
+    # scene handle reaches it on a machine without a GPU
+    s = api.Scene()
+    cfg = api.render_config(spp=1, max_depth=2, block_size=block_size)
+    rays = api.make_rays([[0, 0, 0]], [[0, 0, 1]])
+    out = np.zeros((1, 3), np.float32)
+    st = N.KzRenderStats()
+    cam = N.KzCamera()
+    film = N.KzFilmDesc(4, 4)
+    img = np.zeros((4, 4, 3), np.float32)
+    P = lambda a: a.ctypes.data  # noqa: E731
+    codes = [
+        native_lib.kz_li_batch(s.handle, P(rays), 1, C.byref(cfg), P(out), N.KZ_MEM_HOST, C.byref(st)),
+        native_lib.kz_li_batch_noalloc(s.handle, P(rays), 1, C.byref(cfg), P(out), C.byref(st)),
+        native_lib.kz_render(s.handle, C.byref(cam), C.byref(film), C.byref(cfg), P(img), None, N.KZ_MEM_HOST,
+                             C.byref(st)),
+    ]
+    assert codes == [N.KZ_ERR_INVALID_ARG] * 3
+    assert "block_size" in native_lib.kz_last_error_string().decode()
+    # 256 passes the config check and stops at the scene state instead
+    cfg.block_size = 256
+    assert native_lib.kz_li_batch(s.handle, P(rays), 1, C.byref(cfg), P(out), N.KZ_MEM_HOST,
+                                  C.byref(st)) == N.KZ_ERR_STATE
+    s.close()

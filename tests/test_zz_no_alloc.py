@@ -90,3 +90,46 @@ def test_noalloc_rejects_oversized_wavefront(gpu):
                                                 wavefront_size=N.KZ_LI_NOALLOC_MAX_WAVEFRONT), torch)
     ref, _ = li_batch(s, dr, api.render_config(spp=1, max_depth=5, seed=1), torch)
     assert np.allclose(ok, ref, rtol=RTOL, atol=ATOL)
+
+
+def cone_rays(eye, lookat, n, seed, spread=0.35):
+    """Rays from the camera eye towards jittered points around the look-at point."""
+    rng = np.random.default_rng(seed)
+    eye = np.asarray(eye, np.float32)
+    tgt = np.asarray(lookat, np.float32)[None, :] + rng.uniform(-spread, spread, (n, 3)).astype(np.float32)
+    return api.make_rays(eye, tgt)
+
+
+@pytest.mark.parametrize("case", ["count", "nee_only", "bsdf_only", "block128", "textured_room"])
+def test_noalloc_matches_under_flags_variants_and_block_sizes(gpu, case):
+    torch = pytest.importorskip("torch")
+    import os
+
+    from kazen_proto_gb300 import scene_xml
+    if case == "textured_room":
+        here = os.path.dirname(os.path.abspath(__file__))
+        d = scene_xml.load(os.path.join(here, "golden", "scenes", "textured_room", "scene.xml")).desc
+        rays = cone_rays(d.camera.eye, d.camera.lookat, 30000, 5)
+    else:
+        d = scenes.box_scene(16, 16, spp=1, max_depth=5)
+        rays = camera_rays(d, 30000, 4)
+    s = d.build()
+    dr = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    flags = {"count": N.KZ_RENDER_FLAG_COUNT, "nee_only": N.KZ_RENDER_FLAG_NEE_ONLY,
+             "bsdf_only": N.KZ_RENDER_FLAG_BSDF_ONLY}.get(case, 0)
+    block = 128 if case == "block128" else 0
+    cfg = api.render_config(spp=1, max_depth=5, seed=11, block_size=block, flags=flags)
+    ref, st_ref = li_batch(s, dr, cfg, torch)
+    assert np.isfinite(ref).all() and ref.mean() > 0
+    for _ in range(2):  # two calls in a row on the shared array
+        got, st = li_noalloc(s, dr, cfg, torch)
+        assert np.allclose(got, ref, rtol=RTOL, atol=ATOL), np.abs(got - ref).max()
+        assert st.path_bounces == st_ref.path_bounces and st.shadow_rays == st_ref.shadow_rays
+        if case == "count":
+            # fetch counters accumulate in the static array over the call's
+            # iterations and are cleared at the start of the next call
+            assert st.closest_node_fetches > 0 and st.shadow_node_fetches > 0
+            assert (st.closest_node_fetches, st.closest_tri_fetches, st.shadow_node_fetches,
+                    st.shadow_tri_fetches) == (st_ref.closest_node_fetches, st_ref.closest_tri_fetches,
+                                               st_ref.shadow_node_fetches, st_ref.shadow_tri_fetches)
+    s.close()
