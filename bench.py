@@ -422,11 +422,16 @@ def box_bench(frames=20, W=256, H=256, spp=16, max_depth=5):
 
 
 # ---------------------------------------------------------------- learned guiding, equal time
-def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
-    """Narrow-aperture slit room at R x R: relMSE against a plain FP64
-    reference of ref_spp, plain path tracing for plain_spp vs guided path
-    tracing (network trained online from scratch, inside the same wall-clock
-    budget), plus the equal-spp error of the trained network."""
+def guiding_bench(R=1024, budgets_spp=(1024, 4096), ref_spp=65536, max_depth=10, lr=1e-3, rows=1 << 18):
+    """Learned guiding at its stated size: the narrow-aperture slit room at
+    R x R, depth 10, Adam at lr 1e-3 on 2^18 radiance samples per training
+    step. For each budget, plain path tracing at that spp sets the wall-clock
+    time and guided path tracing (network trained online from scratch, inside
+    the same wall-clock time) renders until the time is up; relMSE of each
+    against a plain FP64 reference of ref_spp, rendered as two independent
+    halves so the reference's own noise is stated (and subtracted in the
+    `_net` ratios). Also the equal-spp error of the network trained in the
+    first budget."""
     from kazen_proto_gb300 import api, scenes
 
     def rel_mse(img, ref, eps=1e-2):
@@ -435,41 +440,69 @@ def guiding_bench(R=256, plain_spp=8192, ref_spp=65536, max_depth=10):
     d = scenes.slit_room_scene(R, R, max_depth=max_depth)
     s = d.build()
     t0 = time.perf_counter()
-    chunk = min(ref_spp, (1 << 31) // (R * R))  # path ids of one render stay below 2^32
-    parts = [api.Renderer(spp=chunk, max_depth=max_depth, seed=99 + k).render(s, d.camera, R, R, fp64=True)[1]
-             for k in range(max(1, ref_spp // chunk))]
-    ref = np.mean(parts, axis=0)
+    chunk = min(ref_spp // 2, (1 << 31) // (R * R))  # path ids of one render stay below 2^32
+    halves = []
+    for h in range(2):
+        parts = [api.Renderer(spp=chunk, max_depth=max_depth, seed=99 + 1000 * h + k).render(
+            s, d.camera, R, R, fp64=True)[1] for k in range(max(1, (ref_spp // 2) // chunk))]
+        halves.append(np.mean(parts, axis=0))
+    ref = 0.5 * (halves[0] + halves[1])
+    ref_noise = float(np.mean(((halves[0] - halves[1]) * 0.5) ** 2 / (ref ** 2 + 1e-2)))
     ref_s = time.perf_counter() - t0
-    r = api.Renderer(spp=plain_spp, max_depth=max_depth, seed=1)
-    r.render(s, d.camera, R, R)  # warm-up
-    t0 = time.perf_counter()
-    img_p = r.render(s, d.camera, R, R)
-    T = time.perf_counter() - t0
-    e_plain = rel_mse(img_p, ref)
     g = api.Guide(seed=3)
     api.render_guided(s, g, d.camera, R, R, spp=4, max_depth=max_depth, seed=2,
                       gcfg=api.guide_config(train=False, spp_per_pass=4))  # warm-up (kernels, buffers)
     g.close()
-    g = api.Guide(seed=3)
-    t0 = time.perf_counter()
-    img_g, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=1 << 20, max_depth=max_depth, seed=7,
-                                          gcfg=api.guide_config(spp_per_pass=16, steps_per_pass=4, learning_rate=1e-2,
-                                                                max_train_steps=256, time_budget_ms=T * 1e3))
-    Tg = time.perf_counter() - t0
-    e_guided = rel_mse(img_g, ref)
-    img_f, _, _, _ = api.render_guided(s, g, d.camera, R, R, spp=plain_spp, max_depth=max_depth, seed=11,
-                                       gcfg=api.guide_config(train=False, spp_per_pass=64))
-    e_frozen = rel_mse(img_f, ref)
+    runs = []
+    frozen = None
+    for bi, spp in enumerate(budgets_spp):
+        r = api.Renderer(spp=spp, max_depth=max_depth, seed=1 + bi)
+        if bi == 0:
+            r.render(s, d.camera, R, R)  # warm-up
+        t0 = time.perf_counter()
+        img_p = r.render(s, d.camera, R, R)
+        T = time.perf_counter() - t0
+        e_plain = rel_mse(img_p, ref)
+        g = api.Guide(seed=3)
+        gc = GUIDE_SETTINGS(lr, rows, T)
+        t0 = time.perf_counter()
+        img_g, _, st, gst = api.render_guided(s, g, d.camera, R, R, spp=1 << 20, max_depth=max_depth, seed=7 + bi,
+                                              gcfg=gc)
+        Tg = time.perf_counter() - t0
+        e_guided = rel_mse(img_g, ref)
+        runs.append({"plain": {"spp": spp, "seconds": round(T, 4), "relmse": e_plain},
+                     "guided": {"seconds": round(Tg, 4), "spp": gst["spp_done"], "train_steps": gst["train_steps"],
+                                "train_ms": round(gst["train_ms"], 1), "train_samples": gst["train_samples"],
+                                "relmse": e_guided},
+                     "relmse_ratio_plain_over_guided": round(e_plain / e_guided, 3),
+                     "relmse_ratio_plain_over_guided_net": round((e_plain - ref_noise) / max(1e-12, e_guided - ref_noise),
+                                                                 3)})
+        if bi == 0:
+            t0 = time.perf_counter()
+            img_f, _, _, _ = api.render_guided(s, g, d.camera, R, R, spp=spp, max_depth=max_depth, seed=11,
+                                               gcfg=api.guide_config(alpha=gc.alpha, train=False, spp_per_pass=64))
+            Tf = time.perf_counter() - t0
+            e_f = rel_mse(img_f, ref)
+            frozen = {"spp": spp, "seconds": round(Tf, 4), "relmse": e_f, "train_steps": gst["train_steps"],
+                      "relmse_ratio_plain_over_guided": round(e_plain / e_f, 3),
+                      "cost_per_sample_vs_plain": round(Tf / T, 3)}
+        g.close()
+    s.close()
     return {"scene": "slit room %dx%d, max depth %d, 24 Lambert quads + 32 GGX spheres, 4x4 exterior light "
                      "(radiance 200) behind a 0.05x0.5 slit" % (R, R, max_depth),
-            "reference": "plain, %d spp, FP64 accumulation (%.1f s)" % (ref_spp, ref_s),
-            "plain": {"spp": plain_spp, "seconds": round(T, 4), "relmse": e_plain},
-            "guided_equal_time": {"seconds": round(Tg, 4), "spp": gst["spp_done"], "train_steps": gst["train_steps"],
-                                  "train_ms": round(gst["train_ms"], 1), "train_samples": gst["train_samples"],
-                                  "relmse": e_guided},
-            "relmse_ratio_plain_over_guided_equal_time": round(e_plain / e_guided, 3),
-            "guided_trained_equal_spp": {"spp": plain_spp, "relmse": e_frozen},
-            "relmse_ratio_plain_over_guided_equal_spp": round(e_plain / e_frozen, 3)}
+            "network": "51 -> 64 -> 64 -> 64 -> 40 (8 vMF lobes), BF16 weights, FP32 accumulation, Adam lr %g, "
+                       "%d radiance samples per training step" % (lr, rows),
+            "reference": "plain, %d spp, FP64 accumulation, two independent halves (%.1f s)" % (ref_spp, ref_s),
+            "reference_noise_relmse": ref_noise,
+            "equal_time": runs, "guided_trained_equal_spp": frozen}
+
+
+def GUIDE_SETTINGS(lr, rows, seconds):
+    """Guided-render settings of the equal-time runs (online training from
+    scratch inside the wall-clock budget)."""
+    from kazen_proto_gb300 import api
+    return api.guide_config(spp_per_pass=16, steps_per_pass=4, learning_rate=lr, max_train_steps=256,
+                            max_train_samples=rows, time_budget_ms=seconds * 1e3)
 
 
 # ---------------------------------------------------------------- batched uneven jobs

@@ -13,7 +13,7 @@ __global__ void k_closure_eval(const kz_lobe* __restrict__ lobes, const float* _
     if (i >= n) return;
     const kz_lobe l = lobes[i];
     const f3 a = ld3(wi + 3 * i), b = ld3(wo + 3 * i);
-    LobeEval e = conv == KZ_CONVENTION_REFERENCE ? lobe_eval_reference(l, a, b) : lobe_eval(l, a, b);
+    LobeEval e = conv == KZ_CONVENTION_REFERENCE ? lobe_eval_reference<true>(l, a, b) : lobe_eval(l, a, b);
     f[3 * i] = e.f.x;
     f[3 * i + 1] = e.f.y;
     f[3 * i + 2] = e.f.z;

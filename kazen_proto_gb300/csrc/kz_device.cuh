@@ -44,6 +44,16 @@ __host__ __device__ __forceinline__ f3 normalize(f3 a) {
     float l = sqrtf(dot(a, a));
     return {a.x / l, a.y / l, a.z / l};
 }
+// base::Vec::normalized() of the reference (src/base/vec.h:784-790): the
+// reciprocal length is taken in double and rounded once to float
+__host__ __device__ __forceinline__ f3 normalize_ref(f3 a) {
+    const float rcp = (float)(1.0 / sqrt((double)dot(a, a)));
+    return {a.x * rcp, a.y * rcp, a.z * rcp};
+}
+template <bool kRefNorm>
+__host__ __device__ __forceinline__ f3 nrm(f3 a) {
+    return kRefNorm ? normalize_ref(a) : normalize(a);
+}
 __host__ __device__ __forceinline__ float sq(float a) { return a * a; }
 __host__ __device__ __forceinline__ bool is_zero(f3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
 __host__ __device__ __forceinline__ float max_comp(f3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
@@ -384,7 +394,11 @@ __device__ __forceinline__ Mdf lobe_mdf(const kz_lobe& l, f3 wi, float& eta) {
 }
 
 // Value and pdf of one lobe exactly as the reference eval functions return
-// them; a configuration the reference rejects gives (0, 0).
+// them; a configuration the reference rejects gives (0, 0). kRefNorm selects
+// the reference's own normalisation of half vectors (a double-precision
+// reciprocal length), used by the reference-convention batch kernel; the
+// shading kernels use the float form.
+template <bool kRefNorm = false>
 __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
     LobeEval r{mk(0.f, 0.f, 0.f), 0.f};
     switch (l.closure_id) {
@@ -400,7 +414,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         Mdf mdf = lobe_mdf(l, wi, eta);
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        f3 m = normalize(wi + wo);
+        f3 m = nrm<kRefNorm>(wi + wo);
         if (dot(wo, m) == 0.f) return r;
         float D = mdf.D(m), G = mdf.G(wo);
         float cmi = dot(m, wi);
@@ -417,7 +431,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         if (eta == 1.f) return r;
         if (ci < 0) eta = 1.f / eta;
         if (ci * co >= 0.f) {
-            f3 m = normalize(wi + wo);
+            f3 m = nrm<kRefNorm>(wi + wo);
             float cmi = dot(wi, m);
             float F = fresnel_refl(eta, cmi);
             r.pdf = cmi == 0.f ? 0.f : (1.f / (4.f * fabsf(cmi))) * mdf.pdf(m);
@@ -425,7 +439,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
             float v = denom == 0.f ? 0.f : F * mdf.D(m) * mdf.G(wo) / denom;
             r.f = mk(v, v, v);
         } else {
-            f3 m = normalize(wi + eta * wo);
+            f3 m = nrm<kRefNorm>(wi + eta * wo);
             if (m.y < 0.f) m = -m;
             float cmi = dot(wi, m);
             float F = fresnel_refl(eta, cmi);
@@ -447,7 +461,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         Mdf mdf = lobe_mdf(l, wi, eta);
         float co = wo.y, ci = wi.y;
         if (ci * co < 0.f) return r;
-        f3 wh = normalize(wi + wo);
+        f3 wh = nrm<kRefNorm>(wi + wo);
         float com = dot(wo, wh);
         if (com == 0.f) return r;
         float D = fminf(4.f, mdf.D(wh));
@@ -465,7 +479,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         Mdf mdf = lobe_mdf(l, wi, eta);
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        f3 m = normalize(wi + wo);
+        f3 m = nrm<kRefNorm>(wi + wo);
         float com = dot(wo, m);
         if (com <= 0.f) return r;
         float w = schlick_weight(com);
@@ -494,7 +508,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         const float ax = l.params[6], ay = l.params[7];
         const float ci = wi.y, co = wo.y;
         if (ci <= 0.f || co <= 0.f) return r;
-        const f3 m = normalize(wi + wo);
+        const f3 m = nrm<kRefNorm>(wi + wo);
         const float sv = sqrtf(fmaxf(0.f, 1.f - ci * ci));
         // stretched_roughness (microfacet.h:60-73) takes sin(theta) of wi here
         const float A = ax == ay ? 1.f / sq(ax) : sq(m.x / (sv * ax)) + sq(m.z / (sv * ay));
@@ -518,7 +532,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         const float alpha = l.params[0], kd = l.params[3];
         const float ci = wi.y, co = wo.y;
         if (ci <= 0.f || co <= 0.f) return r;
-        const f3 wh = normalize(wi + wo);
+        const f3 wh = nrm<kRefNorm>(wi + wo);
         const float D = beckmann_pdf_m(wh, alpha);
         const float F = fresnel_ext_int(dot(wh, wi), l.params[2], l.params[1]);
         const float G = beckmann_g1_walter(wh, wi, alpha) * beckmann_g1_walter(wh, wo, alpha);
@@ -542,14 +556,14 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         if (co <= 0.f || ci <= 0.f) return r;
         r.pdf = co * kInvPi;
         const float FL = pow5(1.f - co), FV = pow5(1.f - ci);
-        const f3 wh = normalize(wi + wo);
+        const f3 wh = nrm<kRefNorm>(wi + wo);
         const float RR = 2.f * l.params[3] * sq(dot(wo, wh));
         const float v = kInvPi * RR * (FL + FV + FL * FV * (RR - 1.f));
         r.f = mk(v, v, v);
         return r;
     }
     case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {  // bsdfs.cpp:614-640 (no hemisphere test)
-        const f3 wh = normalize(wi + wo);
+        const f3 wh = nrm<kRefNorm>(wi + wo);
         const float fss90 = sq(dot(wh, wo)) * l.params[0];
         const float aci = fabsf(wi.y), aco = fabsf(wo.y);
         const float fi = pow5(1.f - aci), fo = pow5(1.f - aco);
@@ -564,7 +578,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
         const float ci = wi.y, co = wo.y;
         if (co <= 0.f || ci <= 0.f) return r;
         r.pdf = co * kInvPi;
-        const f3 wh = normalize(wi + wo);
+        const f3 wh = nrm<kRefNorm>(wi + wo);
         const float cv = dot(wh, wo);
         const float v = cv < 1e-6f ? l.params[3] : l.params[3] * pow5(1.f - cv);
         r.f = mk(v, v, v);
@@ -573,7 +587,7 @@ __device__ inline LobeEval lobe_eval_reference(const kz_lobe& l, f3 wi, f3 wo) {
     case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {  // bsdfs.cpp:736-780: D takes cos, G1 takes tan
         const float ci = wi.y, co = wo.y;
         if (ci <= 0.f || co <= 0.f) return r;
-        const f3 wh = normalize(wi + wo);
+        const f3 wh = nrm<kRefNorm>(wi + wo);
         const float ch = wh.y;
         const float a2 = sq(l.params[3]);
         const float D = (a2 - 1.f) / (kPi * logf(a2) * (1.f + (a2 - 1.f) * ch));

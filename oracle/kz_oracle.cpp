@@ -72,6 +72,16 @@ inline V3 normalize(V3 a) {
     float l = std::sqrt(dot(a, a));
     return {a.x / l, a.y / l, a.z / l};
 }
+// base::Vec::normalized(), src/base/vec.h:784-790: reciprocal length in
+// double, rounded once to float
+inline V3 normalize_ref(V3 a) {
+    const float rcp = (float)(1.0 / std::sqrt((double)dot(a, a)));
+    return {a.x * rcp, a.y * rcp, a.z * rcp};
+}
+template <bool kRefNorm>
+inline V3 nrm(V3 a) {
+    return kRefNorm ? normalize_ref(a) : normalize(a);
+}
 inline float sq(float a) { return a * a; }
 inline bool is_zero(V3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
 inline float max_comp(V3 a) { return std::max(a.x, std::max(a.y, a.z)); }
@@ -736,6 +746,9 @@ Mdf make_mdf(const kz_lobe& l, V3 wi, int& dist, float& eta) {
 // Reference-convention value and pdf of one lobe (eval functions of
 // src/shading/bsdfs.cpp; on a rejected configuration the reference leaves
 // its pdf untouched, here it is 0).
+// kRefNorm: the reference's normalisation of half vectors (reference-convention
+// queries); the path loop uses the float form, as the shading kernels do.
+template <bool kRefNorm = false>
 LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
     LobeEval r{V3(0, 0, 0), 0.f};
     switch (l.closure_id) {
@@ -754,7 +767,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         Mdf mdf = make_mdf(l, wi, dist, eta);
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        V3 m = normalize(wi + wo);
+        V3 m = nrm<kRefNorm>(wi + wo);
         if (dot(wo, m) == 0.f) return r;
         float D = mdf.D(m), G = mdf.G(wo);
         float F = dist == BECKMANN ? fresnel_refl(eta, dot(m, wi)) : fresnel_refl(eta, std::fabs(dot(m, wi)));
@@ -770,7 +783,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         if (eta == 1.f) return r;
         if (ci < 0) eta = 1.f / eta;
         if (ci * co >= 0.f) {
-            V3 m = normalize(wi + wo);
+            V3 m = nrm<kRefNorm>(wi + wo);
             float cmi = dot(wi, m);
             float F = fresnel_refl(eta, cmi);
             // reflection_pdf / eval_reflection, bsdfs.h:541-562
@@ -779,7 +792,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
             float v = denom == 0.f ? 0.f : F * mdf.D(m) * mdf.G(wo) / denom;
             r.f = V3(v, v, v);
         } else {
-            V3 m = normalize(wi + eta * wo);
+            V3 m = nrm<kRefNorm>(wi + eta * wo);
             if (m.y < 0.f) m = -m;
             float cmi = dot(wi, m);
             float F = fresnel_refl(eta, cmi);
@@ -803,7 +816,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         V3 F0(l.params[0], l.params[1], l.params[2]);
         float co = wo.y, ci = wi.y;
         if (ci * co < 0.) return r;
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float com = dot(wo, wh);
         if (com == 0.f) return r;
         float D = std::min(4.f, mdf.D(wh));
@@ -820,7 +833,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         Mdf mdf = make_mdf(l, wi, dist, eta);
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        V3 m = normalize(wi + wo);
+        V3 m = nrm<kRefNorm>(wi + wo);
         float com = dot(wo, m);
         if (com <= 0.f) return r;
         float w = schlick_weight(com);
@@ -851,7 +864,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         float ax = l.params[6], ay = l.params[7];
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        V3 m = normalize(wi + wo);
+        V3 m = nrm<kRefNorm>(wi + wo);
         float sin_v = std::sqrt(std::max(0.f, 1.f - ci * ci));
         float A = stretched_roughness(m, sin_v, ax, ay);
         float tmp = std::exp(-tan2_theta_ref(m) * A) / (4.f * kPi * ax * ay);
@@ -872,7 +885,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         float alpha = l.params[0], int_ior = l.params[1], ext_ior = l.params[2], kd = l.params[3];
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float D = beckmann_pdf_ref(wh, alpha);
         float F = fresnel_utils(dot(wh, wi), ext_ior, int_ior);
         float G = walter_g1_ref(wh, wi, alpha) * walter_g1_ref(wh, wo, alpha);
@@ -896,7 +909,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         if (co <= 0 || ci <= 0) return r;
         r.pdf = std::max(co, 0.f) * kInvPi;
         double FL = std::pow(1. - co, 5.), FV = std::pow(1. - ci, 5.);
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float d = dot(wo, wh);
         float RR = 2.f * l.params[3] * (d * d);
         float v = (float)(kInvPi * RR * (FL + FV + FL * FV * (RR - 1.)));
@@ -904,7 +917,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         return r;
     }
     case KZ_CLOSURE_KP_PRINCIPLE_FAKESS: {  // bsdfs.cpp:614-640
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float ch = dot(wh, wo);
         float fss90 = ch * ch * l.params[0];
         float aco = std::fabs(wo.y), aci = std::fabs(wi.y);
@@ -920,7 +933,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
         float ci = wi.y, co = wo.y;
         if (co <= 0 || ci <= 0) return r;
         r.pdf = std::max(co, 0.f) * kInvPi;
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float cv = dot(wh, wo);
         float v = cv < 1e-6 ? l.params[3] : (float)(l.params[3] * std::pow(1. - cv, 5.));
         r.f = V3(v, v, v);
@@ -929,7 +942,7 @@ LobeEval eval_reference(const kz_lobe& l, V3 wi, V3 wo) {
     case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: {  // bsdfs.cpp:736-780
         float ci = wi.y, co = wo.y;
         if (ci <= 0 || co <= 0) return r;
-        V3 wh = normalize(wi + wo);
+        V3 wh = nrm<kRefNorm>(wi + wo);
         float ch = wh.y;
         float D = gtr1_ref(l.params[3], ch);
         float G = clearcoat_g1_ref(ci) * clearcoat_g1_ref(co);
@@ -1386,6 +1399,119 @@ struct PathCounters {
     uint64_t bounces = 0, shadow = 0;
 };
 
+// ---- the reference's loop as written (compat modes of Li below)
+//
+// Bits of `compat`; 0 is the corrected loop the GPU path computes.
+enum : uint32_t {
+    // next-event estimation of integrator.cpp:465-481: the composite closure's
+    // reference-convention value (Diffuse already includes cos) times
+    // cos(light, shading normal) again, lights below the shading normal
+    // skipped, MIS against the reference-convention composite pdf
+    COMPAT_NEE = 1,
+    // BSDF sampling of integrator.cpp:503-506 with CompositeClosure::sample
+    // (bsdf.cpp:17-55): lobe picked uniformly and divided by its selection
+    // probability, the other lobes' values added undivided, throughput times
+    // that value with no division by the direction pdf; Diffuse samples
+    // uniform theta (sample_hemisphere, sampling.h:25-32), microfacet lobes
+    // MicrofacetInterface::sample_m (microfacet.h:103-213)
+    COMPAT_BSDF = 2,
+    // emission hit of integrator.cpp:444-459: MIS weight from the previous
+    // vertex's BSDF pdf and the light pdf its next-event sample left behind
+    COMPAT_EMISSION = 4,
+    // depth of integrator.cpp:407-420 and :555: max_depth fixed at 8 and
+    // stepped twice per vertex (at most 4 shaded vertices), roulette from the
+    // second vertex on (depth >= 3)
+    COMPAT_DEPTH = 8,
+};
+
+// sample_hemisphere(u), src/core/sampling.h:25-32: theta uniform in [0, pi/2]
+V3 sample_hemisphere_ref(float u0, float u1) {
+    float theta = u0 * (float)M_PI_2;
+    float phi = u1 * (float)M_PI * 2.f;
+    float ct = std::cos(theta), st = std::sin(theta);
+    return normalize_ref(V3(st * std::cos(phi), ct, st * std::sin(phi)));
+}
+
+// GGXDist::sample_slope, src/shading/microfacet.h:103-126
+void ggx_slope_ref(float cos_theta, float s0, float s1, float& sx, float& sy) {
+    float c = cos_theta < 1e-6f ? 1e-6f : cos_theta;
+    float Q = (1 + c) * s0 - c;
+    float num = c * std::sqrt((1 - c) * (1 + c)) - Q * std::sqrt((1 - Q) * (1 + Q));
+    float den = (Q - c) * (Q + c);
+    float eps = 1.f / 4294967296.0f;
+    den = std::fabs(den) < eps ? std::copysign(eps, den) : den;
+    sx = num / den;
+    float Ru = 1 - 2 * s1;
+    float u2 = std::fabs(Ru);
+    float z = (u2 * (u2 * (u2 * 0.27385f - 0.73369f) + 0.46341f)) /
+              (u2 * (u2 * (u2 * 0.093073f + 0.309420f) - 1.0f) + 0.597999f);
+    sy = std::copysign(1.0f, Ru) * z * std::sqrt(1.0f + sx * sx);
+}
+
+// BeckmannDist::sample_slope, src/shading/microfacet.h:128-171, 1/erf where an
+// inverse erf is meant as written; OIIO::fast_exp (:169) taken as exp
+void beckmann_slope_ref(float cos_theta_i, float s0, float s1, float& sx, float& sy) {
+    float ct = cos_theta_i < 1e-6f ? 1e-6f : cos_theta_i;
+    float tan_theta_i = std::sqrt(1 - ct * ct) / ct;
+    float cot_theta_i = 1 / tan_theta_i;
+    float c = std::erf(cot_theta_i);
+    float K = tan_theta_i * 0.564189583547756286948f;
+    float y_approx = s0 * (1.f + c + K * (1 - c * c));
+    float y_exact = s0 * (1.f + c + K * std::exp(-cot_theta_i * cot_theta_i));
+    float b = K > 0 ? (0.5f - std::sqrt(K * (K - y_approx + 1.f) + 0.25f)) / K : y_approx - 1.f;
+    float inv_erf = 1.f / std::erf(b);
+    float value = 1.f + b + K * std::exp(-inv_erf * inv_erf) - y_exact;
+    if (std::fabs(value) > 1e-6f) {
+        b -= value / (1 - inv_erf * tan_theta_i);
+        inv_erf = 1.f / std::erf(b);
+        value = 1.0f + b + K * std::exp(-inv_erf * inv_erf) - y_exact;
+        b -= value / (1 - inv_erf * tan_theta_i);
+        sx = 1.f / std::erf(b);
+    } else {
+        sx = inv_erf;
+    }
+    sy = 1.f / std::erf(2.0f * s1 - 1.0f);
+}
+
+// MicrofacetInterface::sample_m, src/shading/microfacet.h:173-213: the slope
+// is sampled for the unstretched angle and rotated by wi's azimuth
+V3 sample_m_ref(int dist, V3 wi, float ax, float ay, float u0, float u1) {
+    float cos_theta_i = wi.y;
+    float phi = 0.f;
+    if (cos_theta_i < 0.9999f) phi = std::atan2(wi.z, wi.x);
+    float sx, sy;
+    if (dist == BECKMANN) beckmann_slope_ref(cos_theta_i, u0, u1, sx, sy);
+    else ggx_slope_ref(cos_theta_i, u0, u1, sx, sy);
+    const float cp = std::cos(phi), sp = std::sin(phi);
+    const float rx = cp * sx - sp * sy, ry = sp * sx + cp * sy;
+    return normalize_ref(V3(-rx * ax, 1.f, -ry * ay));
+}
+
+// The reference's own sampler for one lobe (the sample functions of
+// bsdfs.cpp): the direction; its value and pdf are the reference-convention
+// eval at that direction, which is what those functions return.
+V3 sample_dir_ref(const kz_lobe& l, V3 wi, float u0, float u1, float u2, bool& ok) {
+    ok = true;
+    switch (l.closure_id) {
+    case KZ_CLOSURE_DIFFUSE:
+        return sample_hemisphere_ref(u0, u1);
+    case KZ_CLOSURE_KP_GLOSS:
+    case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL:
+    case KZ_CLOSURE_CONDUCTOR_GGX: {
+        int dist;
+        float eta;
+        Mdf m = make_mdf(l, wi, dist, eta);
+        V3 h = sample_m_ref(dist, wi, m.ax, m.ay, u0, u1);
+        return reflect_n(wi, h);
+    }
+    default: {  // the restatement's sampler gives the direction of the other lobes
+        LobeSample smp = sample_lobe(l, wi, u0, u1, u2);
+        ok = smp.valid;
+        return smp.wo;
+    }
+    }
+}
+
 // One path of the corrected PathIntegrator::Li (src/core/integrator.cpp:362-561).
 // Random numbers: 9 per shaded vertex, in a fixed order, whatever branches run:
 //   [0] light pick  [1] light triangle  [2,3] point on triangle  [4] roulette
@@ -1394,11 +1520,15 @@ struct PathCounters {
 // (PathEmsIntegrator, integrator.cpp:264-360), 2 BSDF sampling only
 // (PathMatsIntegrator, integrator.cpp:213-262).
 V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_min, PathCounters& pc,
-      int est = 0) {
+      int est = 0, uint32_t compat = 0) {
     V3 L(0, 0, 0), beta(1, 1, 1);
     float prev_pdf = 0.f;
     bool prev_specular = true;
     const uint32_t nl = (uint32_t)sc.lights.size();
+    // compat state: the previous vertex's light pdf (per light, as
+    // GeometryLight::sample leaves it) and BSDF pdf (as bsdf_sample.pdf)
+    float stale_lpdf = 0.f, stale_mpdf = 1.f;
+    if (compat & COMPAT_DEPTH) max_depth = 4;
     for (uint32_t depth = 0; depth < max_depth; ++depth) {
         float t, bu, bv;
         uint32_t prim;
@@ -1445,7 +1575,10 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         V3 wi = -fr.to_local(d);
         // 1. emission on hit (front side of the shading normal, single_emissive_surface)
         V3 Le(mat.Le[0], mat.Le[1], mat.Le[2]);
-        if (!is_zero(Le) && dot(d, Ns) < 0.f) {
+        if (!is_zero(Le) && dot(d, Ns) < 0.f && (compat & COMPAT_EMISSION)) {
+            float w = prev_specular ? 1.f : power_heuristic(stale_mpdf, stale_lpdf);
+            L = L + mul(beta, Le) * w;
+        } else if (!is_zero(Le) && dot(d, Ns) < 0.f) {
             float w = 1.f;
             if (!prev_specular && est != 2) {
                 int li = sc.geom_light[geom];
@@ -1478,7 +1611,47 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         if (wsum > 0.f)
             for (uint32_t i = 0; i < nlobes; ++i) lp[i] /= wsum;
         // 2. next-event estimation (not when sampling the BSDF only)
-        if (est != 2 && nl > 0 && any_smooth && wsum > 0.f) {
+        if ((compat & COMPAT_NEE) && nl > 0) {
+            // integrator.cpp:465-481 with GeometryLight::sample (light.cpp:52-76)
+            uint32_t li = std::min((uint32_t)(u[0] * (float)nl), nl - 1);
+            const OLight& lt = sc.lights[li];
+            if (!lt.point) {
+                uint32_t k = cdf_sample(lt.cdf, u[1]);
+                uint32_t ltri = lt.tris[k];
+                V3 a0 = sc.bvh.v(ltri, 0), a1 = sc.bvh.v(ltri, 1), a2 = sc.bvh.v(ltri, 2);
+                float su0 = std::sqrt(u[2]);
+                float bu0 = 1.f - su0;
+                float bv0 = u[3] * su0;
+                V3 p = a0 * bu0 + a1 * bv0 + a2 * (1.f - bu0 - bv0);
+                V3 nlgt = normalize(cross(a1 - a0, a2 - a0));
+                V3 lv = p - P;
+                float dist2 = dot(lv, lv);
+                float dist = std::sqrt(dist2);
+                V3 ldir = normalize_ref(lv);
+                stale_lpdf = 1.f / lt.area;
+                pc.shadow++;
+                float cos_l = dot(-ldir, nlgt);
+                if (!sc.bvh.any(P, ldir, kRayEps, dist - kRayEps) && cos_l > 0.f) {
+                    stale_lpdf = stale_lpdf * dist2 / cos_l;
+                    V3 Ls = lt.Le * (1.f / stale_lpdf);
+                    float cos_v = dot(ldir, Ns);
+                    if (cos_v > 0.f) {
+                        V3 wo = fr.to_local(ldir);
+                        V3 f(0, 0, 0);
+                        float bpdf = 0.f;
+                        for (uint32_t i = 0; i < nlobes; ++i) {
+                            const kz_lobe& lb = mat.lobes[i];
+                            LobeEval e = eval_reference<true>(lb, wi, wo);
+                            f = f + mul(weight_of(lb, mtex, tint), e.f);
+                            bpdf += lp[i] * e.pdf;
+                        }
+                        float w = power_heuristic(stale_lpdf, bpdf);
+                        if (std::isnan(w)) w = 0.f;
+                        L = L + mul(mul(beta, Ls), f) * (w * cos_v * (float)nl);
+                    }
+                }
+            }
+        } else if (est != 2 && nl > 0 && any_smooth && wsum > 0.f) {
             uint32_t li = std::min((uint32_t)(u[0] * (float)nl), nl - 1);
             const OLight& lt = sc.lights[li];
             V3 p = lt.pos, nlgt(0, 0, 0);
@@ -1524,13 +1697,41 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         }
         if (depth + 1 >= max_depth) break;
         // 3. Russian roulette (integrator.cpp:491-498)
-        if (depth >= rr_min) {
+        if ((compat & COMPAT_DEPTH) ? depth >= 1 : depth >= rr_min) {
             float prob = std::min(max_comp(beta) * 0.9025f, 0.99f);
             if (prob < u[4]) break;
             beta = beta * (1.f / prob);
         }
         // 4. BSDF sampling: lobe by its selection probability, then the
         // one-sample mixture over all non-delta lobes.
+        if (compat & COMPAT_BSDF) {
+            // integrator.cpp:503-506 with CompositeClosure::sample (bsdf.cpp:17-55)
+            if (nlobes == 0) break;
+            uint32_t idx = std::min((uint32_t)(u[5] * 0.9999999f * (float)nlobes), nlobes - 1);
+            const kz_lobe& ls = mat.lobes[idx];
+            bool ok;
+            V3 wo = sample_dir_ref(ls, wi, u[6], u[7], u[8], ok);
+            if (!ok) break;
+            LobeEval e = eval_reference<true>(ls, wi, wo);
+            V3 ret = mul(weight_of(ls, mtex, tint), e.f) * (1.f / lp[idx]);
+            float pdf_acc = e.pdf * lp[idx];
+            for (uint32_t i = 0; i < nlobes; ++i) {
+                if (i == idx) continue;
+                const float before = pdf_acc;  // other_sample copies bsdf_sample first
+                const kz_lobe& lb = mat.lobes[i];
+                LobeEval eo = eval_reference<true>(lb, wi, wo);  // and eval overwrites its pdf
+                ret = ret + mul(weight_of(lb, mtex, tint), eo.f);
+                pdf_acc = eo.pdf + lp[i] * before;
+            }
+            beta = mul(beta, ret);
+            stale_mpdf = pdf_acc;
+            prev_pdf = pdf_acc;
+            prev_specular = lobe_is_delta(ls.closure_id);
+            if (is_zero(beta) || !std::isfinite(beta.x + beta.y + beta.z)) break;
+            o = P;
+            d = normalize_ref(fr.to_world(wo));
+            continue;
+        }
         if (!(wsum > 0.f)) break;
         uint32_t sel = nlobes - 1;
         {
@@ -1566,6 +1767,7 @@ V3 Li(const OScene& sc, V3 o, V3 d, Pcg32& rng, uint32_t max_depth, uint32_t rr_
         beta = mul(beta, weight);
         if (is_zero(beta)) break;
         prev_pdf = pdf_dir;
+        stale_mpdf = pdf_dir;
         prev_specular = smp.delta;
         o = P;
         d = normalize(fr.to_world(smp.wo));
@@ -1636,7 +1838,7 @@ void kzo_closest_brute(const float* tri_verts, uint32_t ntris, const kz_ray* ray
 void kzo_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n, int conv, float* f, float* pdf) {
     for (uint64_t i = 0; i < n; ++i) {
         V3 a(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]), b(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
-        LobeEval e = conv == KZ_CONVENTION_REFERENCE ? eval_reference(lobes[i], a, b) : eval_integrator(lobes[i], a, b);
+        LobeEval e = conv == KZ_CONVENTION_REFERENCE ? eval_reference<true>(lobes[i], a, b) : eval_integrator(lobes[i], a, b);
         f[3 * i] = e.f.x; f[3 * i + 1] = e.f.y; f[3 * i + 2] = e.f.z;
         pdf[i] = e.pdf;
     }
@@ -1790,8 +1992,17 @@ void kzo_scene_set_textures(void* h, const kz_texture* tex, uint32_t n, const fl
 
 // Renders rows [row_begin, row_end) of a W x H frame; out: W*H*3 doubles
 // (spp average, FP64 accumulation); stats[0] = path bounces, stats[1] = shadow rays.
+void kzo_render_compat(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_render_config* cfg,
+                       int nthreads, uint32_t row_begin, uint32_t row_end, uint32_t compat, double* out,
+                       uint64_t* stats);
 void kzo_render(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_render_config* cfg, int nthreads,
                 uint32_t row_begin, uint32_t row_end, double* out, uint64_t* stats) {
+    kzo_render_compat(h, cam, W, H, cfg, nthreads, row_begin, row_end, 0, out, stats);
+}
+// The frame with the path loop in a reference-as-written mode (COMPAT_* bits).
+void kzo_render_compat(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_render_config* cfg,
+                       int nthreads, uint32_t row_begin, uint32_t row_end, uint32_t compat, double* out,
+                       uint64_t* stats) {
     const OScene* sc = static_cast<const OScene*>(h);
     CamBasis cb = cam_basis(*cam, W, H);
     row_end = std::min(row_end, H);
@@ -1808,7 +2019,7 @@ void kzo_render(void* h, const kz_camera* cam, uint32_t W, uint32_t H, const kz_
             rng.seed(cfg->seed, pix * spp + s);
             float jx = rng.nextf(), jy = rng.nextf();
             V3 d = cam_dir(cb, px, py, W, H, jx, jy);
-            V3 L = Li(*sc, cb.eye, d, rng, cfg->max_depth, cfg->rr_min_depth, pc, estimator_of(cfg));
+            V3 L = Li(*sc, cb.eye, d, rng, cfg->max_depth, cfg->rr_min_depth, pc, estimator_of(cfg), compat);
             acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
         }
         for (int c = 0; c < 3; ++c) out[pix * 3 + c] = acc[c] / (double)spp;
@@ -1864,6 +2075,132 @@ void kzo_pcg32_outputs(uint64_t initstate, uint64_t initseq, uint32_t* out, int 
     Pcg32 r;
     r.seed(initstate, initseq);
     for (int i = 0; i < n; ++i) out[i] = r.next();
+}
+
+// ---- the reference's own ray/triangle test (compat intersection mode)
+// moller_trumbore_intersect, src/core/shape.cpp:373-408: single-sided (a
+// determinant below 1e-6 misses, so back faces and grazing hits are culled),
+// hits with t in [0, tmax]; u, v barycentrics of v1, v2.
+bool moller_trumbore_ref(V3 o, V3 d, V3 v0, V3 v1, V3 v2, float tmax, float& t, float& u, float& v) {
+    V3 v1v0 = v1 - v0, v2v0 = v2 - v0;
+    V3 pvec = cross(d, v2v0);
+    float det = dot(v1v0, pvec);
+    if (det < 0.000001) return false;
+    float det_inv = 1.f / det;
+    V3 tvec = o - v0;
+    u = dot(tvec, pvec) * det_inv;
+    if (u < 0.f || u > 1.f) return false;
+    V3 qvec = cross(tvec, v1v0);
+    v = dot(d, qvec) * det_inv;
+    if (v < 0.f || u + v > 1.f) return false;
+    t = dot(v2v0, qvec) * det_inv;
+    if (t < 0 || t > tmax) return false;
+    return true;
+}
+
+// Rays against a triangle list with the reference's test. mode 0: the closest
+// such hit (what a correct traversal over moller_trumbore_intersect gives);
+// mode 1: TriangleMesh::intersect as written (shape.cpp:533-557), the first
+// triangle in index order that the test accepts -- not the closest.
+void kzo_mt_intersect(const float* tri_verts, uint32_t ntris, const kz_ray* rays, uint64_t n, int mode, float* t,
+                      uint32_t* prim, float* u, float* v) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const kz_ray& r = rays[i];
+        V3 o(r.ox, r.oy, r.oz), d(r.dx, r.dy, r.dz);
+        float best = std::numeric_limits<float>::infinity();
+        uint32_t bp = KZ_INVALID_ID;
+        float bu = 0.f, bv = 0.f;
+        for (uint32_t k = 0; k < ntris; ++k) {
+            const float* q = tri_verts + 9 * (size_t)k;
+            float tt, uu, vv;
+            if (!moller_trumbore_ref(o, d, V3(q[0], q[1], q[2]), V3(q[3], q[4], q[5]), V3(q[6], q[7], q[8]),
+                                     mode == 1 ? r.tmax : best, tt, uu, vv))
+                continue;
+            if (mode == 1 || tt < best) {
+                best = tt; bp = k; bu = uu; bv = vv;
+                if (mode == 1) break;
+            }
+        }
+        t[i] = best;
+        prim[i] = bp;
+        u[i] = bu;
+        v[i] = bv;
+    }
+}
+
+// ---- the restatement's scalar building blocks, for the known-answer vectors
+// computed by the reference's own header code (oracle/ref_harness.cpp)
+
+// in: n x 11 (wi, wo, m, ax, ay); out: n x 7 (D(m), lambda(wi), lambda(wo),
+// G1(wi), G1(wo), G(wo), pdf(m)) of MicrofacetInterface (microfacet.h:215-291)
+void kzo_mdf_terms(int dist, const float* in, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* a = in + 11 * i;
+        Mdf m;
+        m.dist = dist;
+        m.wi = V3(a[0], a[1], a[2]);
+        m.ax = a[9];
+        m.ay = a[10];
+        V3 wo(a[3], a[4], a[5]), h(a[6], a[7], a[8]);
+        float* o = out + 7 * i;
+        o[0] = m.D(h);
+        o[1] = m.lambda(m.wi);
+        o[2] = m.lambda(wo);
+        o[3] = m.G1(m.wi);
+        o[4] = m.G1(wo);
+        o[5] = m.G(wo);
+        o[6] = m.pdf(h);
+    }
+}
+
+// in: n x 4 (cos, eta, ext, int); out: n x 4 (fresnel_refl_dielectric(eta, |cos|),
+// fresnel(cos, ext, int), fresnel_schlick(eta, |cos|), schlick_weight(|cos|))
+void kzo_fresnel_terms(const float* in, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* a = in + 4 * i;
+        const float ac = std::fabs(a[0]);
+        float* o = out + 4 * i;
+        o[0] = fresnel_refl(a[1], ac);
+        o[1] = fresnel_utils(a[0], a[2], a[3]);
+        o[2] = fresnel_schlick_eta(a[1], ac);
+        o[3] = schlick_weight(ac);
+    }
+}
+
+// in: n x 7 (wi, n, eta); out: n x 3 refract(wi, n, eta) (utils.h:142-151)
+void kzo_refract(const float* in, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* a = in + 7 * i;
+        V3 t = refract_u(V3(a[0], a[1], a[2]), V3(a[3], a[4], a[5]), a[6]);
+        out[3 * i] = t.x; out[3 * i + 1] = t.y; out[3 * i + 2] = t.z;
+    }
+}
+
+// in: n x 6 (n, v); out: n x 9 (Frame(n).s, .t, to_local(v)) (utils.h:183-210)
+void kzo_frame(const float* in, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* a = in + 6 * i;
+        Frame f(V3(a[0], a[1], a[2]));
+        V3 l = f.to_local(V3(a[3], a[4], a[5]));
+        float* o = out + 9 * i;
+        o[0] = f.s.x; o[1] = f.s.y; o[2] = f.s.z;
+        o[3] = f.t.x; o[4] = f.t.y; o[5] = f.t.z;
+        o[6] = l.x; o[7] = l.y; o[8] = l.z;
+    }
+}
+
+// in: n x 4 (u1, u2, a, b); out: n x 4 (cosine_dir(u2, u1) in the y-up frame,
+// power_heuristic(1, a, 1, b)) -- the cosine warp with the disk mapping of
+// to_uniform_disk / to_cosine_hemisphere (sampling.h:66-108), which returns
+// its cosine in z
+void kzo_warps(const float* in, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* a = in + 4 * i;
+        V3 c = cosine_dir(a[1], a[0]);
+        float* o = out + 4 * i;
+        o[0] = c.x; o[1] = c.y; o[2] = c.z;
+        o[3] = power_heuristic(a[2], a[3]);
+    }
 }
 
 }  // extern "C"

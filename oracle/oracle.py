@@ -56,6 +56,14 @@ def lib():
             "kzo_camera_rays": (None, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P]),
             "kzo_li": (None, [_P, _P, C.c_uint64, C.POINTER(RenderConfig), C.c_int, _P, _P]),
             "kzo_pcg32_outputs": (None, [C.c_uint64, C.c_uint64, _P, C.c_int]),
+            "kzo_mdf_terms": (None, [C.c_int, _P, C.c_uint64, _P]),
+            "kzo_mt_intersect": (None, [_P, C.c_uint32, _P, C.c_uint64, C.c_int, _P, _P, _P, _P]),
+            "kzo_render_compat": (None, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(RenderConfig),
+                                         C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P]),
+            "kzo_fresnel_terms": (None, [_P, C.c_uint64, _P]),
+            "kzo_refract": (None, [_P, C.c_uint64, _P]),
+            "kzo_frame": (None, [_P, C.c_uint64, _P]),
+            "kzo_warps": (None, [_P, C.c_uint64, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(l, name)
@@ -216,6 +224,15 @@ class Scene:
         lib().kzo_render(self.h, C.byref(camera), W, H, C.byref(cfg), nthreads, r0, r1, _p(out), _p(stats))
         return out, {"path_bounces": int(stats[0]), "shadow_rays": int(stats[1])}
 
+    def render_compat(self, camera, W, H, spp, max_depth, compat, seed=0, rr_min_depth=3, nthreads=0):
+        """The frame with the path loop as the reference writes it, per COMPAT_* bit."""
+        cfg = make_config(spp, max_depth, seed, rr_min_depth)
+        out = np.zeros((H, W, 3), np.float64)
+        stats = np.zeros(2, np.uint64)
+        lib().kzo_render_compat(self.h, C.byref(camera), W, H, C.byref(cfg), nthreads, 0, H, compat, _p(out),
+                                _p(stats))
+        return out, {"path_bounces": int(stats[0]), "shadow_rays": int(stats[1])}
+
     def li(self, rays, max_depth, seed=0, rr_min_depth=3, nthreads=0):
         r = np.ascontiguousarray(rays, RAY_DTYPE)
         cfg = make_config(1, max_depth, seed, rr_min_depth)
@@ -225,7 +242,39 @@ class Scene:
         return out, {"path_bounces": int(stats[0]), "shadow_rays": int(stats[1])}
 
 
+# reference-as-written modes of the path loop (kz_oracle.cpp, COMPAT_*)
+COMPAT_NEE, COMPAT_BSDF, COMPAT_EMISSION, COMPAT_DEPTH = 1, 2, 4, 8
+COMPAT_ALL = 15
+
+
+def mt_intersect(tri_verts, rays, first_hit=False):
+    """The reference's single-sided Moller-Trumbore over a triangle list:
+    the closest accepted hit, or (first_hit) the first accepted triangle in
+    index order as TriangleMesh::intersect returns it."""
+    tv = np.ascontiguousarray(tri_verts, np.float32).reshape(-1, 9)
+    r = np.ascontiguousarray(rays, RAY_DTYPE)
+    n = len(r)
+    out = {"t": np.empty(n, np.float32), "prim": np.empty(n, np.uint32), "u": np.empty(n, np.float32),
+           "v": np.empty(n, np.float32)}
+    lib().kzo_mt_intersect(_p(tv), len(tv), _p(r), n, 1 if first_hit else 0, _p(out["t"]), _p(out["prim"]),
+                           _p(out["u"]), _p(out["v"]))
+    return out
+
+
 def camera_rays(camera, W, H, spp, seed):
     rays = np.zeros(W * H * spp, RAY_DTYPE)
     lib().kzo_camera_rays(C.byref(camera), W, H, spp, seed, _p(rays))
     return rays
+
+
+def scalar_terms(name, inp, n_out, dist=None):
+    """The restatement's scalar building blocks over rows of inputs (see
+    kzo_mdf_terms / kzo_fresnel_terms / kzo_refract / kzo_frame / kzo_warps)."""
+    a = np.ascontiguousarray(inp, np.float32)
+    out = np.empty((len(a), n_out), np.float32)
+    f = getattr(lib(), "kzo_" + name)
+    if dist is None:
+        f(_p(a), len(a), _p(out))
+    else:
+        f(dist, _p(a), len(a), _p(out))
+    return out
