@@ -422,7 +422,7 @@ def box_bench(frames=20, W=256, H=256, spp=16, max_depth=5):
 
 
 # ---------------------------------------------------------------- learned guiding, equal time
-def guiding_bench(R=1024, budgets_spp=(1024, 4096), ref_spp=65536, max_depth=10, lr=1e-3, rows=1 << 18):
+def guiding_bench(R=1024, budgets_spp=(1024, 2048), ref_spp=65536, max_depth=10, lr=1e-3, rows=1 << 18):
     """Learned guiding at its stated size: the narrow-aperture slit room at
     R x R, depth 10, Adam at lr 1e-3 on 2^18 radiance samples per training
     step. For each budget, plain path tracing at that spp sets the wall-clock
@@ -534,8 +534,10 @@ def batch_bench(n_jobs=256):
         bounces_single += r.last_stats["path_bounces"]
         errs.append(float(np.abs(img - ref).max() / max(1e-6, float(np.abs(ref).max()))))
         j["scene"].release_scratch()
-    # the megakernel mode at its defaults, for comparison
-    mcfg = api.batch_config(mode=api.BATCH_MEGAKERNEL, use_graph=True)
+    # the megakernel mode at its own best tuned shape, for comparison
+    mega = [t for t in table if t[0].get("mode") == api.BATCH_MEGAKERNEL]
+    best_mega = min(mega, key=lambda t: t[1])[0] if mega else {"mode": api.BATCH_MEGAKERNEL}
+    mcfg = autotune.config_of(best_mega, use_graph=True)
     t0 = time.perf_counter()
     _, mst = api.render_batch(jobs, mcfg)
     wall_m = time.perf_counter() - t0
@@ -545,6 +547,13 @@ def batch_bench(n_jobs=256):
     return {"jobs": n_jobs, "paths": st["paths"], "path_bounces": st["path_bounces"],
             "triangles_total": int(sum(j["desc_args"][0] + 2 for j in jobs)), "scene_build_s": round(build_s, 1),
             "autotuned": best, "autotune_candidates": len(table), "persistent_lanes": st["threads"],
+            "autotune_sample_ms_best_per_mode": {
+                "wavefront": min((ms for c, ms in table if c.get("mode") == api.BATCH_WAVEFRONT), default=None),
+                "megakernel": min((ms for c, ms in table if c.get("mode") == api.BATCH_MEGAKERNEL), default=None)},
+            "autotune_wavefront_by_refill_period": {
+                str(p): min((ms for c, ms in table if c.get("mode") == api.BATCH_WAVEFRONT
+                             and c.get("refill_period") == p), default=None) for p in autotune.WAVE_PERIODS},
+            "megakernel_tuned": best_mega,
             "batched_graph": {"device_ms": round(st["device_ms"], 2), "wall_s": round(wall_b, 3),
                               "mpaths_bounces_per_s": round(mb, 1)},
             "megakernel_graph": {"device_ms": round(mst["device_ms"], 2), "wall_s": round(wall_m, 3),
@@ -665,29 +674,37 @@ def run_ours(args):
     nodes_per_ray = cs["closest_node_fetches"] / max(1, cs["path_bounces"])
     tris_per_ray = cs["closest_tri_fetches"] / max(1, cs["path_bounces"])
 
+    sections = {}
+
+    def timed_section(name, fn):
+        t0 = time.perf_counter()
+        out = fn()
+        sections[name] = round(time.perf_counter() - t0, 1)
+        return out
+
     trav = None
     if rank == 0 and not args.no_traversal and not args.small and not args.profile:
-        trav = traversal_bench(max(3, args.steps), max(3, args.warmup))
+        trav = timed_section("traversal", lambda: traversal_bench(max(3, args.steps), max(3, args.warmup)))
 
     box = None
     if rank == 0 and not args.no_box and not args.small and not args.profile:
-        box = box_bench()
+        box = timed_section("box", box_bench)
 
     guide = None
     if rank == 0 and not args.no_guiding and not args.small and not args.profile:
-        guide = guiding_bench()
+        guide = timed_section("guiding", guiding_bench)
 
     batch = None
     if rank == 0 and not args.no_batch and not args.small and not args.profile:
-        batch = batch_bench()
+        batch = timed_section("batch", batch_bench)
 
     feats = None
     if rank == 0 and not args.no_features and not args.small and not args.profile:
-        feats = features_bench()
+        feats = timed_section("features", features_bench)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
-        cpu = cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0)
+        cpu = timed_section("cpu_baseline", lambda: cpu_baseline(desc, w, budget_s=4.0 if args.small else 15.0))
 
     if rank != 0:
         return
@@ -745,6 +762,7 @@ def run_ours(args):
         "guiding": guide,
         "batch": batch,
         "features": feats,
+        "section_seconds": sections,
     }
     if img is not None:
         line["image_mean"] = float(np.mean(img))

@@ -378,6 +378,13 @@ kz_status kz_guide_create(kz_guide** out_guide, uint64_t seed);
 kz_status kz_guide_destroy(kz_guide* guide);
 kz_status kz_guide_get_params(kz_guide* guide, float* out_params /* KZ_GUIDE_PARAMS, host */);
 kz_status kz_guide_set_params(kz_guide* guide, const float* params /* KZ_GUIDE_PARAMS, host */);
+/* The guide's whole training state, for checkpoint and resume: the FP32
+ * weights, Adam's first and second moments (KZ_GUIDE_PARAMS floats each, in
+ * that order, 3 * KZ_GUIDE_PARAMS in all) and the Adam step count. Training
+ * resumed from a restored state continues as the saved guide would have.
+ * No counterpart in the reference (it has no guiding). */
+kz_status kz_guide_get_state(kz_guide* guide, float* out_state, uint32_t* out_step);
+kz_status kz_guide_set_state(kz_guide* guide, const float* state, uint32_t step);
 /* points: n * 8 floats (p01.xyz, -, n.xyz, -); out_raw: n * 40 network outputs. */
 kz_status kz_guide_forward(kz_guide* guide, const float* points, uint64_t n, float* out_raw, int32_t mem);
 /* samples: n * 12 floats ((p01.xyz, weight), (n.xyz, -), (dir.xyz, -)).
@@ -422,8 +429,9 @@ typedef struct kz_batch_config {
     uint32_t block_size;        /* threads per block (0 = 256 wavefront,
                                    128 megakernel)                           */
     uint32_t ctas_per_sm;       /* megakernel: resident blocks per SM (0 = 2) */
-    uint32_t refill_period;     /* megakernel: vertices between lane refills
-                                   (0 = 1)                                   */
+    uint32_t refill_period;     /* megakernel: vertices between lane refills;
+                                   wavefront: iterations between generations
+                                   of new paths into free slots (0 = 1)      */
     uint32_t use_graph;         /* 1: launch through a captured CUDA graph   */
     uint32_t mode;              /* KZ_BATCH_WAVEFRONT or KZ_BATCH_MEGAKERNEL */
     uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^21)     */

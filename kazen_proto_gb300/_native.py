@@ -11,7 +11,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libkazen_gb300.so")
+# KZ_LIBRARY selects another build of the library (the test builds of
+# kazen_proto_gb300/build.py); the default is the in-tree product build.
+LIB_PATH = os.environ.get("KZ_LIBRARY") or os.path.join(HERE, "_build", "libkazen_gb300.so")
 
 KZ_OK = 0
 KZ_ERR_INVALID_ARG = 1
@@ -195,6 +197,8 @@ SIGNATURES = {
     "kz_guide_destroy": (C.c_int32, [_P]),
     "kz_guide_get_params": (C.c_int32, [_P, _P]),
     "kz_guide_set_params": (C.c_int32, [_P, _P]),
+    "kz_guide_get_state": (C.c_int32, [_P, _P, C.POINTER(C.c_uint32)]),
+    "kz_guide_set_state": (C.c_int32, [_P, _P, C.c_uint32]),
     "kz_guide_forward": (C.c_int32, [_P, _P, C.c_uint64, _P, C.c_int32]),
     "kz_guide_train_step": (C.c_int32, [_P, _P, C.c_uint64, C.c_float, C.c_int32, C.POINTER(C.c_float), _P,
                                         C.c_int32]),

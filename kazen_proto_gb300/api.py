@@ -534,6 +534,18 @@ class Guide:
         assert p.size == N.KZ_GUIDE_PARAMS
         check(lib().kz_guide_set_params(self._h, _ptr(p)))
 
+    def state(self):
+        """(weights, Adam first moments, Adam second moments) and the step count."""
+        st = np.empty(3 * N.KZ_GUIDE_PARAMS, np.float32)
+        step = C.c_uint32()
+        check(lib().kz_guide_get_state(self._h, _ptr(st), C.byref(step)))
+        p = N.KZ_GUIDE_PARAMS
+        return (st[:p], st[p:2 * p], st[2 * p:]), step.value
+
+    def set_state(self, params, m, v, step) -> None:
+        st = np.ascontiguousarray(np.concatenate([params, m, v]), np.float32)
+        check(lib().kz_guide_set_state(self._h, _ptr(st), int(step)))
+
     def forward(self, p01, nrm) -> np.ndarray:
         """Raw network outputs (n, 40) for points in the unit scene box with normals."""
         p01 = np.asarray(p01, np.float32).reshape(-1, 3)

@@ -1,8 +1,9 @@
 """Autotuner of the batch renderer (kz_render_batch).
 
-Sweeps, on a sample of the jobs, the wavefront mode's paths in flight and
-block size, and the megakernel mode's block size, resident blocks per SM and
-lane refill period; keeps the fastest by CUDA-event time and stores it in
+Sweeps, on a sample of the jobs, the wavefront mode's paths in flight, block
+size and refill period (iterations between generations of new paths), and
+the megakernel mode's block size, resident blocks per SM and lane refill
+period; keeps the fastest by CUDA-event time and stores it in
 kazen_proto_gb300/_build/autotune.json for later calls on the same machine.
 """
 from __future__ import annotations
@@ -22,9 +23,12 @@ CTAS_PER_SM = (1, 2, 4)
 PERIODS = (1, 2, 4)
 
 
+WAVE_PERIODS = (1, 2, 3)
+
+
 def candidates():
-    out = [{"mode": api.BATCH_WAVEFRONT, "block_size": b, "wavefront_size": w}
-           for w in WAVEFRONT_SIZES for b in WAVE_BLOCKS]
+    out = [{"mode": api.BATCH_WAVEFRONT, "block_size": b, "wavefront_size": w, "refill_period": p}
+           for w in WAVEFRONT_SIZES for b in WAVE_BLOCKS for p in WAVE_PERIODS]
     out += [{"mode": api.BATCH_MEGAKERNEL, "block_size": b, "ctas_per_sm": c, "refill_period": p}
             for b in BLOCKS for c in CTAS_PER_SM for p in PERIODS]
     return out

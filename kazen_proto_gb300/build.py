@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libkazen_gb300.so")
 
 SOURCES = ["kz_api.cu", "kz_trace.cu", "kz_kernels.cu", "kz_shade_guided.cu", "kz_batch.cu", "kz_megakernel.cu",
-           "kz_closures.cu", "kz_mlp.cu", "kz_bvh.cpp"]
+           "kz_closures.cu", "kz_mlp.cu", "kz_mlp_tc.cu", "kz_bvh.cpp"]
 DEPS = ["kz_device.cuh", "kz_traverse.cuh", "kz_guide.cuh", "kz_stages.cuh", "kz_internal.h", "kz_bvh.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,12 +55,22 @@ def extra_flags() -> list[str]:
     return os.environ.get("KZ_NVCC_FLAGS", "").split()
 
 
-def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+# Test builds: the library compiled with extra defines into its own folder
+# (kazen_proto_gb300/_build_<name>/), loaded by tests in a separate process
+# through KZ_LIBRARY. "stack2": a two-entry traversal stack, which makes the
+# traversal kernels take their stack-overflow path (KZ_ERR_STACK).
+TEST_VARIANTS = {"stack2": ["-DKZ_WIDE_STACK=2", "-DKZ_SMEM_STACK=0"]}
+
+
+def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = False, variant: str | None = None) -> str:
+    out_dir = BUILD if variant is None else os.path.join(HERE, "_build_" + variant)
+    lib_path = LIB if variant is None else os.path.join(out_dir, "libkazen_gb300.so")
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = nvcc_path()
+    flags = extra_flags() if variant is None else TEST_VARIANTS[variant]
     # a change of the extra flags rebuilds everything
-    stamp = os.path.join(BUILD, "flags.txt")
-    flags_now = " ".join(extra_flags())
+    stamp = os.path.join(out_dir, "flags.txt")
+    flags_now = " ".join(flags)
     if not os.path.exists(stamp) or open(stamp).read() != flags_now:
         force = True
         with open(stamp, "w") as f:
@@ -70,11 +80,11 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
     jobs = []
     for src in SOURCES:
         sp = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(out_dir, src + ".o")
         objs.append(obj)
         if not force and _newer(obj, [sp] + hdrs):
             continue
-        cmd = [nvcc, "-c", sp, "-o", obj] + common_flags() + extra_flags()
+        cmd = [nvcc, "-c", sp, "-o", obj] + common_flags() + flags
         if ptxas_verbose and src.endswith(".cu"):
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)
@@ -89,15 +99,15 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed for {cmd[2]}")
-    if force or jobs or not _newer(LIB, objs):
-        tmp = LIB + ".tmp"
+    if force or jobs or not _newer(lib_path, objs):
+        tmp = lib_path + ".tmp"
         cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -1,10 +1,12 @@
 // kz_api.cu — the C ABI of include/kazen_gb300.h: scene management, host
 // validation, device memory, and the wavefront render loop driver.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -44,6 +46,18 @@ kz_status fail(kz_status code, const char* fmt, ...) {
     } while (0)
 
 // A growable device allocation.
+// Host-side fault injection for tests: with KZ_FAIL_ALLOC_AFTER=N in the
+// environment, device allocations after the first N of the process fail as
+// an out-of-memory would (KZ_ERR_OOM), without touching the GPU.
+bool injected_alloc_failure() {
+    static const long limit = [] {
+        const char* v = std::getenv("KZ_FAIL_ALLOC_AFTER");
+        return v ? std::strtol(v, nullptr, 10) : -1L;
+    }();
+    static std::atomic<long> count{0};
+    return limit >= 0 && count.fetch_add(1) >= limit;
+}
+
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -53,6 +67,8 @@ struct DevBuf {
         ptr = nullptr;
         bytes = 0;
         size_t b = std::max<size_t>(want, 256);
+        if (injected_alloc_failure())
+            return fail(KZ_ERR_OOM, "cudaMalloc(%zu): refused by KZ_FAIL_ALLOC_AFTER (injected)", b);
         cudaError_t e = cudaMalloc(&ptr, b);
         if (e != cudaSuccess) {
             ptr = nullptr;
@@ -1249,15 +1265,30 @@ kz_status guide_train_device(kz_guide* g, const float4* samples, uint32_t count,
                              cudaStream_t st) {
     KZ_TRY(g->train_rec.ensure((size_t)rows * 496 * 2));
     KZ_CUDA(cudaMemsetAsync(g->grad.ptr, 0, KZ_GUIDE_PARAMS * 4, st));
-    KZ_CUDA(cudaMemsetAsync(g->loss.ptr, 0, 4, st));
-    kz::launch_guide_train(samples, count, rows, stride, offset, wscale, wcap, g->dev(sc),
-                           static_cast<__nv_bfloat16*>(g->train_rec.ptr), g->grad.as<float>(), g->loss.as<float>(), st);
+    KZ_CUDA(cudaMemsetAsync(g->loss.ptr, 0, 4, st));  // the loss sum; the status word after it is sticky
+    KZ_CUDA(kz::launch_guide_train(samples, count, rows, stride, offset, wscale, wcap, g->dev(sc),
+                                   static_cast<__nv_bfloat16*>(g->train_rec.ptr), g->grad.as<float>(),
+                                   g->loss.as<float>(), reinterpret_cast<uint32_t*>(g->loss.as<float>() + 1), st));
     KZ_CUDA(cudaGetLastError());
     if (apply) {
         g->step += 1;
         kz::launch_guide_adam(g->w.as<float>(), g->m.as<float>(), g->v.as<float>(), g->grad.as<float>(),
                               static_cast<__nv_bfloat16*>(g->wbf.ptr), lr, g->step, st);
         KZ_CUDA(cudaGetLastError());
+    }
+    return KZ_OK;
+}
+
+// The loss of the last training step and the weight-gradient kernel's
+// status word (set when one of its waits ran out; cleared once reported).
+kz_status guide_read_loss(kz_guide* g, float* loss, cudaStream_t st) {
+    uint32_t h[2] = {0, 0};
+    KZ_CUDA(cudaMemcpyAsync(h, g->loss.ptr, 8, cudaMemcpyDeviceToHost, st));
+    KZ_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(loss, &h[0], 4);
+    if (h[1]) {
+        KZ_CUDA(cudaMemsetAsync(g->loss.as<float>() + 1, 0, 4, st));
+        return fail((kz_status)h[1], "guiding weight-gradient kernel: a wait ran out (status %u)", h[1]);
     }
     return KZ_OK;
 }
@@ -1294,6 +1325,7 @@ kz_status kz_guide_create(kz_guide** out, uint64_t seed) {
         if (st == KZ_OK) st = b->ensure(KZ_GUIDE_PARAMS * 4);
     if (st == KZ_OK) st = g->wbf.ensure(KZ_GUIDE_PARAMS * 2);
     if (st == KZ_OK) st = g->loss.ensure(16);
+    if (st == KZ_OK && cudaMemset(g->loss.ptr, 0, 16) != cudaSuccess) st = fail(KZ_ERR_CUDA, "cudaMemset failed");
     if (st == KZ_OK) st = g->ctr.ensure(16);
     if (st != KZ_OK) return bail(st);
     std::vector<float> p;
@@ -1315,6 +1347,36 @@ kz_status kz_guide_get_params(kz_guide* g, float* out) {
     KZ_CUDA(cudaSetDevice(g->device));
     KZ_CUDA(cudaMemcpyAsync(out, g->w.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, g->stream));
     KZ_CUDA(cudaStreamSynchronize(g->stream));
+    return KZ_OK;
+}
+
+kz_status kz_guide_get_state(kz_guide* g, float* out, uint32_t* out_step) {
+    if (!g || !out) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    KZ_CUDA(cudaMemcpyAsync(out, g->w.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, g->stream));
+    KZ_CUDA(cudaMemcpyAsync(out + KZ_GUIDE_PARAMS, g->m.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, g->stream));
+    KZ_CUDA(cudaMemcpyAsync(out + 2 * KZ_GUIDE_PARAMS, g->v.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost,
+                            g->stream));
+    KZ_CUDA(cudaStreamSynchronize(g->stream));
+    if (out_step) *out_step = (uint32_t)g->step;
+    return KZ_OK;
+}
+
+kz_status kz_guide_set_state(kz_guide* g, const float* in, uint32_t step) {
+    if (!g || !in) return fail(KZ_ERR_INVALID_ARG, "NULL argument");
+    for (int i = 0; i < 3 * KZ_GUIDE_PARAMS; ++i)
+        if (!std::isfinite(in[i])) return fail(KZ_ERR_INVALID_ARG, "state value %d is not finite", i);
+    for (int i = 2 * KZ_GUIDE_PARAMS; i < 3 * KZ_GUIDE_PARAMS; ++i)
+        if (in[i] < 0.f) return fail(KZ_ERR_INVALID_ARG, "second moment %d is negative", i - 2 * KZ_GUIDE_PARAMS);
+    std::lock_guard<std::mutex> lk(g->mu);
+    KZ_CUDA(cudaSetDevice(g->device));
+    KZ_TRY(guide_upload_params(g, in));  // weights (and their BF16 copy); zeroes the moments
+    KZ_CUDA(cudaMemcpyAsync(g->m.ptr, in + KZ_GUIDE_PARAMS, KZ_GUIDE_PARAMS * 4, cudaMemcpyHostToDevice, g->stream));
+    KZ_CUDA(cudaMemcpyAsync(g->v.ptr, in + 2 * KZ_GUIDE_PARAMS, KZ_GUIDE_PARAMS * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+    KZ_CUDA(cudaStreamSynchronize(g->stream));
+    g->step = (int)step;
     return KZ_OK;
 }
 
@@ -1371,9 +1433,8 @@ kz_status kz_guide_train_step(kz_guide* g, const float* samples, uint64_t n, flo
     KZ_TRY(guide_train_device(g, ds, (uint32_t)n, (uint32_t)n, 1, 0, 1.0f / (float)n, 3.0e38f, lr, apply != 0,
                               nullptr, st));
     float loss = 0.f;
-    KZ_CUDA(cudaMemcpyAsync(&loss, g->loss.ptr, 4, cudaMemcpyDeviceToHost, st));
     if (out_grad) KZ_CUDA(cudaMemcpyAsync(out_grad, g->grad.ptr, KZ_GUIDE_PARAMS * 4, cudaMemcpyDeviceToHost, st));
-    KZ_CUDA(cudaStreamSynchronize(st));
+    KZ_TRY(guide_read_loss(g, &loss, st));
     if (out_loss) *out_loss = loss;
     return KZ_OK;
 }
@@ -1514,8 +1575,7 @@ kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, co
                     gs.train_steps += 1;
                 }
                 float loss = 0.f;
-                KZ_CUDA(cudaMemcpyAsync(&loss, g->loss.ptr, 4, cudaMemcpyDeviceToHost, strm));
-                KZ_CUDA(cudaStreamSynchronize(strm));
+                KZ_TRY(guide_read_loss(g, &loss, strm));
                 gs.last_loss = loss;
             }
             train_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1600,11 +1660,18 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
     bool textured = false;  // the texture tint is compiled out unless a job needs it
     for (uint32_t j = 0; j < n_jobs; ++j)
         textured |= jobs[j].scene->dev.mat_tex != nullptr || jobs[j].scene->dev.tri_nrm != nullptr;
+    // refill period P: free wavefront slots take new paths every P-th
+    // iteration (P = 1: every iteration); in between the wavefront drains, so
+    // the generation launches are fewer and the live paths fewer too
+    const uint32_t period = std::max<uint32_t>(1, cfg.refill_period);
+    if (iters % period) iters += period - iters % period;
+    iters += iters & 1u;
     auto enqueue = [&]() {
         kz::PathSoA a = A, b = B;
         for (uint32_t it = 0; it < iters; ++it) {
-            kz::launch_plan(ctr, cap, strm);
-            kz::launch_generate_batch_dev(djobs, n_jobs, a, ctr, cap, block, strm);
+            const bool gen = it % period == 0;
+            kz::launch_plan(ctr, cap, strm, gen);
+            if (gen) kz::launch_generate_batch_dev(djobs, n_jobs, a, ctr, cap, block, strm);
             kz::launch_trace_paths_batch(djobs, a, cap, ctr, strm);
             kz::launch_shade_batch(djobs, a, cap, b, sq, ctr, block, textured, strm);
             kz::launch_trace_shadow_batch(djobs, sq, cap, ctr, strm);

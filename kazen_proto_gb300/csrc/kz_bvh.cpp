@@ -520,7 +520,7 @@ void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out, const WideBuild
             }
     }
     out.n_nodes = (uint32_t)(out.nodes.size() / kWideWords);
-    if (out.depth > (uint32_t)kWideStack) throw std::length_error("wide BVH deeper than the traversal stack");
+    if (out.depth > (uint32_t)kWideDepthCap) throw std::length_error("wide BVH deeper than the traversal stack");
 }
 
 }  // namespace kz

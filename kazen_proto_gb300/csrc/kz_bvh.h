@@ -45,7 +45,17 @@ constexpr int kMaxBvhDepth = 60;
 // them: (v0.xyz, global triangle id), (v1.xyz, geom id), (v2.xyz, material
 // id), the integer fields stored as raw 32-bit patterns.
 constexpr int kWideWords = 20;
-constexpr int kWideStack = 96;  // >= wide depth: binary depth cap + 32 count splits
+// The builder rejects trees deeper than kWideDepthCap (binary depth cap + 32
+// count splits); the traversal's group stack has kWideStack entries. They are
+// equal in every product build. A test build may define KZ_WIDE_STACK smaller
+// to drive the traversal into its stack-overflow path (KZ_ERR_STACK) on
+// ordinary trees.
+constexpr int kWideDepthCap = 96;
+#ifndef KZ_WIDE_STACK
+#define KZ_WIDE_STACK 96
+#endif
+constexpr int kWideStack = KZ_WIDE_STACK;
+static_assert(kWideStack >= 1 && kWideStack <= kWideDepthCap, "traversal stack size out of range");
 
 struct WideBvhOutput {
     std::vector<uint32_t> nodes;   // n_nodes * kWideWords

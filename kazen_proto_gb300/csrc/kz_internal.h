@@ -205,10 +205,17 @@ void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const Gu
 void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd, float* raw, cudaStream_t st);
 // One training batch of `rows` samples; row r reads sample ((r + offset) * stride) % count.
 // Adds the weighted loss to *loss and the gradient to grad; a sample's weight
-// is min(weight * wscale, wcap).
-void launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, uint32_t stride, uint32_t offset,
-                        float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
-                        cudaStream_t st);
+// is min(weight * wscale, wcap). The weight gradients run on the tcgen05
+// kernel (kz_mlp_tc.cu), which records a stuck wait in *status; with
+// KZ_GUIDE_WGRAD=mma in the environment the warp-level mma.sync kernel runs
+// instead (for side-by-side measurement).
+cudaError_t launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, uint32_t stride,
+                               uint32_t offset, float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec,
+                               float* grad, float* loss, uint32_t* status, cudaStream_t st);
+// ---- tcgen05 weight gradients (kz_mlp_tc.cu) --------------------------------
+cudaError_t guide_wgrad_tc_setup();
+cudaError_t launch_guide_wgrad_tc(const __nv_bfloat16* rec, uint32_t n, float* grad, uint32_t* status,
+                                  cudaStream_t st);
 void launch_guide_adam(float* w, float* m, float* v, const float* grad, __nv_bfloat16* wbf, float lr, int step,
                        cudaStream_t st);
 void launch_guide_to_bf16(const float* w, __nv_bfloat16* wbf, cudaStream_t st);
@@ -223,7 +230,9 @@ void launch_scale(float* film, double* film64, uint64_t n, float sf, double sd, 
 // shade, shadow, finish; every count lives in DevCounters, so the host can
 // enqueue many iterations between synchronisations. Grids are sized for the
 // capacity `cap`; threads beyond the device-side count exit.
-void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st);
+// plan: reserve slots for new paths (unless !generate) and reset the
+// iteration's queue counters
+void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st, bool generate = true);
 void launch_finish(DevCounters* ctr, cudaStream_t st);
 void launch_generate_camera_dev(const DevCamera& cam, const PathParams& pp, PathSoA dst, DevCounters* ctr,
                                 uint32_t cap, uint32_t block, cudaStream_t st);

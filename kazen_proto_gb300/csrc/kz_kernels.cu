@@ -57,10 +57,10 @@ __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __res
 }
 
 // ------------------------------------------------------------------ device-driven loop
-__global__ void k_plan(DevCounters* c, uint32_t cap) {
+__global__ void k_plan(DevCounters* c, uint32_t cap, bool generate) {
     const uint64_t remaining = c->total - c->next_path;
     const uint32_t room = cap - c->n_active;
-    const uint32_t n_new = (uint32_t)(remaining < room ? remaining : room);
+    const uint32_t n_new = generate ? (uint32_t)(remaining < room ? remaining : room) : 0u;
     c->gen_first = c->next_path;
     c->gen_count = n_new;
     c->gen_slot = c->n_active;
@@ -113,7 +113,9 @@ void launch_generate_rays(const kz_ray* rays, const PathParams& pp, PathSoA dst,
     if (!n_new) return;
     k_generate_rays<<<grid_for(n_new, block), block, 0, st>>>(rays, pp, dst, dst_offset, first_path, n_new);
 }
-void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st) { k_plan<<<1, 1, 0, st>>>(ctr, cap); }
+void launch_plan(DevCounters* ctr, uint32_t cap, cudaStream_t st, bool generate) {
+    k_plan<<<1, 1, 0, st>>>(ctr, cap, generate);
+}
 void launch_finish(DevCounters* ctr, cudaStream_t st) { k_finish<<<1, 1, 0, st>>>(ctr); }
 void launch_generate_camera_dev(const DevCamera& cam, const PathParams& pp, PathSoA dst, DevCounters* ctr,
                                 uint32_t cap, uint32_t block, cudaStream_t st) {

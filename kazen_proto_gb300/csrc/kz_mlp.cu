@@ -11,6 +11,9 @@
 // so activations never leave registers inside the fused kernels.
 #include <cuda_bf16.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "kz_guide.cuh"
 #include "kz_internal.h"
 
@@ -487,6 +490,7 @@ cudaError_t guide_kernel_setup() {
         e = cudaFuncSetAttribute(k_guide_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTrain);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemWgrad);
+    if (e == cudaSuccess) e = guide_wgrad_tc_setup();
     return e;
 }
 
@@ -515,19 +519,22 @@ void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd
     k_guide_infer<false><<<grid, 128, kSmemInfer, st>>>(none, np, pts, n, gd, raw, nullptr);
 }
 
-void launch_guide_train(const float4* samples, uint32_t count, uint32_t n, uint32_t stride, uint32_t offset,
-                        float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec, float* grad, float* loss,
-                        cudaStream_t st) {
-    if (!n || !count) return;
+cudaError_t launch_guide_train(const float4* samples, uint32_t count, uint32_t n, uint32_t stride,
+                               uint32_t offset, float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec,
+                               float* grad, float* loss, uint32_t* status, cudaStream_t st) {
+    if (!n || !count) return cudaSuccess;
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = min((tiles + kTrainWarps - 1) / kTrainWarps, (uint32_t)sm_count() * 2);
     k_guide_train_fb<<<grid, kTrainWarps * 32, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, wcap,
                                                                   rec, loss);
+    const char* sel = getenv("KZ_GUIDE_WGRAD");
+    if (!(sel && strcmp(sel, "mma") == 0)) return launch_guide_wgrad_tc(rec, n, grad, status, st);
     const uint32_t ctas = min((n + kChunk - 1) / kChunk, (uint32_t)sm_count() * 2);
     uint32_t rows = (n + ctas - 1) / ctas;
     rows = (rows + kChunk - 1) / kChunk * kChunk;
     const uint32_t g2 = (n + rows - 1) / rows;
     k_guide_wgrad<<<g2, kWgWarps * 32, kSmemWgrad, st>>>(rec, n, rows, grad);
+    return cudaGetLastError();
 }
 
 void launch_guide_adam(float* w, float* m, float* v, const float* grad, __nv_bfloat16* wbf, float lr, int step,

@@ -424,7 +424,7 @@ __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& ov
 #ifndef KZ_SMEM_STACK
 #define KZ_SMEM_STACK 8
 #endif
-#if KZ_SMEM_STACK > 0
+#if KZ_SMEM_STACK > 0 && KZ_SMEM_STACK < KZ_WIDE_STACK
 #define KZ_CLOSEST_STACK(name)                       \
     __shared__ uint2 name##_sm[KZ_SMEM_STACK * 256]; \
     uint2 name##_lm[kWideStack - KZ_SMEM_STACK];     \

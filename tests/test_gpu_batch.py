@@ -35,6 +35,9 @@ WAVE = api.BATCH_WAVEFRONT
 @pytest.mark.parametrize("cfg", [dict(mode=WAVE, use_graph=True),
                                  dict(mode=WAVE, block_size=128, wavefront_size=4096, use_graph=False),
                                  dict(mode=WAVE, block_size=64, wavefront_size=1000, use_graph=True),
+                                 dict(mode=WAVE, wavefront_size=3000, refill_period=2, use_graph=True),
+                                 dict(mode=WAVE, block_size=128, wavefront_size=5000, refill_period=3,
+                                      use_graph=False),
                                  dict(mode=MEGA, block_size=128, ctas_per_sm=2, refill_period=1, use_graph=True),
                                  dict(mode=MEGA, block_size=64, ctas_per_sm=1, refill_period=4, use_graph=False),
                                  dict(mode=MEGA, block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True)])
