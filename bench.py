@@ -53,6 +53,9 @@ def parse():
     p.add_argument("--no-box", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-features", action="store_true")
+    p.add_argument("--profile-wgrad", action="store_true",
+                   help="guiding training steps at 2^18 rows (fused tcgen05, split tcgen05, mma.sync), for ncu "
+                        "captures of the training kernels; prints the step times and exits")
     p.add_argument("--profile-guide", action="store_true",
                    help="one small guided render with training (slit room 128x128, 32 spp), for ncu captures "
                         "of the guiding network kernels; prints its stats and exits")
@@ -488,8 +491,10 @@ def guiding_bench(R=1024, budgets_spp=(1024, 2048), ref_spp=65536, max_depth=10,
                       "cost_per_sample_vs_plain": round(Tf / T, 3)}
         g.close()
     s.close()
+    net = network_bench()
     return {"scene": "slit room %dx%d, max depth %d, 24 Lambert quads + 32 GGX spheres, 4x4 exterior light "
                      "(radiance 200) behind a 0.05x0.5 slit" % (R, R, max_depth),
+            "training_step": net,
             "network": "51 -> 64 -> 64 -> 64 -> 40 (8 vMF lobes), BF16 weights, FP32 accumulation, Adam lr %g, "
                        "%d radiance samples per training step" % (lr, rows),
             "reference": "plain, %d spp, FP64 accumulation, two independent halves (%.1f s)" % (ref_spp, ref_s),
@@ -582,6 +587,58 @@ def load_traffic():
         if m:
             out[key] = float(m.group(1))
     return out if "dram_bytes_per_ray" in out else None
+
+
+def network_bench(rows=1 << 18, steps=20):
+    """The guiding network's training step at its stated batch (2^18 radiance
+    samples, random positions, normals and directions, device-resident): mean
+    wall time per step (forward + mixture loss + backward + weight gradients)
+    of the three implementations: one tcgen05 kernel (the default), the
+    warp-level forward/backward with tcgen05 weight gradients, and both
+    warp-level (KZ_GUIDE_TRAIN = fused / tc / mma)."""
+    import ctypes as C
+
+    import torch
+
+    from kazen_proto_gb300 import _native as N
+    from kazen_proto_gb300 import api
+    rng = np.random.default_rng(1)
+    smp = np.zeros((rows, 12), np.float32)
+    smp[:, 0:3] = rng.random((rows, 3))
+    smp[:, 3] = rng.random(rows) + 0.1
+    n = rng.standard_normal((rows, 3))
+    smp[:, 4:7] = n / np.linalg.norm(n, axis=1, keepdims=True)
+    dv = rng.standard_normal((rows, 3))
+    smp[:, 8:11] = dv / np.linalg.norm(dv, axis=1, keepdims=True)
+    dsmp = torch.from_numpy(smp).cuda()
+    g = api.Guide(seed=2)
+    lib = N.lib()
+    loss = C.c_float()
+    out = {}
+    for name, val in (("fused_tcgen05", "fused"), ("split_tcgen05_wgrad", "tc"), ("mma_sync", "mma")):
+        os.environ["KZ_GUIDE_TRAIN"] = val
+        for _ in range(3):
+            N.check(lib.kz_guide_train_step(g.handle, C.c_void_p(dsmp.data_ptr()), rows, 1e-3, 0, C.byref(loss),
+                                            None, N.KZ_MEM_DEVICE))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            N.check(lib.kz_guide_train_step(g.handle, C.c_void_p(dsmp.data_ptr()), rows, 1e-3, 0, C.byref(loss),
+                                            None, N.KZ_MEM_DEVICE))
+        out[name + "_ms_per_step"] = round((time.perf_counter() - t0) / steps * 1e3, 3)
+    os.environ.pop("KZ_GUIDE_TRAIN", None)
+    g.close()
+    out["rows"] = rows
+    out["note"] = "wall time per kz_guide_train_step call (device samples, gradient only, one host sync per step)"
+    return out
+
+
+def profile_wgrad():
+    """Training steps at 2^18 rows in each implementation (three warm-up
+    steps, then four timed ones, per implementation): the command the
+    training-kernel ncu captures run."""
+    from kazen_proto_gb300 import build as kbuild
+    kbuild.build()
+    print(json.dumps({"workload": "guide_train_step_262144_rows", **network_bench(steps=4)}))
 
 
 def profile_guide():
@@ -815,6 +872,8 @@ if __name__ == "__main__":
     a = parse()
     if a.profile_guide:
         profile_guide()
+    elif a.profile_wgrad:
+        profile_wgrad()
     elif a.impl == "reference":
         run_reference(a)
     else:

@@ -20,8 +20,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libkazen_gb300.so")
 
 SOURCES = ["kz_api.cu", "kz_trace.cu", "kz_kernels.cu", "kz_shade_guided.cu", "kz_batch.cu", "kz_megakernel.cu",
-           "kz_closures.cu", "kz_mlp.cu", "kz_mlp_tc.cu", "kz_bvh.cpp"]
-DEPS = ["kz_device.cuh", "kz_traverse.cuh", "kz_guide.cuh", "kz_stages.cuh", "kz_internal.h", "kz_bvh.h"]
+           "kz_closures.cu", "kz_mlp.cu", "kz_mlp_tc.cu", "kz_guide_tc.cu",
+           "kz_bvh.cpp"]
+DEPS = ["kz_device.cuh", "kz_traverse.cuh", "kz_guide.cuh", "kz_stages.cuh", "kz_internal.h", "kz_bvh.h", "kz_tc.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1263,7 +1263,7 @@ kz_status guide_upload_params(kz_guide* g, const float* host) {
 kz_status guide_train_device(kz_guide* g, const float4* samples, uint32_t count, uint32_t rows, uint32_t stride,
                              uint32_t offset, float wscale, float wcap, float lr, bool apply, const kz::DevScene* sc,
                              cudaStream_t st) {
-    KZ_TRY(g->train_rec.ensure((size_t)rows * 496 * 2));
+    if (kz::guide_train_mode() != 0) KZ_TRY(g->train_rec.ensure((size_t)rows * 496 * 2));  // split paths only
     KZ_CUDA(cudaMemsetAsync(g->grad.ptr, 0, KZ_GUIDE_PARAMS * 4, st));
     KZ_CUDA(cudaMemsetAsync(g->loss.ptr, 0, 4, st));  // the loss sum; the status word after it is sticky
     KZ_CUDA(kz::launch_guide_train(samples, count, rows, stride, offset, wscale, wcap, g->dev(sc),

@@ -54,6 +54,16 @@ __device__ __forceinline__ float guide_feature(int j, f3 p01, f3 n, float band_s
     return 0.f;
 }
 
+// sin and cos of 2^b * pi * bs * x (the input encoding of every guiding
+// kernel). The argument is reduced exactly, t - 2 rint(t / 2) in [-1, 1],
+// before the fast hardware sine and cosine, whose absolute error on
+// [-pi, pi] (~2^-21) is far below the BF16 rounding the features then get.
+__device__ __forceinline__ void band_sincos(float x, int b, float bs, float& sn, float& cs) {
+    const float t = x * (float)(1 << b) * bs;
+    const float r = t - 2.f * rintf(0.5f * t);
+    __sincosf(kPi * r, &sn, &cs);
+}
+
 struct VmfMixture {
     f3 mu[kGuideLobes];
     float kappa[kGuideLobes];

@@ -205,13 +205,23 @@ void launch_guide_infer_paths(const DevScene& s, PathSoA p, uint32_t n, const Gu
 void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd, float* raw, cudaStream_t st);
 // One training batch of `rows` samples; row r reads sample ((r + offset) * stride) % count.
 // Adds the weighted loss to *loss and the gradient to grad; a sample's weight
-// is min(weight * wscale, wcap). The weight gradients run on the tcgen05
-// kernel (kz_mlp_tc.cu), which records a stuck wait in *status; with
-// KZ_GUIDE_WGRAD=mma in the environment the warp-level mma.sync kernel runs
-// instead (for side-by-side measurement).
+// is min(weight * wscale, wcap). A tcgen05 kernel that finds a wait stuck
+// records it in *status. The implementation is chosen by guide_train_mode():
+//   0: one tcgen05 kernel for the whole step (kz_guide_tc.cu; `rec` unused),
+//   1: warp-level forward/backward writing 992-byte records to `rec`, then the
+//      tcgen05 weight gradients (kz_mlp_tc.cu),
+//   2: the same records, then the warp-level weight gradients.
 cudaError_t launch_guide_train(const float4* samples, uint32_t count, uint32_t rows, uint32_t stride,
                                uint32_t offset, float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec,
                                float* grad, float* loss, uint32_t* status, cudaStream_t st);
+// KZ_GUIDE_TRAIN in the environment: "fused" (default) = 0, "tc" = 1, "mma" = 2
+// (the split paths serve side-by-side measurement).
+int guide_train_mode();
+// ---- one-kernel tcgen05 training step (kz_guide_tc.cu) ---------------------
+cudaError_t guide_train_tc_setup();
+cudaError_t launch_guide_train_tc(const float4* samples, uint32_t count, uint32_t n, uint32_t stride,
+                                  uint32_t offset, float wscale, float wcap, const GuideDev& gd, float* grad,
+                                  float* loss, uint32_t* status, cudaStream_t st);
 // ---- tcgen05 weight gradients (kz_mlp_tc.cu) --------------------------------
 cudaError_t guide_wgrad_tc_setup();
 cudaError_t launch_guide_wgrad_tc(const __nv_bfloat16* rec, uint32_t n, float* grad, uint32_t* status,

@@ -81,16 +81,6 @@ __device__ __forceinline__ void to_afrag(const float (&c)[NT][4], uint32_t (&a)[
     }
 }
 
-// sin and cos of 2^b * pi * bs * x. The argument is reduced exactly,
-// t - 2 rint(t / 2) in [-1, 1], before the fast hardware sine and cosine,
-// whose absolute error on [-pi, pi] (~2^-21) is far below the BF16 rounding
-// the features then get.
-__device__ __forceinline__ void band_sincos(float x, int b, float bs, float& sn, float& cs) {
-    const float t = x * (float)(1 << b) * bs;
-    const float r = t - 2.f * rintf(0.5f * t);
-    __sincosf(kPi * r, &sn, &cs);
-}
-
 // Input features of rows g and g+8 straight into A fragments (4 k-tiles).
 // Lane t holds columns 16 kt + 2t (+1) and 16 kt + 2t + 8 (+9): for the
 // position axes kt = 0..2, the sin/cos pairs of bands t and t + 4 (the
@@ -491,6 +481,7 @@ cudaError_t guide_kernel_setup() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemWgrad);
     if (e == cudaSuccess) e = guide_wgrad_tc_setup();
+    if (e == cudaSuccess) e = guide_train_tc_setup();
     return e;
 }
 
@@ -519,16 +510,25 @@ void launch_guide_infer_points(const float4* pts, uint32_t n, const GuideDev& gd
     k_guide_infer<false><<<grid, 128, kSmemInfer, st>>>(none, np, pts, n, gd, raw, nullptr);
 }
 
+int guide_train_mode() {
+    const char* sel = getenv("KZ_GUIDE_TRAIN");
+    if (sel && strcmp(sel, "tc") == 0) return 1;
+    if (sel && strcmp(sel, "mma") == 0) return 2;
+    return 0;
+}
+
 cudaError_t launch_guide_train(const float4* samples, uint32_t count, uint32_t n, uint32_t stride,
                                uint32_t offset, float wscale, float wcap, const GuideDev& gd, __nv_bfloat16* rec,
                                float* grad, float* loss, uint32_t* status, cudaStream_t st) {
     if (!n || !count) return cudaSuccess;
+    const int mode = guide_train_mode();
+    if (mode == 0)
+        return launch_guide_train_tc(samples, count, n, stride, offset, wscale, wcap, gd, grad, loss, status, st);
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = min((tiles + kTrainWarps - 1) / kTrainWarps, (uint32_t)sm_count() * 2);
     k_guide_train_fb<<<grid, kTrainWarps * 32, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, wcap,
                                                                   rec, loss);
-    const char* sel = getenv("KZ_GUIDE_WGRAD");
-    if (!(sel && strcmp(sel, "mma") == 0)) return launch_guide_wgrad_tc(rec, n, grad, status, st);
+    if (mode == 1) return launch_guide_wgrad_tc(rec, n, grad, status, st);
     const uint32_t ctas = min((n + kChunk - 1) / kChunk, (uint32_t)sm_count() * 2);
     uint32_t rows = (n + ctas - 1) / ctas;
     rows = (rows + kChunk - 1) / kChunk * kChunk;

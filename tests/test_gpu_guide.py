@@ -54,33 +54,43 @@ def test_gradient_matches_restatement(gpu, n):
     assert np.array_equal(g.params(), p)
 
 
+@pytest.mark.parametrize("mode", ["fused", "tc"])
 @pytest.mark.parametrize("n", [64, 1000, 70000, 1 << 18])
-def test_tcgen05_weight_gradients_match_warp_mma(gpu, n, monkeypatch):
-    """The weight gradients of the tcgen05 kernel (TMA-staged operands, TMEM
-    accumulators; the default) against the warp-level mma.sync kernel on the
-    same training records: both sum the same BF16 products in FP32, in a
-    different order, so they agree to FP32 rounding of 2^18-term sums. Row
-    counts that are not a multiple of the 64-row chunk exercise the
-    zero-filled tail."""
+def test_tcgen05_training_matches_warp_mma(gpu, n, mode, monkeypatch):
+    """The tcgen05 training paths against the warp-level mma.sync kernels on
+    the same samples: "tc" keeps the warp-level forward/backward and runs the
+    weight gradients on tcgen05 (TMA-staged records, TMEM accumulators) -- the
+    same BF16 products summed in another order, so FP32 rounding apart;
+    "fused" (the default) runs the whole step in one tcgen05 kernel, whose
+    layer sums in another order can flip a BF16 rounding of an activation, so
+    it agrees to a few 1e-3 of the gradient's norm. Row counts that are not a
+    multiple of the tiles exercise the tails."""
     rng = np.random.default_rng(n + 1)
     g = api.Guide(seed=1)
     p = G.init_params(4)
     g.set_params(p)
     p01, nrm, d, w = rand_batch(rng, n)
+    monkeypatch.setenv("KZ_GUIDE_TRAIN", mode)
     loss_tc, grad_tc = g.train_step(p01, nrm, d, w, apply=False, want_grad=True)
-    monkeypatch.setenv("KZ_GUIDE_WGRAD", "mma")
+    monkeypatch.setenv("KZ_GUIDE_TRAIN", "mma")
     loss_mma, grad_mma = g.train_step(p01, nrm, d, w, apply=False, want_grad=True)
-    monkeypatch.delenv("KZ_GUIDE_WGRAD")
-    # the forward/backward kernel is shared (its loss is an atomic sum)
-    assert abs(loss_tc - loss_mma) <= 1e-5 * abs(loss_mma) + 1e-7
+    monkeypatch.delenv("KZ_GUIDE_TRAIN")
     live = np.ones_like(grad_tc, bool)
     live[:64 * 64] = (np.arange(64 * 64) % 64) < 51  # layer-1 padding columns are not parameters
     scale = np.abs(grad_mma[live]).max()
-    assert np.abs(grad_tc[live] - grad_mma[live]).max() <= 1e-4 * scale + 1e-7
-    assert np.linalg.norm(grad_tc[live] - grad_mma[live]) <= 1e-4 * np.linalg.norm(grad_mma[live]) + 1e-7
-    # biases come from the ones block of the tensor-core product
-    b = slice(64 * 64, 64 * 64 + 64)
-    assert np.allclose(grad_tc[b], grad_mma[b], rtol=1e-4, atol=1e-6 * scale)
+    nrm_mma = np.linalg.norm(grad_mma[live])
+    b = slice(64 * 64, 64 * 64 + 64)  # layer-1 biases: the ones block of the tensor-core product
+    if mode == "tc":
+        # the forward/backward kernel is shared (its loss is an atomic sum)
+        assert abs(loss_tc - loss_mma) <= 1e-5 * abs(loss_mma) + 1e-7
+        assert np.abs(grad_tc[live] - grad_mma[live]).max() <= 1e-4 * scale + 1e-7
+        assert np.linalg.norm(grad_tc[live] - grad_mma[live]) <= 1e-4 * nrm_mma + 1e-7
+        assert np.allclose(grad_tc[b], grad_mma[b], rtol=1e-4, atol=1e-6 * scale)
+    else:
+        assert abs(loss_tc - loss_mma) <= 1e-3 * abs(loss_mma) + 1e-6, (loss_tc, loss_mma)
+        assert np.linalg.norm(grad_tc[live] - grad_mma[live]) <= 5e-3 * nrm_mma, \
+            np.linalg.norm(grad_tc[live] - grad_mma[live]) / nrm_mma
+        assert np.linalg.norm(grad_tc[b] - grad_mma[b]) <= 5e-3 * np.linalg.norm(grad_mma[b]) + 1e-7
 
 
 def test_training_fits_a_direction_field(gpu):
