@@ -190,7 +190,7 @@ struct kz_scene {
     kz_scene_info info{};
 
     // device scene
-    DevBuf nodes, tris, geom_offset, geom_light, mats, lights, light_cdf, light_tris;
+    DevBuf nodes, tris, geom_offset, geom_light, mats, lights, light_cdf, light_tris, mat_class;
     // textures and environment
     std::vector<kz::DevTexture> textures;  // offsets into tex_texels
     std::vector<float> tex_texels;
@@ -215,8 +215,9 @@ struct kz_scene {
         if (!cuda_ready) return;
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
-        DevBuf* all[] = {&nodes, &tris, &geom_offset, &geom_light, &mats, &lights, &light_cdf, &light_tris,
-                         &status, &s_rays, &s_t, &s_prim, &s_geom, &s_u, &s_v, &s_occ, &s_ctr, &s_next, &ctr, &film, &film64};
+        DevBuf* all[] = {&nodes, &tris, &geom_offset, &geom_light, &mats, &mat_class, &lights, &light_cdf,
+                         &light_tris, &status, &s_rays, &s_t, &s_prim, &s_geom, &s_u, &s_v, &s_occ, &s_ctr, &s_next,
+                         &ctr, &film, &film64, &d_tri_uv, &d_mat_tex, &d_textures, &d_texels, &d_tri_nrm};
         for (DevBuf* b : all) b->release();
         for (auto& b : pa) b.release();
         for (auto& b : pb) b.release();
@@ -821,6 +822,32 @@ kz_status kz_scene_build(kz_scene* s) {
     KZ_TRY(upload(s->geom_offset, goff, st));
     KZ_TRY(upload(s->geom_light, glight, st));
     KZ_TRY(upload(s->mats, s->materials, st));
+    {
+        // shading class of each material (by its first lobe), the key the
+        // shading kernel groups a block's paths by
+        std::vector<uint8_t> cls(s->materials.size());
+        for (size_t m = 0; m < s->materials.size(); ++m) {
+            const kz_material& mt = s->materials[m];
+            uint8_t c = 3;  // no lobe (emitter only)
+            if (mt.n_lobes > 0) {
+                switch (mt.lobes[0].closure_id) {
+                case KZ_CLOSURE_KP_MIRROR: case KZ_CLOSURE_KP_DIELECTRIC: case KZ_CLOSURE_REFLECTION:
+                case KZ_CLOSURE_REFRACTION: case KZ_CLOSURE_TRANSPARENT:
+                    c = 2;  // delta
+                    break;
+                case KZ_CLOSURE_KP_GLOSS: case KZ_CLOSURE_KP_GLASS: case KZ_CLOSURE_CONDUCTOR_GGX:
+                case KZ_CLOSURE_KP_PRINCIPLE_SPECULAR_REFL: case KZ_CLOSURE_WARD: case KZ_CLOSURE_KP_MICROFACET:
+                case KZ_CLOSURE_KP_PRINCIPLE_CLEARCOAT: case KZ_CLOSURE_PHONG:
+                    c = 1;  // glossy
+                    break;
+                default:
+                    c = 0;  // diffuse-like
+                }
+            }
+            cls[m] = c;
+        }
+        KZ_TRY(upload(s->mat_class, cls, st));
+    }
     KZ_TRY(upload(s->lights, lights, st));
     KZ_TRY(upload(s->light_cdf, cdf, st));
     KZ_TRY(upload(s->light_tris, ltris, st));
@@ -858,6 +885,7 @@ kz_status kz_scene_build(kz_scene* s) {
     d.geom_offset = s->geom_offset.as<uint32_t>();
     d.geom_light = s->geom_light.as<int32_t>();
     d.materials = s->mats.as<kz_material>();
+    d.mat_class = s->mat_class.as<uint8_t>();
     d.n_materials = (uint32_t)s->materials.size();
     d.lights = s->lights.as<kz::DevLight>();
     d.light_cdf = s->light_cdf.as<float>();

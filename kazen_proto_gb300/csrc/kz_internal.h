@@ -39,6 +39,7 @@ struct DevScene {
     const uint32_t* geom_offset = nullptr;  // first global triangle id per mesh
     const int32_t* geom_light = nullptr;    // light index per mesh or -1
     const kz_material* materials = nullptr;
+    const uint8_t* mat_class = nullptr;  // per material: 0 diffuse-like, 1 glossy, 2 delta, 3 no lobe
     uint32_t n_materials = 0;
     const DevLight* lights = nullptr;
     const float* light_cdf = nullptr;

@@ -601,13 +601,42 @@ static unsigned resident_grid(F f, unsigned block) {
 #ifndef KZ_SHADE_MIN_BLOCKS
 #define KZ_SHADE_MIN_BLOCKS 4
 #endif
+// KZ_SHADE_SORT: group each block's paths by kind (miss, material shading
+// class) before shading them
+#ifndef KZ_SHADE_SORT
+#define KZ_SHADE_SORT 0
+#endif
 template <bool kGuided, bool kAttr = true>
 __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
                                                GuideShade gs, const uint32_t* n_dev) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n_in = *n_dev;
+#if KZ_SHADE_SORT
+    // regroup the block's paths by kind before shading them: misses, then
+    // hits by the material's shading class, then empty slots, so that each
+    // warp runs one branch of shade_vertex (counting sort in shared memory;
+    // the order within a kind is arbitrary, each path's result is not)
+    __shared__ uint32_t s_cnt[6];
+    __shared__ uint32_t s_perm[256];
+    uint32_t key = 5u;
+    if (i < n_in) {
+        const int rec = __float_as_int(in.hit[i].w);
+        key = rec < 0 ? 0u
+                      : 1u + __ldg(s.mat_class +
+                                   __float_as_uint(__ldg(reinterpret_cast<const float*>(s.tris + (size_t)rec * 3 + 2) + 3)));
+    }
+    if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t rank = atomicAdd(&s_cnt[key], 1u);
+    __syncthreads();
+    uint32_t first = 0u;
+    for (uint32_t k = 0; k < key; ++k) first += s_cnt[k];
+    s_perm[first + rank] = i;
+    __syncthreads();
+    i = s_perm[threadIdx.x];
+#endif
     ShadeOut so;
     if (i < n_in) {
         shade_vertex<kGuided, kAttr>(s, pp, in.hit[i], in.o4[i], in.d4[i], in.b4[i], in.rng[i], gs,
