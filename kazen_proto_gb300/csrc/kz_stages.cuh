@@ -602,9 +602,11 @@ static unsigned resident_grid(F f, unsigned block) {
 #define KZ_SHADE_MIN_BLOCKS 4
 #endif
 // KZ_SHADE_SORT: group each block's paths by kind (miss, material shading
-// class) before shading them
+// class) before shading them. Measured on the terrain frame: shade stage
+// 40.4 -> 33.4 ms, trace +1.3 ms (the next wavefront's order changes), frame
+// 1,441 -> 1,480 Mpaths*bounces/s.
 #ifndef KZ_SHADE_SORT
-#define KZ_SHADE_SORT 0
+#define KZ_SHADE_SORT 1
 #endif
 template <bool kGuided, bool kAttr = true>
 __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
