@@ -28,8 +28,12 @@ __global__ void k_generate_batch_dev(const DevJob* __restrict__ jobs, uint32_t n
 template <bool kAttr>
 __global__ void __launch_bounds__(256, 4) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
                                                      ShadowSoA sq, DevCounters* ctr) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n_in = ctr->n_active;
+#if KZ_SHADE_SORT
+    i = block_group_by_kind(
+        i, i < n_in ? shade_kind(jobs[__float_as_uint(in.d4[i].w) >> kJobShift].scene, in.hit[i]) : 5u);
+#endif
     ShadeOut so;
     if (i < n_in) {
         const float4 d4 = in.d4[i];

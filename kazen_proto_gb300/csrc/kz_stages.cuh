@@ -595,6 +595,33 @@ static unsigned resident_grid(F f, unsigned block) {
     return (unsigned)(sms > 0 ? sms : 1) * (unsigned)(per_sm > 0 ? per_sm : 1);
 }
 
+// Shading kind of a traced path: 0 a miss, 1 + the material's shading class
+// for a hit (diffuse-like, glossy, delta, no lobe).
+__device__ __forceinline__ uint32_t shade_kind(const DevScene& s, const float4 hit) {
+    const int rec = __float_as_int(hit.w);
+    if (rec < 0) return 0u;
+    const uint32_t m = __float_as_uint(__ldg(reinterpret_cast<const float*>(s.tris + (size_t)rec * 3 + 2) + 3));
+    return 1u + __ldg(s.mat_class + m);
+}
+
+// Regroups a block's paths by kind (0..5, 5 = no path) before they are
+// shaded, so each warp runs one branch of shade_vertex: a counting sort in
+// shared memory; returns the path index this thread shades. The order within
+// a kind is arbitrary; each path's result is not. blockDim.x <= 256.
+__device__ __forceinline__ uint32_t block_group_by_kind(uint32_t i, uint32_t kind) {
+    __shared__ uint32_t s_cnt[6];
+    __shared__ uint32_t s_perm[256];
+    if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t rank = atomicAdd(&s_cnt[kind], 1u);
+    __syncthreads();
+    uint32_t first = 0u;
+    for (uint32_t k = 0; k < kind; ++k) first += s_cnt[k];
+    s_perm[first + rank] = i;
+    __syncthreads();
+    return s_perm[threadIdx.x];
+}
+
 // Plain shading is capped at 64 registers (4 blocks per SM): the occupancy
 // gained outweighs a few spills (measured: 5 % faster); the guided variant
 // keeps its registers (at 64 it spills 728 bytes per thread).
@@ -604,7 +631,9 @@ static unsigned resident_grid(F f, unsigned block) {
 // KZ_SHADE_SORT: group each block's paths by kind (miss, material shading
 // class) before shading them. Measured on the terrain frame: shade stage
 // 40.4 -> 33.4 ms, trace +1.3 ms (the next wavefront's order changes), frame
-// 1,441 -> 1,480 Mpaths*bounces/s.
+// 1,441 -> 1,480 Mpaths*bounces/s. (Also writing the continuing paths
+// grouped by the octant of their next direction, one atomic per block,
+// measured trace -3.0 ms but shade +4.2 ms: not kept.)
 #ifndef KZ_SHADE_SORT
 #define KZ_SHADE_SORT 1
 #endif
@@ -616,28 +645,7 @@ __global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n_in = *n_dev;
 #if KZ_SHADE_SORT
-    // regroup the block's paths by kind before shading them: misses, then
-    // hits by the material's shading class, then empty slots, so that each
-    // warp runs one branch of shade_vertex (counting sort in shared memory;
-    // the order within a kind is arbitrary, each path's result is not)
-    __shared__ uint32_t s_cnt[6];
-    __shared__ uint32_t s_perm[256];
-    uint32_t key = 5u;
-    if (i < n_in) {
-        const int rec = __float_as_int(in.hit[i].w);
-        key = rec < 0 ? 0u
-                      : 1u + __ldg(s.mat_class +
-                                   __float_as_uint(__ldg(reinterpret_cast<const float*>(s.tris + (size_t)rec * 3 + 2) + 3)));
-    }
-    if (threadIdx.x < 6) s_cnt[threadIdx.x] = 0u;
-    __syncthreads();
-    const uint32_t rank = atomicAdd(&s_cnt[key], 1u);
-    __syncthreads();
-    uint32_t first = 0u;
-    for (uint32_t k = 0; k < key; ++k) first += s_cnt[k];
-    s_perm[first + rank] = i;
-    __syncthreads();
-    i = s_perm[threadIdx.x];
+    i = block_group_by_kind(i, i < n_in ? shade_kind(s, in.hit[i]) : 5u);
 #endif
     ShadeOut so;
     if (i < n_in) {
