@@ -3,8 +3,10 @@
 // with every contraction on the 5th-generation tensor cores and the weight
 // gradients accumulated in tensor memory across the CTA's rows.
 //
-// A CTA of 128 threads owns tiles of 128 training rows; thread t is row t of
-// the tile and lane t of tensor memory. Per tile:
+// A CTA of 256 threads owns tiles of 128 training rows; warps w and w + 4
+// serve TMEM lanes 32 (w % 4) .. + 31, i.e. rows r = t % 128, and split every
+// 64-column epilogue into halves (h = t / 128: columns 32h .. 32h + 31). Per
+// tile:
 //   X  = features (8-band sin/cos of the position, normal)   -> smem tile
 //   Hl = ReLU(H(l-1) W_l^T + b_l), l = 1..3                  -> smem tiles
 //   O  = H3 W4^T + b4 (40 outputs); dO = d(w * -log q)/dO     -> smem tile
@@ -12,9 +14,11 @@
 //   dZ1 = (dZ2 W2) * [H1 > 0]                                 -> smem tiles
 //   dW += [dZ1 | dZ2]^T [X | H1 | 1],  [dZ3 | dO]^T [H2 | H3 | 1]
 // Each product is one tcgen05.mma chain issued by thread 0 (M = 128 rows);
-// its FP32 result in tensor memory is read back by all four warps
-// (tcgen05.ld, 32 lanes each), which apply bias, ReLU or the ReLU mask and
-// store the BF16 operand of the next product into shared memory. Every
+// its FP32 result in tensor memory is read back by all eight warps
+// (tcgen05.ld, 32 lanes x 32 columns each), which apply bias, ReLU or the
+// ReLU mask and store the BF16 operand of the next product into shared
+// memory. The mixture loss of a row is computed by its half-0 thread (the
+// other half's output columns pass through shared memory). Every
 // activation tile is a [128 rows][64] BF16 matrix in the 128-byte-swizzled
 // layout (kz_tc.cuh): K-major for the forward and backward products, and,
 // unchanged, the MN-major transpose for the weight-gradient products (rows
@@ -42,7 +46,8 @@ namespace kz {
 namespace {
 using namespace tc;
 
-constexpr int kT = 128;               // rows per tile = threads = TMEM lanes
+constexpr int kT = 128;               // rows per tile = TMEM lanes
+constexpr int kThreads = 256;         // two threads per row
 constexpr uint32_t kTile = kT * 128;  // bytes of a [128][64] BF16 tile (16 KB)
 constexpr uint32_t kWt = 64 * 128;    // bytes of a [64][64] BF16 weight tile (8 KB)
 // shared-memory layout (from the 1024-byte-aligned base)
@@ -66,31 +71,33 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// store 64 floats as one BF16 line (row `r`) of a swizzled tile
-__device__ __forceinline__ void store_line(unsigned char* tile, uint32_t r, const float* v) {
+// store 32 floats as half `h` (chunks 4h .. 4h + 3) of the BF16 line of row `r`
+__device__ __forceinline__ void store_half(unsigned char* tile, uint32_t r, uint32_t h, const float* v) {
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int cc = 0; cc < 4; ++cc) {
+        const int c = 4 * (int)h + cc;
         uint4 q;
-        q.x = pack2(v[8 * c + 0], v[8 * c + 1]);
-        q.y = pack2(v[8 * c + 2], v[8 * c + 3]);
-        q.z = pack2(v[8 * c + 4], v[8 * c + 5]);
-        q.w = pack2(v[8 * c + 6], v[8 * c + 7]);
+        q.x = pack2(v[8 * cc + 0], v[8 * cc + 1]);
+        q.y = pack2(v[8 * cc + 2], v[8 * cc + 3]);
+        q.z = pack2(v[8 * cc + 4], v[8 * cc + 5]);
+        q.w = pack2(v[8 * cc + 6], v[8 * cc + 7]);
         *reinterpret_cast<uint4*>(tile + sw128(r, c)) = q;
     }
 }
 
-// the positive-part mask of a stored BF16 line: bit k set where element k > 0
-__device__ __forceinline__ uint64_t positive_mask(const unsigned char* tile, uint32_t r) {
-    uint64_t m = 0;
+// the positive-part mask of half `h` of a stored BF16 line: bit k set where
+// element 32h + k > 0
+__device__ __forceinline__ uint32_t positive_mask_half(const unsigned char* tile, uint32_t r, uint32_t h) {
+    uint32_t m = 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const uint4 q = *reinterpret_cast<const uint4*>(tile + sw128(r, c));
+    for (int cc = 0; cc < 4; ++cc) {
+        const uint4 q = *reinterpret_cast<const uint4*>(tile + sw128(r, 4 * h + cc));
         const uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int e = 0; e < 4; ++e) {
             // BF16 > 0: sign bit clear and not +0
-            if (!(w[h] & 0x8000u) && (w[h] & 0x7FFFu)) m |= 1ull << (8 * c + 2 * h);
-            if (!(w[h] & 0x80000000u) && (w[h] & 0x7FFF0000u)) m |= 1ull << (8 * c + 2 * h + 1);
+            if (!(w[e] & 0x8000u) && (w[e] & 0x7FFFu)) m |= 1u << (8 * cc + 2 * e);
+            if (!(w[e] & 0x80000000u) && (w[e] & 0x7FFF0000u)) m |= 1u << (8 * cc + 2 * e + 1);
         }
     }
     return m;
@@ -102,10 +109,11 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
         umma_bf16(d, desc_sw128(a + 32u * ks, 16, 1024), desc_sw128(b + 32u * ks, 16, 1024), idesc, ks > 0);
 }
 
-__global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restrict__ samples, uint32_t count,
-                                                           uint32_t n, uint32_t stride, uint32_t offset, GuideDev gd,
-                                                           float inv_n, float wcap, float* __restrict__ grad,
-                                                           float* __restrict__ loss, uint32_t* __restrict__ status) {
+__global__ void __launch_bounds__(kThreads, 1) k_guide_train_tc(const float4* __restrict__ samples, uint32_t count,
+                                                                 uint32_t n, uint32_t stride, uint32_t offset,
+                                                                 GuideDev gd, float inv_n, float wcap,
+                                                                 float* __restrict__ grad, float* __restrict__ loss,
+                                                                 uint32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char* sm =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -115,6 +123,8 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
     volatile uint32_t* failed = reinterpret_cast<volatile uint32_t*>(bars + 4);
     const uint32_t bar_mma = smem_u32(&bars[0]), bar_wg = smem_u32(&bars[1]), bar_end = smem_u32(&bars[2]);
     const int t = threadIdx.x, warp = t >> 5;
+    const uint32_t row = (uint32_t)t & (kT - 1);  // tile row = TMEM lane
+    const uint32_t half = (uint32_t)t >> 7;       // columns 32 * half .. + 31 of each product
     const uint32_t tiles = (n + kT - 1) / kT;
     if (blockIdx.x >= tiles) return;  // uniform over the CTA
 
@@ -123,7 +133,7 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
     const int offs[4] = {kOffW1, kOffW2, kOffW3, kOffW4};
     const uint32_t wt[4] = {oW1, oW2, oW3, oW4};
     for (int l = 0; l < 4; ++l)
-        for (int i = t; i < 64 * 8; i += kT) {
+        for (int i = t; i < 64 * 8; i += kThreads) {
             const int line = i >> 3, c = i & 7;
             uint4 q = make_uint4(0u, 0u, 0u, 0u);
             if (l < 3 || line < 40) q = *reinterpret_cast<const uint4*>(Wg + offs[l] + line * 64 + 8 * c);
@@ -131,14 +141,14 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
         }
     const uint32_t wtt[3] = {oW2T, oW3T, oW4T};
     for (int l = 1; l < 4; ++l)
-        for (int i = t; i < 64 * 64; i += kT) {
+        for (int i = t; i < 64 * 64; i += kThreads) {
             const int in = i >> 6, o = i & 63;  // line `in` of W_l^T holds W_l[o][in] over o
             __nv_bfloat16 v = __float2bfloat16_rn(0.f);
             if (l < 3 || o < 40) v = Wg[offs[l] + o * 64 + in];
             *reinterpret_cast<__nv_bfloat16*>(sm + wtt[l - 1] + sw128(in, o >> 3) + 2 * (o & 7)) = v;
         }
     const uint32_t one2 = pack2(1.f, 1.f);
-    for (uint32_t i = t; i < kTile / 4; i += kT) {
+    for (uint32_t i = t; i < kTile / 4; i += kThreads) {
         reinterpret_cast<uint32_t*>(sm + oOne0)[i] = one2;
         reinterpret_cast<uint32_t*>(sm + oOne1)[i] = one2;
     }
@@ -155,8 +165,9 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lanes = (uint32_t)(32 * warp) << 16;  // this warp's TMEM lane quadrant
-    const uint32_t S = tmem + lanes + kScratch;            // scratch accumulator, this thread's lane
+    const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;  // this warp's TMEM lane quadrant
+    const uint32_t S = tmem + lanes + kScratch + 32u * half;  // this thread's 32 scratch columns
+    float* raw_hi = reinterpret_cast<float*>(sm + oD1);       // [128][8] outputs 32..39 (dZ1's tile is free then)
 
     const f3 ext = mk(1.f / gd.box_inv.x, 1.f / gd.box_inv.y, 1.f / gd.box_inv.z);
     const float* Wf = gd.wf;
@@ -178,96 +189,114 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
         fence_after_sync();
         return *failed == 0u;
     };
-    // one product into the scratch accumulator, then this row's 64 (or 48) columns
-    auto product = [&](uint32_t a, uint32_t b, int ksteps, uint32_t idesc, float* v, int cols) {
+    // one product into the scratch accumulator, then this thread's 32 columns
+    // (16 for half 1 of the 48-column product; the rest zero)
+    auto product = [&](uint32_t a, uint32_t b, int ksteps, uint32_t idesc, float (&v)[32], bool narrow) {
         if (t == 0) {
             mma_chain(tmem + kScratch, base + a, base + b, ksteps, idesc);
             umma_commit(bar_mma);
         }
         wait_phase(bar_mma, ph_mma);
-        float tmp[32];
-        tmem_ld32(S, tmp);
+        if (narrow && half) {
+            tmem_ld16(S, v);
 #pragma unroll
-        for (int k = 0; k < 32; ++k) v[k] = tmp[k];
-        if (cols == 64) {
-            tmem_ld32(S + 32, tmp);
-#pragma unroll
-            for (int k = 0; k < 32; ++k) v[32 + k] = tmp[k];
+            for (int k = 16; k < 32; ++k) v[k] = 0.f;
         } else {
-            tmem_ld16(S + 32, v + 32);
-#pragma unroll
-            for (int k = 48; k < 64; ++k) v[k] = 0.f;
+            tmem_ld32(S, v);
         }
     };
 
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t r = tile * kT + t;
+        const uint32_t r = tile * kT + row;
         const bool valid = r < n;
         f3 p = mk(0.5f, 0.5f, 0.5f), nn = mk(0.f, 1.f, 0.f), dir = mk(0.f, 1.f, 0.f);
         float w = 0.f;
         if (valid) {
             const size_t si = (size_t)(((uint64_t)(r + offset) * stride) % count);
-            const float4 a = samples[3 * si], b = samples[3 * si + 1], c = samples[3 * si + 2];
+            const float4 a = samples[3 * si], b = samples[3 * si + 1];
             p = mk(a.x, a.y, a.z);
             nn = mk(b.x, b.y, b.z);
-            dir = mk(c.x, c.y, c.z);
-            w = fminf(a.w * inv_n, wcap);
+            if (half == 0) {
+                const float4 c = samples[3 * si + 2];
+                dir = mk(c.x, c.y, c.z);
+                w = fminf(a.w * inv_n, wcap);
+            }
         }
         // the previous tile's weight-gradient products read the tiles rewritten below
         if (any_wg) wait_phase(bar_wg, ph_wg);
-        float v[64];
-        // ---- features
+        float v[32];
+        // ---- features: half 0 the x and y bands (columns 0..31), half 1 the
+        // z bands, the normal and the zero padding (32..63)
+        if (half == 0) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+            for (int a = 0; a < 2; ++a)
 #pragma unroll
-            for (int b = 0; b < 8; ++b)
-                band_sincos(comp(p, a), b, gd.band_scale, v[16 * a + 2 * b], v[16 * a + 2 * b + 1]);
-        v[48] = nn.x;
-        v[49] = nn.y;
-        v[50] = nn.z;
+                for (int b = 0; b < 8; ++b)
+                    band_sincos(comp(p, a), b, gd.band_scale, v[16 * a + 2 * b], v[16 * a + 2 * b + 1]);
+        } else {
 #pragma unroll
-        for (int k = 51; k < 64; ++k) v[k] = 0.f;
-        store_line(sm + oX, t, v);
+            for (int b = 0; b < 8; ++b) band_sincos(p.z, b, gd.band_scale, v[2 * b], v[2 * b + 1]);
+            v[16] = nn.x;
+            v[17] = nn.y;
+            v[18] = nn.z;
+#pragma unroll
+            for (int k = 19; k < 32; ++k) v[k] = 0.f;
+        }
+        store_half(sm + oX, row, half, v);
         if (!stage_sync()) break;
         // ---- hidden layers
         const uint32_t ain[3] = {oX, oH1, oH2}, aout[3] = {oH1, oH2, oH3}, wl[3] = {oW1, oW2, oW3};
         const int boff[3] = {kOffB1, kOffB2, kOffB3};
         bool ok = true;
         for (int l = 0; l < 3 && ok; ++l) {
-            product(ain[l], wl[l], 4, kIdF64, v, 64);
+            product(ain[l], wl[l], 4, kIdF64, v, false);
+            const float* bias = Wf + boff[l] + 32 * half;
 #pragma unroll
-            for (int k = 0; k < 64; ++k) v[k] = fmaxf(v[k] + __ldg(Wf + boff[l] + k), 0.f);
-            store_line(sm + aout[l], t, v);
+            for (int k = 0; k < 32; ++k) v[k] = fmaxf(v[k] + __ldg(bias + k), 0.f);
+            store_half(sm + aout[l], row, half, v);
             ok = stage_sync();
         }
         if (!ok) break;
-        // ---- outputs, loss and its gradient
-        product(oH3, oW4, 4, kIdF48, v, 48);
-        float raw[kGuideOut], g[kGuideOut];
+        // ---- outputs, loss and its gradient (the half-0 thread of the row)
+        product(oH3, oW4, 4, kIdF48, v, true);
+        if (half) {
 #pragma unroll
-        for (int k = 0; k < kGuideOut; ++k) raw[k] = v[k] + __ldg(Wf + kOffB4 + k);
-        if (valid) {
-            loss_acc += w * mixture_nll_grad(raw, dir, w, g, p, ext);
-        } else {
-#pragma unroll
-            for (int k = 0; k < kGuideOut; ++k) g[k] = 0.f;
+            for (int k = 0; k < 8; ++k) raw_hi[row * 8 + k] = v[k];  // outputs 32..39
         }
+        __syncthreads();
+        if (half == 0) {
+            float raw[kGuideOut], g[kGuideOut];
 #pragma unroll
-        for (int k = 0; k < kGuideOut; ++k) v[k] = g[k];
+            for (int k = 0; k < 32; ++k) raw[k] = v[k] + __ldg(Wf + kOffB4 + k);
 #pragma unroll
-        for (int k = kGuideOut; k < 64; ++k) v[k] = 0.f;
-        store_line(sm + oDO, t, v);
+            for (int k = 0; k < 8; ++k) raw[32 + k] = raw_hi[row * 8 + k] + __ldg(Wf + kOffB4 + 32 + k);
+            if (valid) {
+                loss_acc += w * mixture_nll_grad(raw, dir, w, g, p, ext);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kGuideOut; ++k) g[k] = 0.f;
+            }
+            float lo[32], hi[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) lo[k] = g[k];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) hi[k] = g[32 + k];
+#pragma unroll
+            for (int k = 8; k < 32; ++k) hi[k] = 0.f;
+            store_half(sm + oDO, row, 0, lo);
+            store_half(sm + oDO, row, 1, hi);
+        }
         if (!stage_sync()) break;
         // ---- backward: dZ3, dZ2, dZ1
         const uint32_t bin[3] = {oDO, oD3, oD2}, bw[3] = {oW4T, oW3T, oW2T}, hmask[3] = {oH3, oH2, oH1},
                        bout[3] = {oD3, oD2, oD1};
         const int ksteps[3] = {3, 4, 4};  // dO has 48 columns
         for (int l = 0; l < 3 && ok; ++l) {
-            product(bin[l], bw[l], ksteps[l], kIdF64, v, 64);
-            const uint64_t m = positive_mask(sm + hmask[l], t);
+            product(bin[l], bw[l], ksteps[l], kIdF64, v, false);
+            const uint32_t m = positive_mask_half(sm + hmask[l], row, half);
 #pragma unroll
-            for (int k = 0; k < 64; ++k) v[k] = ((m >> k) & 1ull) ? v[k] : 0.f;
-            store_line(sm + bout[l], t, v);
+            for (int k = 0; k < 32; ++k) v[k] = ((m >> k) & 1u) ? v[k] : 0.f;
+            store_half(sm + bout[l], row, half, v);
             ok = stage_sync();
         }
         if (!ok) break;
@@ -294,7 +323,6 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
     fence_after_sync();
     const bool ok_all = *failed == 0u;
     if (ok_all && any_wg) {
-        const uint32_t row = 32 * warp + (t & 31);
         const uint32_t coff = row < 64 ? 0u : 64u;  // the diagonal block's columns
 #pragma unroll
         for (int pair = 0; pair < 2; ++pair) {
@@ -304,21 +332,18 @@ __global__ void __launch_bounds__(kT, 1) k_guide_train_tc(const float4* __restri
             const int outs = layer == 3 ? 40 : 64;
             const int woff = layer == 0 ? kOffW1 : layer == 1 ? kOffW2 : layer == 2 ? kOffW3 : kOffW4;
             const int bo = layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : layer == 2 ? kOffB3 : kOffB4;
+            float d[32];
+            tmem_ld32(dbase + coff + 32 * half, d);
+            if (o < outs)
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float d[32];
-                tmem_ld32(dbase + coff + 32 * h, d);
-                if (o < outs)
-#pragma unroll
-                    for (int k = 0; k < 32; ++k)
-                        if (d[k] != 0.f) atomicAdd(grad + woff + o * 64 + 32 * h + k, d[k]);
-            }
+                for (int k = 0; k < 32; ++k)
+                    if (d[k] != 0.f) atomicAdd(grad + woff + o * 64 + 32 * half + k, d[k]);
             const float db = tmem_ld1(dbase + 128);
-            if (o < outs && db != 0.f) atomicAdd(grad + bo + o, db);
+            if (half == 0 && o < outs && db != 0.f) atomicAdd(grad + bo + o, db);
         }
     }
     if (!ok_all && t == 0) atomicExch(status, (uint32_t)KZ_ERR_TIMEOUT);
-    // the loss of the CTA's rows
+    // the loss of the CTA's rows (the half-0 threads hold it)
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, s);
     if ((t & 31) == 0 && loss_acc != 0.f) atomicAdd(loss, loss_acc);
@@ -350,8 +375,8 @@ cudaError_t launch_guide_train_tc(const float4* samples, uint32_t count, uint32_
     if (!n || !count) return cudaSuccess;
     const uint32_t tiles = (n + kT - 1) / kT;
     const uint32_t grid = min(tiles, (uint32_t)sm_count_train());
-    k_guide_train_tc<<<grid, kT, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, wcap, grad, loss,
-                                                   status);
+    k_guide_train_tc<<<grid, kThreads, kSmemTrain, st>>>(samples, count, n, stride, offset, gd, wscale, wcap, grad,
+                                                         loss, status);
     return cudaGetLastError();
 }
 
