@@ -46,7 +46,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--small", action="store_true", help="reduced workload (quick checks only)")
     p.add_argument("--profile", action="store_true",
-                   help="full-size scene, 640x360 frame at 4 spp, for ncu captures of single launches")
+                   help="full-size scene, 640x360 frame at 16 spp (3.7 M paths: full 2^21-path wavefronts), for ncu "
+                        "captures of single launches")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-traversal", action="store_true")
     p.add_argument("--no-guiding", action="store_true")
@@ -66,7 +67,7 @@ def workload(args):
     if args.small:
         return dict(width=320, height=180, spp=8, max_depth=8, cells=256, n_spheres=64, wavefront=1 << 18)
     if getattr(args, "profile", False):
-        return dict(width=640, height=360, spp=4, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
+        return dict(width=640, height=360, spp=16, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
     return dict(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
 
 

@@ -102,7 +102,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
                 raise RuntimeError(f"nvcc failed for {cmd[2]}")
     if force or jobs or not _newer(lib_path, objs):
         tmp = lib_path + ".tmp"
-        cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC"]
+        cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -10,6 +10,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+
+#include <nvtx3/nvToolsExt.h>
 #include <vector>
 
 #include "kz_bvh.h"
@@ -18,6 +20,15 @@
 namespace {
 
 thread_local std::string g_last_error;
+
+// Host range of one API call or wavefront batch, seen by NVTX-aware
+// profilers (no-op without one attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 kz_status fail(kz_status code, const char* fmt, ...) {
     char buf[512];
@@ -378,6 +389,7 @@ kz_status run_wavefront(kz_scene* s, const kz::DevCamera* cam, const kz_ray* ray
     kz_render_stats st{};
     st.paths = total;
     for (;;) {
+        const NvtxRange batch_range("wavefront batch");
         for (uint32_t it = 0; it < batch; ++it) {
             cudaEvent_t* e = timing ? &ev[5 * (size_t)it] : nullptr;
             if (e) KZ_CUDA(cudaEventRecord(e[0], strm));
@@ -651,6 +663,7 @@ kz_status kz_scene_set_environment(kz_scene* s, const float rgb[3], int32_t text
 }
 
 kz_status kz_scene_build(kz_scene* s) {
+    const NvtxRange nvtx_range("kz_scene_build");
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     // validate everything on the host before any device work
@@ -938,6 +951,7 @@ kz_status kz_scene_synchronize(kz_scene* s) {
 }
 
 kz_status kz_intersect_closest(kz_scene* s, const kz_ray* rays, uint64_t n, kz_hits hits, int32_t mem) {
+    const NvtxRange nvtx_range("kz_intersect_closest");
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1002,6 +1016,7 @@ kz_status kz_intersect_closest(kz_scene* s, const kz_ray* rays, uint64_t n, kz_h
 }
 
 kz_status kz_intersect_any(kz_scene* s, const kz_ray* rays, uint64_t n, uint8_t* occluded, int32_t mem) {
+    const NvtxRange nvtx_range("kz_intersect_any");
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1030,6 +1045,7 @@ kz_status kz_intersect_any(kz_scene* s, const kz_ray* rays, uint64_t n, uint8_t*
 
 kz_status kz_intersect_stats(kz_scene* s, const kz_ray* rays, uint64_t n, int32_t mem, uint64_t* out_nodes,
                              uint64_t* out_tris) {
+    const NvtxRange nvtx_range("kz_intersect_stats");
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1143,6 +1159,7 @@ static kz_status check_cfg(const kz_render_config* cfg) {
 
 kz_status kz_li_batch(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_render_config* cfg, float* out_rgb,
                       int32_t mem, kz_render_stats* out_stats) {
+    const NvtxRange nvtx_range("kz_li_batch");
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1174,6 +1191,7 @@ kz_status kz_li_batch(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_rend
 
 kz_status kz_render(kz_scene* s, const kz_camera* camera, const kz_film_desc* fd, const kz_render_config* cfg,
                     float* out_rgb, double* out_rgb64, int32_t mem, kz_render_stats* out_stats) {
+    const NvtxRange nvtx_range("kz_render");
     KZ_TRY(check_mem(mem));
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1418,6 +1436,7 @@ kz_status kz_guide_set_params(kz_guide* g, const float* in) {
 }
 
 kz_status kz_guide_forward(kz_guide* g, const float* points, uint64_t n, float* out_raw, int32_t mem) {
+    const NvtxRange nvtx_range("kz_guide_forward");
     KZ_TRY(check_mem(mem));
     if (!g) return fail(KZ_ERR_INVALID_ARG, "guide is NULL");
     if (n == 0) return KZ_OK;
@@ -1444,6 +1463,7 @@ kz_status kz_guide_forward(kz_guide* g, const float* points, uint64_t n, float* 
 
 kz_status kz_guide_train_step(kz_guide* g, const float* samples, uint64_t n, float lr, int32_t apply,
                               float* out_loss, float* out_grad, int32_t mem) {
+    const NvtxRange nvtx_range("kz_guide_train_step");
     KZ_TRY(check_mem(mem));
     if (!g) return fail(KZ_ERR_INVALID_ARG, "guide is NULL");
     if (n == 0 || n > (1u << 20)) return fail(KZ_ERR_INVALID_ARG, "n must be in [1, 2^20]");
@@ -1470,6 +1490,7 @@ kz_status kz_guide_train_step(kz_guide* g, const float* samples, uint64_t n, flo
 kz_status kz_render_guided(kz_scene* s, kz_guide* g, const kz_camera* camera, const kz_film_desc* fd,
                            const kz_render_config* cfg, const kz_guide_config* gcfg_in, float* out_rgb,
                            double* out_rgb64, int32_t mem, kz_render_stats* out_stats, kz_guide_stats* out_gstats) {
+    const NvtxRange nvtx_range("kz_render_guided");
     const auto t_start = std::chrono::steady_clock::now();
     KZ_TRY(check_mem(mem));
     if (!s || !g) return fail(KZ_ERR_INVALID_ARG, "scene and guide are required");
@@ -1773,6 +1794,7 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
 
 extern "C" kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, const kz_batch_config* cfg_in,
                                      int32_t mem, kz_batch_stats* out_stats) {
+    const NvtxRange nvtx_range("kz_render_batch");
     KZ_TRY(check_mem(mem));
     if (n_jobs == 0) return KZ_OK;
     if (!jobs) return fail(KZ_ERR_INVALID_ARG, "jobs is NULL");
@@ -2011,6 +2033,7 @@ kz::PathSoA carve_paths(unsigned char* base) {
 
 extern "C" kz_status kz_li_batch_noalloc(kz_scene* s, const kz_ray* rays, uint64_t n, const kz_render_config* cfg,
                                          float* out_rgb, kz_render_stats* out_stats) {
+    const NvtxRange nvtx_range("kz_li_batch_noalloc");
     if (!s) return fail(KZ_ERR_INVALID_ARG, "scene is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     KZ_TRY(check_cfg(cfg));  // before the scene check: needs no device

@@ -110,13 +110,49 @@ __device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long
     }
 }
 
+// Leaf triangles of the persistent kernels tested warp-wide
+// (persistent_rays_shared) rather than per lane (persistent_rays).
+#ifndef KZ_SHARE_LEAVES
+#define KZ_SHARE_LEAVES 1
+#endif
+
 // Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
 // ray up, store(k, hit) writes the result.
-// `s` is the lane's scene; load may repoint it per ray (batched jobs).
-template <bool kCount, typename Ctr, typename Load, typename Store>
+// `s` is the lane's scene; load may repoint it per ray (batched jobs: kOwnScene).
+template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Store>
 __device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
                                                    Store store, uint32_t& dn, uint32_t& dt) {
     KZ_CLOSEST_STACK(stack);
+#if KZ_SHARE_LEAVES
+    KZ_LEAF_SHARE(sh);
+    ClosestState c;
+    TRay r;
+    float tmax = 0.f;
+    uint32_t octp = 0;
+    Ctr ray = 0;
+    persistent_rays_shared(
+        n, next, kTraceRefill,
+        [&](Ctr k) {
+            ray = k;
+            load(k, r, tmax);
+            octp = wide_octant(r);
+            closest_begin(c, tmax);
+            publish_ray(sh, r);
+        },
+        [&](uint32_t& tbits, uint32_t& tbase) {
+            return closest_node<kCount>(s, r, octp, c, stack, tbits, tbase, dn, dt);
+        },
+        [&](uint32_t tbits, uint32_t tbase) { closest_leaves<kOwnScene>(sh, s.tris, tbits, tbase, c); },
+        [&](int rc) {
+            if (rc == 0) rc = group_pop(c, stack);
+            if (rc == 0) return false;
+            HitRec h;
+            closest_finish(c, rc > 0, tmax, h);
+            if (rc < 0) set_status(status, KZ_ERR_STACK);
+            store(ray, h);
+            return true;
+        });
+#else
     ClosestState c;
     TRay r;
     float tmax = 0.f;
@@ -137,6 +173,47 @@ __device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next
             closest_finish(c, rc > 0, tmax, h);
             if (rc < 0) set_status(status, KZ_ERR_STACK);
             store(ray, h);
+            return true;
+        });
+#endif
+}
+
+// Any hit of ray k through persistent_rays_shared: load(k, r, tmax) sets the
+// ray up, done(k, rc) gets 1 (no hit), 2 (hit) or -1 (aborted: miss).
+template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Done>
+__device__ __forceinline__ void persistent_any(DevScene& s, Ctr n, Ctr* next, Load load, Done done, uint32_t& dn,
+                                               uint32_t& dt) {
+    uint2 stack_lm[kWideStack];
+    const LocalStack stack{stack_lm};
+    KZ_LEAF_SHARE_ANY(sh);
+    AnyState c;
+    TRay r;
+    float tmax = 0.f;
+    uint32_t octp = 0;
+    Ctr ray = 0;
+    bool hit = false;
+    persistent_rays_shared(
+        n, next, kTraceRefill,
+        [&](Ctr k) {
+            ray = k;
+            load(k, r, tmax);
+            octp = wide_octant(r);
+            any_begin(c);
+            publish_ray(sh, r);
+            publish_tmax(sh, tmax);
+        },
+        [&](uint32_t& tbits, uint32_t& tbase) {
+            return any_node<kCount>(s, r, octp, tmax, c, stack, tbits, tbase, dn, dt);
+        },
+        [&](uint32_t tbits, uint32_t tbase) {
+            const uint32_t hits = any_leaves<kOwnScene>(sh, s.tris, tbits, tbase);
+            hit = hits != 0u;
+            if (kCount) dt += any_tested(tbits, hits);
+        },
+        [&](int rc) {
+            if (rc == 0) rc = hit ? 2 : group_pop(c, stack);
+            if (rc == 0) return false;
+            done(ray, rc);
             return true;
         });
 }

@@ -4,6 +4,12 @@
 // global cursor, for single renders and batched jobs.
 #include "kz_stages.cuh"
 
+// Resident 256-thread blocks per SM the persistent traversal kernels are
+// compiled for (4: at most 64 registers a thread).
+#ifndef KZ_TRACE_MINB
+#define KZ_TRACE_MINB 4
+#endif
+
 namespace kz {
 namespace {
 
@@ -64,7 +70,7 @@ __global__ void __launch_bounds__(256) k_trace_paths(DevScene s, PathSoA p, uint
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_trace_paths_persistent(DevScene s, PathSoA p, DevCounters* ctr) {
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_paths_persistent(DevScene s, PathSoA p, DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
     persistent_closest<kCount>(
         s, ctr->n_active, &ctr->trace_next, &ctr->status,
@@ -78,7 +84,7 @@ __global__ void __launch_bounds__(256) k_trace_paths_persistent(DevScene s, Path
 }
 
 // kz_intersect_closest: rays (o, tmin, d, tmax) in, hit fields out.
-__global__ void __launch_bounds__(256) k_intersect_closest_persistent(DevScene s, const kz_ray* __restrict__ rays,
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_intersect_closest_persistent(DevScene s, const kz_ray* __restrict__ rays,
                                                                       unsigned long long n, kz_hits hits,
                                                                       unsigned long long* next, uint32_t* status) {
     uint32_t dn = 0, dt = 0;
@@ -121,10 +127,34 @@ __global__ void __launch_bounds__(256) k_trace_shadow(DevScene s, ShadowSoA sq, 
 // Persistent form of k_trace_shadow for the device-driven loop (k_plan zeroes
 // shadow_next each iteration).
 template <bool kCount, bool kGuided>
-__global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, ShadowSoA sq, DevCounters* ctr,
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_persistent(DevScene s, ShadowSoA sq, DevCounters* ctr,
                                                                  float* film, double* film64, VRec* recs, NRec* nee,
                                                                  uint32_t max_depth) {
     uint32_t dn = 0, dt = 0;
+    const auto unoccluded = [&](uint32_t ray) {
+        const float4 cc = sq.c4[ray];
+        film_add(film, film64, __float_as_uint(sq.d4[ray].w), xyz(cc));
+        if (kGuided && recs) {
+            const uint32_t tag = __float_as_uint(cc.w);
+            const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
+            propagate(recs, rb, tag & 15u, xyz(cc));
+            if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
+        }
+    };
+#if KZ_SHARE_LEAVES
+    persistent_any<kCount>(
+        s, ctr->n_shadow, &ctr->shadow_next,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = sq.o4[k], d = sq.d4[k];
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = o.w;
+        },
+        [&](uint32_t ray, int rc) {
+            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
+            if (rc == 1) unoccluded(ray);
+        },
+        dn, dt);
+#else
     uint2 stack_lm[kWideStack];
     const LocalStack stack{stack_lm};
     AnyState c;
@@ -145,18 +175,10 @@ __global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, Sha
             const int rc = any_step<kCount>(s, r, octp, tmax, c, stack, dn, dt);
             if (rc == 0) return false;
             if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
-            if (rc == 1) {
-                const float4 cc = sq.c4[ray];
-                film_add(film, film64, __float_as_uint(sq.d4[ray].w), xyz(cc));
-                if (kGuided && recs) {
-                    const uint32_t tag = __float_as_uint(cc.w);
-                    const uint64_t rb = (uint64_t)(tag >> 4) * max_depth;
-                    propagate(recs, rb, tag & 15u, xyz(cc));
-                    if (nee) nee[rb + (tag & 15u)].n.w = 1.f;
-                }
-            }
+            if (rc == 1) unoccluded(ray);
             return true;
         });
+#endif
     if (kCount) warp_count(dn, dt, &ctr->fetch[2]);
 }
 
@@ -164,11 +186,11 @@ __global__ void __launch_bounds__(256) k_trace_shadow_persistent(DevScene s, Sha
 // whose integrand estimate L*f*cos is positive, weighted by its luminance
 // over the pdf the direction was sampled with.
 
-__global__ void __launch_bounds__(256) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
                                                            DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
     DevScene ls;
-    persistent_closest<false>(
+    persistent_closest<false, true>(
         ls, ctr->n_active, &ctr->trace_next, &ctr->status,
         [&](uint32_t k, TRay& r, float& tmax) {
             const float4 o = p.o4[k], d = p.d4[k];
@@ -179,14 +201,31 @@ __global__ void __launch_bounds__(256) k_trace_paths_batch(const DevJob* __restr
         [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
 }
 
-__global__ void __launch_bounds__(256) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
                                                             DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
+    DevScene ls;
+#if KZ_SHARE_LEAVES
+    persistent_any<false, true>(
+        ls, ctr->n_shadow, &ctr->shadow_next,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = sq.o4[k], d = sq.d4[k];
+            trace_fields(ls, jobs[__float_as_uint(sq.c4[k].w)].scene);
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = o.w;
+        },
+        [&](uint32_t ray, int rc) {
+            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
+            if (rc == 1)
+                film_add(jobs[__float_as_uint(sq.c4[ray].w)].film, nullptr, __float_as_uint(sq.d4[ray].w),
+                         xyz(sq.c4[ray]));
+        },
+        dn, dt);
+#else
     uint2 stack_lm[kWideStack];
     const LocalStack stack{stack_lm};
     AnyState c;
     TRay r;
-    DevScene ls;
     float tmax = 0.f;
     uint32_t octp = 0, ray = 0, job = 0;
     persistent_rays(
@@ -208,6 +247,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow_batch(const DevJob* __rest
             if (rc == 1) film_add(jobs[job].film, nullptr, __float_as_uint(sq.d4[ray].w), xyz(sq.c4[ray]));
             return true;
         });
+#endif
 }
 
 }  // namespace

@@ -88,11 +88,34 @@ __device__ __forceinline__ bool tri_test(const TRay& r, float4 a, float4 b, floa
     return true;
 }
 
+// The per-ray terms of the watertight test: the origin in the permuted axes
+// (kx, ky, kz), the shear and the ray's lower bound.
+struct TriRay {
+    float okx, oky, okz, tmin;
+    float Sx, Sy, Sz;
+    int kx, ky, kz;
+};
+
+__device__ __forceinline__ TriRay tri_ray(const TRay& r) {
+    TriRay q;
+    q.okx = comp(r.o, r.kx);
+    q.oky = comp(r.o, r.ky);
+    q.okz = comp(r.o, r.kz);
+    q.tmin = r.tmin;
+    q.Sx = r.Sx;
+    q.Sy = r.Sy;
+    q.Sz = r.Sz;
+    q.kx = r.kx;
+    q.ky = r.ky;
+    q.kz = r.kz;
+    return q;
+}
+
 // The same test with the barycentric divisions left to the caller:
 // u = V / det, v = W / det for the hit that is kept.
-__device__ __forceinline__ bool tri_test_t(const TRay& r, float4 a, float4 b, float4 c, float& t, float& V_, float& W_,
-                                           float& det_) {
-    const float okx = comp(r.o, r.kx), oky = comp(r.o, r.ky), okz = comp(r.o, r.kz);
+__device__ __forceinline__ bool tri_test_t(const TriRay& r, float4 a, float4 b, float4 c, float& t, float& V_,
+                                           float& W_, float& det_) {
+    const float okx = r.okx, oky = r.oky, okz = r.okz;
     const float Akx = pick(a, r.kx) - okx, Aky = pick(a, r.ky) - oky, Akz = pick(a, r.kz) - okz;
     const float Bkx = pick(b, r.kx) - okx, Bky = pick(b, r.ky) - oky, Bkz = pick(b, r.kz) - okz;
     const float Ckx = pick(c, r.kx) - okx, Cky = pick(c, r.ky) - oky, Ckz = pick(c, r.kz) - okz;
@@ -116,6 +139,10 @@ __device__ __forceinline__ bool tri_test_t(const TRay& r, float4 a, float4 b, fl
     W_ = W;
     det_ = det;
     return true;
+}
+__device__ __forceinline__ bool tri_test_t(const TRay& r, float4 a, float4 b, float4 c, float& t, float& V_, float& W_,
+                                           float& det_) {
+    return tri_test_t(tri_ray(r), a, b, c, t, V_, W_, det_);
 }
 
 struct HitRec {
@@ -408,6 +435,288 @@ __device__ bool trace_any(const DevScene& s, const TRay& r, float tmax, bool& ov
     return rc == 2;
 }
 
+// ---- warp-shared leaf tests ---------------------------------------------------
+//
+// In the persistent kernels a traversal step is split into a node part (the
+// lane's node test; its leaf triangles are left pending), a warp-wide part in
+// which all 32 lanes, busy or idle, test the pending (ray, triangle) pairs of
+// the whole warp, 32 at a time, and a pop of the next node group. A per-lane
+// triangle loop would run for the warp's largest leaf count with a few lanes
+// active; sharing the pairs spreads them over the warp.
+//
+// Each lane publishes its ray (TriRay) in shared memory when it starts one.
+// The closest hit of a step is exact and independent of which lane tested
+// what: candidates are combined by a 64-bit atomicMin of (t in a total order,
+// global triangle id) on the owner's slot, the lexicographic minimum that the
+// sequential loop keeps (smaller t, then smaller id), then the lane whose
+// candidate won writes its record, its unrounded t and the barycentric terms.
+struct LeafShare {
+    float4* ray;              // [2 * 256]: (okx, oky, okz, tmin), (Sx, Sy, Sz, kx | ky << 2 | kz << 4)
+    unsigned long long* key;  // [256] closest: best (t, id); any hit: tmax bits
+    uint32_t* rec;            // [256] closest: record of the best; any hit: mask of the triangles hit
+    float4* vwdt;             // [256] closest: V, W, det, t of the best
+};
+
+#define KZ_LEAF_SHARE(name)                       \
+    __shared__ float4 name##_ray[2 * 256];        \
+    __shared__ unsigned long long name##_key[256]; \
+    __shared__ uint32_t name##_rec[256];          \
+    __shared__ float4 name##_vwdt[256];           \
+    const LeafShare name { name##_ray, name##_key, name##_rec, name##_vwdt }
+
+#define KZ_LEAF_SHARE_ANY(name)                    \
+    __shared__ float4 name##_ray[2 * 256];         \
+    __shared__ unsigned long long name##_key[256]; \
+    __shared__ uint32_t name##_rec[256];           \
+    const LeafShare name { name##_ray, name##_key, name##_rec, nullptr }
+
+__device__ __forceinline__ void publish_ray(const LeafShare& sh, const TRay& r) {
+    const TriRay q = tri_ray(r);
+    sh.ray[2 * threadIdx.x] = make_float4(q.okx, q.oky, q.okz, q.tmin);
+    sh.ray[2 * threadIdx.x + 1] =
+        make_float4(q.Sx, q.Sy, q.Sz, __uint_as_float((uint32_t)q.kx | ((uint32_t)q.ky << 2) | ((uint32_t)q.kz << 4)));
+}
+
+__device__ __forceinline__ TriRay shared_ray(const LeafShare& sh, uint32_t slot) {
+    const float4 a = sh.ray[2 * slot], b = sh.ray[2 * slot + 1];
+    const uint32_t k = __float_as_uint(b.w);
+    TriRay q;
+    q.okx = a.x;
+    q.oky = a.y;
+    q.okz = a.z;
+    q.tmin = a.w;
+    q.Sx = b.x;
+    q.Sy = b.y;
+    q.Sz = b.z;
+    q.kx = (int)(k & 3u);
+    q.ky = (int)((k >> 2) & 3u);
+    q.kz = (int)((k >> 4) & 3u);
+    return q;
+}
+
+// (t, id) as one 64-bit key whose unsigned order is float order of t (-0 as
+// +0), then id.
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t prim) {
+    const uint32_t u = __float_as_uint(t == 0.f ? 0.f : t);
+    const uint32_t o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((unsigned long long)o << 32) | prim;
+}
+
+// Position of the (k+1)-th set bit of m (k < popc(m), m below bit 31).
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t s = 16; s; s >>= 1)
+        if ((uint32_t)__popc(m & ((1u << (pos + s)) - 1u)) <= k) pos += s;
+    return pos;
+}
+
+// Assignment of pair p (0 <= p < total) of a warp whose lanes hold cnt pairs
+// each (inclusive prefix incl): the owner lane and the owner's bit. Every
+// lane must call it (full-warp shuffles).
+struct LeafPair {
+    uint32_t owner, bit, rec;
+};
+__device__ __forceinline__ LeafPair leaf_pair(uint32_t p, uint32_t incl, uint32_t cnt, uint32_t tbits, uint32_t tbase) {
+    uint32_t o = 0;
+#pragma unroll
+    for (uint32_t s = 16; s; s >>= 1) {
+        const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, o + s - 1);
+        if (v <= p) o += s;
+    }
+    const uint32_t o_incl = __shfl_sync(0xFFFFFFFFu, incl, o);
+    const uint32_t o_cnt = __shfl_sync(0xFFFFFFFFu, cnt, o);
+    const uint32_t o_bits = __shfl_sync(0xFFFFFFFFu, tbits, o);
+    const uint32_t o_base = __shfl_sync(0xFFFFFFFFu, tbase, o);
+    LeafPair lp;
+    lp.owner = o;
+    lp.bit = nth_set_bit(o_bits, p - (o_incl - o_cnt));
+    lp.rec = o_base + lp.bit;
+    return lp;
+}
+
+// Lane's pair count and its inclusive prefix over the warp; returns the total.
+__device__ __forceinline__ uint32_t leaf_scan(uint32_t tbits, uint32_t& cnt, uint32_t& incl) {
+    const uint32_t lane = threadIdx.x & 31u;
+    cnt = __popc(tbits);
+    incl = cnt;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    return __shfl_sync(0xFFFFFFFFu, incl, 31);
+}
+
+// Node part of a closest-hit step: visits one node; its leaf triangles are
+// returned in tbits (relative to tbase) for the warp-wide test. Returns -1 on
+// an abort (as closest_step), else 0.
+template <bool kCount, typename Stack>
+__device__ __forceinline__ int closest_node(const DevScene& s, const TRay& r, uint32_t octp, ClosestState& c,
+                                            const Stack& stack, uint32_t& tbits, uint32_t& tbase, uint32_t& nnode,
+                                            uint32_t& ntri) {
+    const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
+    if (c.gbits > 0x00FFFFFFu) {
+        if (c.sp >= kWideStack) return -1;
+        stack.put(c.sp++, make_uint2(c.gbase, c.gbits));
+    }
+    if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
+    uint32_t imask;
+    const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, c.t, c.gbase, tbase, imask);
+    if (kCount) ++nnode;
+    c.gbits = (hm & 0xFF000000u) | imask;
+    const uint32_t tb = hm & 0x00FFFFFFu;
+    if (tb && (uint64_t)tbase + (31u - __clz(tb)) >= s.n_tris) return -1;
+    if (kCount) ntri += __popc(tb);
+    tbits = tb;
+    return 0;
+}
+
+// Next node group from the stack: 1 when the traversal is complete, else 0.
+template <typename State, typename Stack>
+__device__ __forceinline__ int group_pop(State& c, const Stack& stack) {
+    while (c.gbits <= 0x00FFFFFFu && c.sp > 0) {
+        const uint2 e = stack.get(--c.sp);
+        c.gbase = e.x;
+        c.gbits = e.y;
+    }
+    return c.gbits <= 0x00FFFFFFu ? 1 : 0;
+}
+
+// Warp-wide closest-hit leaf tests; every lane of the warp calls it, lanes
+// without pending triangles with tbits = 0. `tris` is the calling lane's
+// triangle array: with kOwnScene each owner's array is fetched from its lane
+// (batched jobs trace different scenes in one warp).
+template <bool kOwnScene>
+__device__ __forceinline__ void closest_leaves(const LeafShare& sh, const float4* tris, uint32_t tbits, uint32_t tbase,
+                                               ClosestState& c) {
+    if (__ballot_sync(0xFFFFFFFFu, tbits != 0) == 0) return;
+    const uint32_t lane = threadIdx.x & 31u, wbase = threadIdx.x - lane;
+    uint32_t cnt, incl;
+    const uint32_t total = leaf_scan(tbits, cnt, incl);
+    unsigned long long init = 0;
+    if (tbits) {
+        init = hit_key(c.t, c.prim);
+        sh.key[threadIdx.x] = init;
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t p = base + lane;
+        const LeafPair lp = leaf_pair(p, incl, cnt, tbits, tbase);
+        const float4* tp = tris;
+        if (kOwnScene) {
+            const uint64_t tv = reinterpret_cast<uint64_t>(tris);
+            const uint32_t lo = __shfl_sync(0xFFFFFFFFu, (uint32_t)tv, lp.owner);
+            const uint32_t hi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(tv >> 32), lp.owner);
+            tp = reinterpret_cast<const float4*>(((uint64_t)hi << 32) | lo);
+        }
+        const uint32_t slot = wbase + lp.owner;
+        bool cand = false;
+        unsigned long long key = 0;
+        float t = 0.f, V = 0.f, W = 0.f, det = 0.f;
+        if (p < total) {
+            const TriRay q = shared_ray(sh, slot);
+            const float4* tr = tp + (size_t)lp.rec * 3;
+            const float4 a = __ldg(tr), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+            if (tri_test_t(q, a, b, cc, t, V, W, det) && t > q.tmin) {
+                key = hit_key(t, __float_as_uint(a.w));
+                atomicMin(sh.key + slot, key);
+                cand = true;
+            }
+        }
+        __syncwarp();
+        if (cand && sh.key[slot] == key) {
+            sh.rec[slot] = lp.rec;
+            sh.vwdt[slot] = make_float4(V, W, det, t);
+        }
+        __syncwarp();
+    }
+    if (tbits) {
+        const unsigned long long k = sh.key[threadIdx.x];
+        if (k != init) {
+            const float4 w = sh.vwdt[threadIdx.x];
+            const uint32_t prim = (uint32_t)k;
+            if (w.w < c.t || (w.w == c.t && prim < c.prim)) {
+                c.t = w.w;
+                c.V = w.x;
+                c.W = w.y;
+                c.det = w.z;
+                c.prim = prim;
+                c.rec = (int32_t)sh.rec[threadIdx.x];
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// Node part of an any-hit step (as closest_node, culling against tmax).
+template <bool kCount, typename Stack>
+__device__ __forceinline__ int any_node(const DevScene& s, const TRay& r, uint32_t octp, float tmax, AnyState& c,
+                                        const Stack& stack, uint32_t& tbits, uint32_t& tbase, uint32_t& nnode,
+                                        uint32_t& ntri) {
+    const uint32_t node = wide_pop_child(c.gbase, c.gbits, octp);
+    if (c.gbits > 0x00FFFFFFu) {
+        if (c.sp >= kWideStack) return -1;
+        stack.put(c.sp++, make_uint2(c.gbase, c.gbits));
+    }
+    if (++c.visits > s.n_nodes || node >= s.n_nodes) return -1;
+    uint32_t imask;
+    const uint32_t hm = wide_node(s.nodes + (size_t)node * 5, r, octp, tmax, c.gbase, tbase, imask);
+    if (kCount) ++nnode;
+    c.gbits = (hm & 0xFF000000u) | imask;
+    const uint32_t tb = hm & 0x00FFFFFFu;
+    if (tb && (uint64_t)tbase + (31u - __clz(tb)) >= s.n_tris) return -1;
+    tbits = tb;
+    return 0;
+}
+
+// Triangles a sequential any-hit loop over tbits (lowest bit first) tests
+// before it stops at the first hit of `hits`.
+__device__ __forceinline__ uint32_t any_tested(uint32_t tbits, uint32_t hits) {
+    return hits ? __popc(tbits & (((hits & (0u - hits)) << 1) - 1u)) : __popc(tbits);
+}
+
+// Warp-wide any-hit leaf tests: the mask of the lane's pending triangles
+// (bits of tbits) with a hit in (tmin, tmax]. The lane's tmax is in key[] as
+// float bits (publish_tmax).
+__device__ __forceinline__ void publish_tmax(const LeafShare& sh, float tmax) {
+    sh.key[threadIdx.x] = __float_as_uint(tmax);
+}
+template <bool kOwnScene>
+__device__ __forceinline__ uint32_t any_leaves(const LeafShare& sh, const float4* tris, uint32_t tbits,
+                                               uint32_t tbase) {
+    if (__ballot_sync(0xFFFFFFFFu, tbits != 0) == 0) return 0u;
+    const uint32_t lane = threadIdx.x & 31u, wbase = threadIdx.x - lane;
+    uint32_t cnt, incl;
+    const uint32_t total = leaf_scan(tbits, cnt, incl);
+    if (tbits) sh.rec[threadIdx.x] = 0u;
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t p = base + lane;
+        const LeafPair lp = leaf_pair(p, incl, cnt, tbits, tbase);
+        const float4* tp = tris;
+        if (kOwnScene) {
+            const uint64_t tv = reinterpret_cast<uint64_t>(tris);
+            const uint32_t lo = __shfl_sync(0xFFFFFFFFu, (uint32_t)tv, lp.owner);
+            const uint32_t hi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(tv >> 32), lp.owner);
+            tp = reinterpret_cast<const float4*>(((uint64_t)hi << 32) | lo);
+        }
+        const uint32_t slot = wbase + lp.owner;
+        if (p < total) {
+            const TriRay q = shared_ray(sh, slot);
+            const float tmax = __uint_as_float((uint32_t)sh.key[slot]);
+            const float4* tr = tp + (size_t)lp.rec * 3;
+            float t, V, W, det;
+            if (tri_test_t(q, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t, V, W, det) && t > q.tmin && t <= tmax)
+                atomicOr(sh.rec + slot, 1u << lp.bit);
+        }
+    }
+    __syncwarp();
+    const uint32_t hits = tbits ? sh.rec[threadIdx.x] : 0u;
+    __syncwarp();
+    return hits;
+}
+
 // Persistent ray loop: each warp keeps its lanes busy by fetching new rays
 // (one atomic per warp) whenever at least `refill` of its lanes are idle,
 // instead of running until its slowest ray ends. Warp-synchronous: one ballot
@@ -462,6 +771,40 @@ __device__ __forceinline__ void persistent_rays(Ctr n, Ctr* next, uint32_t refil
             }
         }
         if (busy && step()) busy = false;
+    }
+}
+
+// persistent_rays with the warp-wide leaf part: node(tbits, tbase) runs on
+// the busy lanes and returns -1 on an abort, else 0; leaves(tbits, tbase)
+// runs on all 32 lanes; finish(rc) on the busy lanes returns true once the
+// ray is finished and its result written.
+template <typename Ctr, typename Start, typename Node, typename Leaves, typename Finish>
+__device__ __forceinline__ void persistent_rays_shared(Ctr n, Ctr* next, uint32_t refill, Start start, Node node,
+                                                       Leaves leaves, Finish finish) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool busy = false, more = true;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
+        if (!more && idle == 0xFFFFFFFFu) break;
+        const uint32_t n_idle = __popc(idle);
+        if (more && n_idle >= refill) {
+            Ctr base = 0;
+            if (lane == 0) base = atomicAdd(next, (Ctr)n_idle);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + n_idle >= n) more = false;
+            if (!busy) {
+                const Ctr k = base + __popc(idle & ((1u << lane) - 1u));
+                if (k < n) {
+                    busy = true;
+                    start(k);
+                }
+            }
+        }
+        uint32_t tbits = 0, tbase = 0;
+        int rc = 0;
+        if (busy) rc = node(tbits, tbase);
+        leaves(tbits, tbase);
+        if (busy && finish(rc)) busy = false;
     }
 }
 
