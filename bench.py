@@ -4,7 +4,7 @@ Headline workload (one step = one full frame): the plain wavefront path
 tracer on the procedural terrain scene — 1024 x 1024-cell fBm heightfield
 (2,097,152 triangles) + 64 icospheres (1,280 triangles each), Lambert / GGX
 conductor / smooth dielectric materials, 4 quad lights, 1920 x 1080, 64 spp,
-max depth 8, 2M-path wavefront, FP32. Metric: Mpaths*bounces/s (closest-hit
+max depth 8, 8M-path wavefront, FP32. Metric: Mpaths*bounces/s (closest-hit
 extension rays traced, camera rays included, per second).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -46,8 +46,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--small", action="store_true", help="reduced workload (quick checks only)")
     p.add_argument("--profile", action="store_true",
-                   help="full-size scene, 640x360 frame at 16 spp (3.7 M paths: full 2^21-path wavefronts), for ncu "
+                   help="full-size scene, 640x360 frame at 64 spp (14.7 M paths: full 2^23-path wavefronts), for ncu "
                         "captures of single launches")
+    p.add_argument("--wavefront-log2", type=int, default=None,
+                   help="paths in flight as a power of two (default 23 for the frame workloads)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-traversal", action="store_true")
     p.add_argument("--no-guiding", action="store_true")
@@ -64,11 +66,18 @@ def parse():
 
 
 def workload(args):
+    w = _workload(args)
+    if getattr(args, "wavefront_log2", None):
+        w["wavefront"] = 1 << args.wavefront_log2
+    return w
+
+
+def _workload(args):
     if args.small:
         return dict(width=320, height=180, spp=8, max_depth=8, cells=256, n_spheres=64, wavefront=1 << 18)
     if getattr(args, "profile", False):
-        return dict(width=640, height=360, spp=16, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
-    return dict(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 21)
+        return dict(width=640, height=360, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 23)
+    return dict(width=1920, height=1080, spp=64, max_depth=8, cells=1024, n_spheres=64, wavefront=1 << 23)
 
 
 def config_dict(w, extra=None):
@@ -551,6 +560,14 @@ def batch_bench(n_jobs=256):
     t0 = time.perf_counter()
     _, mst = api.render_batch(jobs, mcfg)
     wall_m = time.perf_counter() - t0
+    # the whole wavefront loop in one cooperative launch, at its best tuned shape
+    pers = [t for t in table if t[0].get("mode") == api.BATCH_PERSISTENT]
+    best_pers = min(pers, key=lambda t: t[1])[0] if pers else {"mode": api.BATCH_PERSISTENT}
+    t0 = time.perf_counter()
+    pimgs, pst = api.render_batch(jobs, autotune.config_of(best_pers, use_graph=True))
+    wall_p = time.perf_counter() - t0
+    perr = max(float(np.abs(a - b).max() / max(1e-6, float(np.abs(b).max()))) for a, b in zip(pimgs, imgs))
+    del pimgs
     for j in jobs:
         j["scene"].close()
     mb = st["path_bounces"] / (st["device_ms"] / 1e3) / 1e6
@@ -559,13 +576,19 @@ def batch_bench(n_jobs=256):
             "autotuned": best, "autotune_candidates": len(table), "persistent_lanes": st["threads"],
             "autotune_sample_ms_best_per_mode": {
                 "wavefront": min((ms for c, ms in table if c.get("mode") == api.BATCH_WAVEFRONT), default=None),
-                "megakernel": min((ms for c, ms in table if c.get("mode") == api.BATCH_MEGAKERNEL), default=None)},
+                "megakernel": min((ms for c, ms in table if c.get("mode") == api.BATCH_MEGAKERNEL), default=None),
+                "persistent": min((ms for c, ms in table if c.get("mode") == api.BATCH_PERSISTENT), default=None)},
             "autotune_wavefront_by_refill_period": {
                 str(p): min((ms for c, ms in table if c.get("mode") == api.BATCH_WAVEFRONT
                              and c.get("refill_period") == p), default=None) for p in autotune.WAVE_PERIODS},
             "megakernel_tuned": best_mega,
             "batched_graph": {"device_ms": round(st["device_ms"], 2), "wall_s": round(wall_b, 3),
                               "mpaths_bounces_per_s": round(mb, 1)},
+            "persistent_tuned": best_pers,
+            "persistent_one_launch_graph": {
+                "device_ms": round(pst["device_ms"], 2), "wall_s": round(wall_p, 3),
+                "mpaths_bounces_per_s": round(pst["path_bounces"] / (pst["device_ms"] / 1e3) / 1e6, 1),
+                "max_rel_difference_vs_batched": perr},
             "megakernel_graph": {"device_ms": round(mst["device_ms"], 2), "wall_s": round(wall_m, 3),
                                  "mpaths_bounces_per_s": round(mst["path_bounces"] / (mst["device_ms"] / 1e3) / 1e6,
                                                                1)},

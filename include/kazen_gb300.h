@@ -168,7 +168,12 @@ typedef struct kz_film_desc {
     uint32_t height;
 } kz_film_desc;
 
-#define KZ_RENDER_DEFAULT_WAVEFRONT (1u << 21)
+/* Paths in flight by default: 2^23 (path state ~1.6 GB). On the 1080p,
+ * 64-spp terrain frame 2^21 / 2^22 / 2^23 / 2^24 gave 1,532 / 1,622 / 1,666 /
+ * 1,681 Mpaths*bounces/s (end to end 1,509 / 1,618 / 1,662 / 1,651): longer
+ * launches amortise each persistent kernel's tail and the per-iteration
+ * launches. A render never holds more than its own path count. */
+#define KZ_RENDER_DEFAULT_WAVEFRONT (1u << 23)
 
 typedef struct kz_render_config {
     uint32_t spp;            /* samples per pixel                              */
@@ -412,10 +417,16 @@ kz_status kz_render_guided(kz_scene* scene, kz_guide* guide, const kz_camera* ca
  *    graph launch (one host synchronisation per batch).
  *  KZ_BATCH_MEGAKERNEL: one persistent kernel; lanes keep a path each and
  *    refill from a global path counter every refill_period vertices.
+ *  KZ_BATCH_PERSISTENT: the wavefront's whole loop (every stage of every
+ *    iteration) in one cooperative kernel launch, its stages separated by
+ *    grid-wide barriers (bounded waits: KZ_ERR_TIMEOUT); wavefront_size and
+ *    refill_period as in KZ_BATCH_WAVEFRONT, block_size fixed at 256. With
+ *    use_graph the launch is replayed from a captured graph.
  * All scenes must be built on the same device; the call runs on the first
  * job's scene stream. */
 #define KZ_BATCH_WAVEFRONT  0
 #define KZ_BATCH_MEGAKERNEL 1
+#define KZ_BATCH_PERSISTENT 2
 typedef struct kz_batch_job {
     kz_scene* scene;
     kz_camera camera;
@@ -433,8 +444,8 @@ typedef struct kz_batch_config {
                                    wavefront: iterations between generations
                                    of new paths into free slots (0 = 1)      */
     uint32_t use_graph;         /* 1: launch through a captured CUDA graph   */
-    uint32_t mode;              /* KZ_BATCH_WAVEFRONT or KZ_BATCH_MEGAKERNEL */
-    uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^21)     */
+    uint32_t mode;              /* KZ_BATCH_WAVEFRONT, _MEGAKERNEL or _PERSISTENT */
+    uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^23)     */
 } kz_batch_config;
 
 typedef struct kz_batch_stats {

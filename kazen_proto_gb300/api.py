@@ -604,6 +604,7 @@ def render_guided(scene: Scene, guide: Guide, camera: Camera, width: int, height
 # ---------------------------------------------------------------- batched rendering
 BATCH_WAVEFRONT = 0
 BATCH_MEGAKERNEL = 1
+BATCH_PERSISTENT = 2
 
 
 def batch_config(block_size=0, ctas_per_sm=0, refill_period=0, use_graph=True, mode=BATCH_WAVEFRONT,
@@ -620,8 +621,10 @@ def batch_config(block_size=0, ctas_per_sm=0, refill_period=0, use_graph=True, m
 
 def render_batch(jobs, cfg=None):
     """jobs: list of dicts {scene, camera, width, height, spp, max_depth, seed[, rr_min_depth]}.
-    Returns (list of (H, W, 3) images, stats). All jobs in one wavefront (or one
-    persistent megakernel launch, cfg.mode = BATCH_MEGAKERNEL)."""
+    Returns (list of (H, W, 3) images, stats). All jobs in one wavefront: stage
+    kernels per iteration (BATCH_WAVEFRONT) or the whole loop in one cooperative
+    launch (BATCH_PERSISTENT); or one persistent megakernel launch
+    (BATCH_MEGAKERNEL)."""
     arr = (N.KzBatchJob * len(jobs))()
     outs = []
     for k, j in enumerate(jobs):

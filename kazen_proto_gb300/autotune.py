@@ -1,9 +1,10 @@
 """Autotuner of the batch renderer (kz_render_batch).
 
 Sweeps, on a sample of the jobs, the wavefront mode's paths in flight, block
-size and refill period (iterations between generations of new paths), and
-the megakernel mode's block size, resident blocks per SM and lane refill
-period; keeps the fastest by CUDA-event time and stores it in
+size and refill period (iterations between generations of new paths), the
+single-launch persistent mode's paths in flight and refill period, and the
+megakernel mode's block size, resident blocks per SM and lane refill period;
+keeps the fastest by CUDA-event time and stores it in
 kazen_proto_gb300/_build/autotune.json for later calls on the same machine.
 """
 from __future__ import annotations
@@ -16,7 +17,7 @@ from . import api
 HERE = os.path.dirname(os.path.abspath(__file__))
 PATH = os.path.join(HERE, "_build", "autotune.json")
 
-WAVEFRONT_SIZES = (1 << 19, 1 << 20, 1 << 21, 1 << 22)
+WAVEFRONT_SIZES = (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)
 WAVE_BLOCKS = (128, 256)
 BLOCKS = (64, 128, 256)
 CTAS_PER_SM = (1, 2, 4)
@@ -29,6 +30,8 @@ WAVE_PERIODS = (1, 2, 3)
 def candidates():
     out = [{"mode": api.BATCH_WAVEFRONT, "block_size": b, "wavefront_size": w, "refill_period": p}
            for w in WAVEFRONT_SIZES for b in WAVE_BLOCKS for p in WAVE_PERIODS]
+    out += [{"mode": api.BATCH_PERSISTENT, "wavefront_size": w, "refill_period": p}
+            for w in WAVEFRONT_SIZES for p in WAVE_PERIODS]
     out += [{"mode": api.BATCH_MEGAKERNEL, "block_size": b, "ctas_per_sm": c, "refill_period": p}
             for b in BLOCKS for c in CTAS_PER_SM for p in PERIODS]
     return out

@@ -1728,6 +1728,19 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
             std::swap(a, b);
         }
     };
+    const bool persistent = cfg.mode == KZ_BATCH_PERSISTENT;
+    uint32_t coop_blocks = 0;
+    if (persistent) {
+        int sms = 0;
+        KZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+        const int per_sm = kz::batch_persistent_blocks_per_sm(textured);
+        if (per_sm <= 0) return fail(KZ_ERR_CUDA, "the persistent batch kernel does not fit on an SM");
+        coop_blocks = (uint32_t)sms * (uint32_t)per_sm;
+    }
+    // the persistent mode's one launch runs the whole loop
+    auto enqueue_persistent = [&]() -> cudaError_t {
+        return kz::launch_batch_persistent(djobs, n_jobs, A, B, sq, ctr, cap, period, coop_blocks, textured, strm);
+    };
     kz::prepare_batch_wavefront();
     cudaGraphExec_t exec = nullptr;
     struct ExecGuard {
@@ -1739,8 +1752,14 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
     if (cfg.use_graph) {
         cudaGraph_t graph = nullptr;
         KZ_CUDA(cudaStreamBeginCapture(strm, cudaStreamCaptureModeThreadLocal));
-        enqueue();
+        cudaError_t le = cudaSuccess;
+        if (persistent) le = enqueue_persistent();
+        else enqueue();
         cudaError_t ce = cudaStreamEndCapture(strm, &graph);
+        if (le != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(KZ_ERR_CUDA, "persistent batch launch (capture): %s", cudaGetErrorString(le));
+        }
         if (ce != cudaSuccess) return fail(KZ_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
         ce = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
@@ -1762,6 +1781,7 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
     KZ_CUDA(cudaEventRecord(e0, strm));
     for (;;) {
         if (exec) KZ_CUDA(cudaGraphLaunch(exec, strm));
+        else if (persistent) KZ_CUDA(enqueue_persistent());
         else enqueue();
         KZ_CUDA(cudaGetLastError());
         KZ_CUDA(cudaMemcpyAsync(s->ctr_host, ctr, sizeof(kz::DevCounters), cudaMemcpyDeviceToHost, strm));
@@ -1769,6 +1789,7 @@ kz_status batch_wavefront(const kz_batch_job* jobs, uint32_t n_jobs, const kz_ba
         const kz::DevCounters& hc = *s->ctr_host;
         if (hc.status) return fail((kz_status)hc.status, "device status %u during batched rendering", hc.status);
         if (hc.n_active == 0 && hc.next_path >= hc.total) break;
+        if (persistent) return fail(KZ_ERR_CUDA, "persistent batch kernel ended with paths left");
     }
     for (uint32_t j = 0; j < n_jobs; ++j)
         kz::launch_scale(fptr[j], nullptr, npix[j] * 3, 1.0f / (float)jobs[j].spp, 0.0, strm);
@@ -1799,9 +1820,9 @@ extern "C" kz_status kz_render_batch(const kz_batch_job* jobs, uint32_t n_jobs, 
     if (n_jobs == 0) return KZ_OK;
     if (!jobs) return fail(KZ_ERR_INVALID_ARG, "jobs is NULL");
     kz_batch_config cfg = cfg_in ? *cfg_in : kz_batch_config{};
-    if (cfg.mode != KZ_BATCH_WAVEFRONT && cfg.mode != KZ_BATCH_MEGAKERNEL)
+    if (cfg.mode != KZ_BATCH_WAVEFRONT && cfg.mode != KZ_BATCH_MEGAKERNEL && cfg.mode != KZ_BATCH_PERSISTENT)
         return fail(KZ_ERR_INVALID_ARG, "unknown batch mode %u", cfg.mode);
-    const bool wavefront = cfg.mode == KZ_BATCH_WAVEFRONT;
+    const bool wavefront = cfg.mode != KZ_BATCH_MEGAKERNEL;  // the persistent mode runs the wavefront's stages
     if (cfg.block_size == 0) cfg.block_size = wavefront ? 256 : 128;
     if (cfg.ctas_per_sm == 0) cfg.ctas_per_sm = 2;
     if (cfg.refill_period == 0) cfg.refill_period = 1;

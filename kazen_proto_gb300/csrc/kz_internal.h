@@ -149,6 +149,8 @@ struct DevCounters {
     uint32_t gen_count, gen_slot;  // how many, and where in the buffer
     uint32_t trace_next;           // persistent kernels: next path / shadow ray to fetch
     uint32_t shadow_next;
+    uint32_t bar_count, bar_gen;   // grid barrier of the persistent batch kernel
+    uint32_t bar_abort;            // set when a barrier wait ran out
 };
 
 // One job of a batched render: its scene, camera and film.
@@ -267,6 +269,10 @@ void launch_trace_paths_batch(const DevJob* jobs, PathSoA p, uint32_t cap, DevCo
 void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,
                         uint32_t block, bool textured, cudaStream_t st);
 void launch_trace_shadow_batch(const DevJob* jobs, ShadowSoA sq, uint32_t cap, DevCounters* ctr, cudaStream_t st);
+int batch_persistent_blocks_per_sm(bool textured);
+cudaError_t launch_batch_persistent(const DevJob* jobs, uint32_t n_jobs, PathSoA A, PathSoA B, ShadowSoA sq,
+                                   DevCounters* ctr, uint32_t cap, uint32_t period, uint32_t blocks, bool textured,
+                                   cudaStream_t st);
 // Queries the persistent stages' grid sizes (call before a stream capture).
 void prepare_batch_wavefront();
 constexpr uint32_t kMaxBatchJobs = 1u << 20;  // job index in 20 bits of a path's flags

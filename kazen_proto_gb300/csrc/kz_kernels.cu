@@ -57,29 +57,9 @@ __global__ void k_guide_collect(const VRec* __restrict__ recs, const NRec* __res
 }
 
 // ------------------------------------------------------------------ device-driven loop
-__global__ void k_plan(DevCounters* c, uint32_t cap, bool generate) {
-    const uint64_t remaining = c->total - c->next_path;
-    const uint32_t room = cap - c->n_active;
-    const uint32_t n_new = generate ? (uint32_t)(remaining < room ? remaining : room) : 0u;
-    c->gen_first = c->next_path;
-    c->gen_count = n_new;
-    c->gen_slot = c->n_active;
-    c->next_path += n_new;
-    c->n_active += n_new;
-    c->n_next = 0;
-    c->n_shadow = 0;
-    c->trace_next = 0;
-    c->shadow_next = 0;
-    if (c->n_active) {
-        c->iterations += 1;
-        c->path_bounces += c->n_active;
-    }
-}
+__global__ void k_plan(DevCounters* c, uint32_t cap, bool generate) { plan_iteration(c, cap, generate); }
 
-__global__ void k_finish(DevCounters* c) {
-    c->shadow_rays += c->n_shadow;
-    c->n_active = c->n_next;
-}
+__global__ void k_finish(DevCounters* c) { finish_iteration(c); }
 
 __global__ void k_generate_camera_dev(DevCamera cam, PathParams pp, PathSoA dst, const DevCounters* c) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;

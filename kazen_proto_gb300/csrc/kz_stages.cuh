@@ -660,6 +660,85 @@ __device__ __forceinline__ void trace_fields(DevScene& dst, const DevScene& src)
     dst.n_tris = src.n_tris;
 }
 
+// ---- stages of the batched wavefront (jobs of several scenes in one
+// wavefront), as device functions shared by the per-stage kernels and the
+// single persistent kernel of KZ_BATCH_PERSISTENT.
+
+// Closest hits of the wavefront's paths; each path's scene through its job.
+__device__ __forceinline__ void batch_trace_paths(const DevJob* __restrict__ jobs, PathSoA p, DevCounters* ctr) {
+    uint32_t dn = 0, dt = 0;
+    DevScene ls;
+    persistent_closest<false, true>(
+        ls, ctr->n_active, &ctr->trace_next, &ctr->status,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = p.o4[k], d = p.d4[k];
+            trace_fields(ls, jobs[__float_as_uint(d.w) >> kJobShift].scene);
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = __int_as_float(0x7f800000);
+        },
+        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
+}
+
+// Shadow rays of the wavefront; an unoccluded one adds its contribution to
+// its job's film.
+__device__ __forceinline__ void batch_trace_shadow(const DevJob* __restrict__ jobs, ShadowSoA sq, DevCounters* ctr) {
+    uint32_t dn = 0, dt = 0;
+    DevScene ls;
+    persistent_any<false, true>(
+        ls, ctr->n_shadow, &ctr->shadow_next,
+        [&](uint32_t k, TRay& r, float& tmax) {
+            const float4 o = sq.o4[k], d = sq.d4[k];
+            trace_fields(ls, jobs[__float_as_uint(sq.c4[k].w)].scene);
+            r = make_tray(xyz(o), xyz(d), kRayEps);
+            tmax = o.w;
+        },
+        [&](uint32_t ray, int rc) {
+            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
+            if (rc == 1)
+                film_add(jobs[__float_as_uint(sq.c4[ray].w)].film, nullptr, __float_as_uint(sq.d4[ray].w),
+                         xyz(sq.c4[ray]));
+        },
+        dn, dt);
+}
+
+// Camera path j of this iteration's generation (j < gen_count).
+__device__ __forceinline__ void batch_generate(const DevJob* __restrict__ jobs, uint32_t n_jobs, PathSoA dst,
+                                               const DevCounters* c, uint32_t j) {
+    const unsigned long long g = c->gen_first + j;
+    const uint32_t job = find_job(jobs, n_jobs, g);
+    const DevJob& J = jobs[job];
+    const uint32_t k = c->gen_slot + j;
+    generate_camera_path(J.cam, J.pp, dst, k, g - J.path_begin);
+    dst.d4[k].w = __uint_as_float(__float_as_uint(dst.d4[k].w) | (job << kJobShift));
+}
+
+// Counters of one iteration of the device-driven loop: how many new paths
+// fill the free slots (when `generate`), and the per-iteration cursors reset.
+__device__ __forceinline__ void plan_iteration(DevCounters* c, uint32_t cap, bool generate) {
+    const uint64_t remaining = c->total - c->next_path;
+    const uint32_t room = cap - c->n_active;
+    const uint32_t n_new = generate ? (uint32_t)(remaining < room ? remaining : room) : 0u;
+    c->gen_first = c->next_path;
+    c->gen_count = n_new;
+    c->gen_slot = c->n_active;
+    c->next_path += n_new;
+    c->n_active += n_new;
+    c->n_next = 0;
+    c->n_shadow = 0;
+    c->trace_next = 0;
+    c->shadow_next = 0;
+    if (c->n_active) {
+        c->iterations += 1;
+        c->path_bounces += c->n_active;
+    }
+}
+
+// End of an iteration: the continuing paths become the next wavefront.
+__device__ __forceinline__ void finish_iteration(DevCounters* c) {
+    c->shadow_rays += c->n_shadow;
+    c->n_active = c->n_next;
+}
+
 inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
 // Blocks of `block` threads resident on the whole device for kernel f.

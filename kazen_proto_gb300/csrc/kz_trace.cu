@@ -187,67 +187,13 @@ __global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_persistent(
 // over the pdf the direction was sampled with.
 
 __global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
-                                                           DevCounters* ctr) {
-    uint32_t dn = 0, dt = 0;
-    DevScene ls;
-    persistent_closest<false, true>(
-        ls, ctr->n_active, &ctr->trace_next, &ctr->status,
-        [&](uint32_t k, TRay& r, float& tmax) {
-            const float4 o = p.o4[k], d = p.d4[k];
-            trace_fields(ls, jobs[__float_as_uint(d.w) >> kJobShift].scene);
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = __int_as_float(0x7f800000);
-        },
-        [&](uint32_t k, const HitRec& h) { p.hit[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec)); }, dn, dt);
+                                                                          DevCounters* ctr) {
+    batch_trace_paths(jobs, p, ctr);
 }
 
-__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_batch(const DevJob* __restrict__ jobs, ShadowSoA sq,
-                                                            DevCounters* ctr) {
-    uint32_t dn = 0, dt = 0;
-    DevScene ls;
-#if KZ_SHARE_LEAVES
-    persistent_any<false, true>(
-        ls, ctr->n_shadow, &ctr->shadow_next,
-        [&](uint32_t k, TRay& r, float& tmax) {
-            const float4 o = sq.o4[k], d = sq.d4[k];
-            trace_fields(ls, jobs[__float_as_uint(sq.c4[k].w)].scene);
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = o.w;
-        },
-        [&](uint32_t ray, int rc) {
-            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
-            if (rc == 1)
-                film_add(jobs[__float_as_uint(sq.c4[ray].w)].film, nullptr, __float_as_uint(sq.d4[ray].w),
-                         xyz(sq.c4[ray]));
-        },
-        dn, dt);
-#else
-    uint2 stack_lm[kWideStack];
-    const LocalStack stack{stack_lm};
-    AnyState c;
-    TRay r;
-    float tmax = 0.f;
-    uint32_t octp = 0, ray = 0, job = 0;
-    persistent_rays(
-        ctr->n_shadow, &ctr->shadow_next, kTraceRefill,
-        [&](uint32_t k) {
-            ray = k;
-            const float4 o = sq.o4[k], d = sq.d4[k];
-            job = __float_as_uint(sq.c4[k].w);
-            trace_fields(ls, jobs[job].scene);
-            r = make_tray(xyz(o), xyz(d), kRayEps);
-            tmax = o.w;
-            octp = wide_octant(r);
-            any_begin(c);
-        },
-        [&]() {
-            const int rc = any_step<false>(ls, r, octp, tmax, c, stack, dn, dt);
-            if (rc == 0) return false;
-            if (rc < 0) set_status(&ctr->status, KZ_ERR_STACK);
-            if (rc == 1) film_add(jobs[job].film, nullptr, __float_as_uint(sq.d4[ray].w), xyz(sq.c4[ray]));
-            return true;
-        });
-#endif
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_batch(const DevJob* __restrict__ jobs,
+                                                                           ShadowSoA sq, DevCounters* ctr) {
+    batch_trace_shadow(jobs, sq, ctr);
 }
 
 }  // namespace

@@ -1,5 +1,6 @@
-"""Batched rendering: many uneven jobs in one wavefront (or one persistent
-megakernel launch), optionally through CUDA graphs, must give each job the
+"""Batched rendering: many uneven jobs in one wavefront (stage kernels per
+iteration, or the whole loop in one cooperative launch) or one persistent
+megakernel launch, optionally through CUDA graphs, must give each job the
 same film as rendering it alone."""
 import numpy as np
 import pytest
@@ -30,6 +31,7 @@ def singles(jobs):
 
 MEGA = api.BATCH_MEGAKERNEL
 WAVE = api.BATCH_WAVEFRONT
+PERS = api.BATCH_PERSISTENT
 
 
 @pytest.mark.parametrize("cfg", [dict(mode=WAVE, use_graph=True),
@@ -40,7 +42,10 @@ WAVE = api.BATCH_WAVEFRONT
                                       use_graph=False),
                                  dict(mode=MEGA, block_size=128, ctas_per_sm=2, refill_period=1, use_graph=True),
                                  dict(mode=MEGA, block_size=64, ctas_per_sm=1, refill_period=4, use_graph=False),
-                                 dict(mode=MEGA, block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True)])
+                                 dict(mode=MEGA, block_size=256, ctas_per_sm=4, refill_period=2, use_graph=True),
+                                 dict(mode=PERS, use_graph=True),
+                                 dict(mode=PERS, wavefront_size=1000, use_graph=False),
+                                 dict(mode=PERS, wavefront_size=3000, refill_period=3, use_graph=True)])
 def test_batch_matches_single_renders(gpu, jobs, cfg):
     imgs, st = api.render_batch(jobs, api.batch_config(**cfg))
     ref = singles(jobs)
