@@ -482,7 +482,12 @@ __device__ __forceinline__ void shade_vertex(const DevScene& s, const PathParams
                     f = f + hmul(lobe_weight(lb, textured, tint), e.f);
                     bpdf += lp[k] * e.pdf;
                 }
-                if (kGuided && guided) bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
+                // the MIS partner of this light sample is the next direction,
+                // sampled from the guide mixture; at the last vertex no
+                // direction follows, so the weight is the plain one and the
+                // guided image converges to the plain image at every depth
+                if (kGuided && guided && depth + 1 < pp.max_depth)
+                    bpdf = alpha * mixture_pdf_shading(mix, ldir) + (1.f - alpha) * bpdf;
                 if (!is_zero(f)) {
                     const float w = point || pp.estimator == 1u ? 1.f : power_heuristic(lpdf, bpdf);
                     // PointLight::sample's falloff: radiance / (0.1 |d|^2)

@@ -182,6 +182,22 @@ def test_guided_render_is_unbiased(gpu, slit):
         assert_unbiased(biased, ref, ref_var, "planted bias")
 
 
+def test_guided_render_is_unbiased_at_depth_2(gpu, slit):
+    """Depth 2 (direct light and one bounce), where half of the shaded
+    vertices are the last one: the light sample there has no sampled
+    direction after it as its MIS partner, so it must weigh like the plain
+    tracer's, or the guided image converges to another value than plain."""
+    d, s, _, _ = slit
+    parts = np.stack([api.Renderer(spp=1024, max_depth=2, seed=300 + k).render(s, d.camera, R, R, fp64=True)[1]
+                      for k in range(16)])
+    ref, ref_var = parts.mean(0), parts.var(0, ddof=1) / len(parts)
+    g = api.Guide(seed=12)
+    api.render_guided(s, g, d.camera, R, R, spp=512, max_depth=2, seed=7, gcfg=api.guide_config(spp_per_pass=8))
+    frozen = [api.render_guided(s, g, d.camera, R, R, spp=512, max_depth=2, seed=400 + k,
+                                gcfg=api.guide_config(train=False, spp_per_pass=64))[0] for k in range(8)]
+    assert_unbiased(frozen, ref, ref_var, "trained, depth 2")
+
+
 def test_trained_guide_reduces_error(gpu, slit):
     """What the trained network gains: after training, at equal spp, guided
     rendering of the narrow-aperture scene has lower relMSE than plain."""
