@@ -1029,15 +1029,19 @@ kz_status kz_intersect_any(kz_scene* s, const kz_ray* rays, uint64_t n, uint8_t*
         else std::memset(occluded, 0, n);
         return KZ_OK;
     }
+    KZ_TRY(s->s_next.ensure(sizeof(unsigned long long)));
+    KZ_CUDA(cudaMemsetAsync(s->s_next.ptr, 0, sizeof(unsigned long long), st));
     if (mem == KZ_MEM_DEVICE) {
-        kz::launch_intersect_any(s->dev, rays, n, occluded, s->status.as<uint32_t>(), st);
+        kz::launch_intersect_any(s->dev, rays, n, occluded, s->s_next.as<unsigned long long>(),
+                                 s->status.as<uint32_t>(), st);
         KZ_CUDA(cudaGetLastError());
         return KZ_OK;
     }
     KZ_TRY(s->s_rays.ensure(n * sizeof(kz_ray)));
     KZ_TRY(s->s_occ.ensure(n));
     KZ_CUDA(cudaMemcpyAsync(s->s_rays.ptr, rays, n * sizeof(kz_ray), cudaMemcpyHostToDevice, st));
-    kz::launch_intersect_any(s->dev, s->s_rays.as<kz_ray>(), n, s->s_occ.as<uint8_t>(), s->status.as<uint32_t>(), st);
+    kz::launch_intersect_any(s->dev, s->s_rays.as<kz_ray>(), n, s->s_occ.as<uint8_t>(),
+                             s->s_next.as<unsigned long long>(), s->status.as<uint32_t>(), st);
     KZ_CUDA(cudaGetLastError());
     KZ_CUDA(cudaMemcpyAsync(occluded, s->s_occ.ptr, n, cudaMemcpyDeviceToHost, st));
     return sync_and_status(s);

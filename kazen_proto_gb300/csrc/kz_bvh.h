@@ -67,14 +67,20 @@ struct WideBvhOutput {
 
 // Collapse of the binary build into wide nodes: SAH-optimal slot assignment
 // (default) or greedy (open the largest-area child until 8 slots). Costs are
-// relative SAH weights of a wide-node visit and of one triangle test; on
-// GB300 a triangle test (a divergent loop) weighs about twice a node visit
-// (eight slot tests in lockstep): measured on the terrain workload, trace time
-// falls 10 % from tri_cost 0.3 to 2 and is flat above.
+// relative SAH weights of a wide-node visit and of one triangle test
+// (KZ_BVH_TRI_COST).
+// Relative cost of one triangle test against a wide-node visit in the SAH
+// collapse. With the leaf tests shared by the warp (32 pairs per round), a
+// triangle is cheap next to an eight-slot node test: on the terrain frame
+// (1080p, 64 spp) the frame rate for 2.0 / 1.0 / 0.5 / 0.35 / 0.25 / 0.15
+// was 1,665 / 1,690 / 1,732 / 1,744 / 1,747 / 1,743 Mpaths*bounces/s.
+#ifndef KZ_BVH_TRI_COST
+#define KZ_BVH_TRI_COST 0.25f
+#endif
 struct WideBuildOptions {
     bool sah_collapse = true;
     float node_cost = 1.0f;
-    float tri_cost = 2.0f;
+    float tri_cost = KZ_BVH_TRI_COST;
     int binary_max_leaf = 1;  // leaf size of the binary build the SAH collapse regroups (<= 3)
 };
 

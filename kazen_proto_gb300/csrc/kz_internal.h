@@ -173,7 +173,7 @@ struct BatchCounters {
 void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n, kz_hits hits,
                               unsigned long long* next, uint32_t* status, cudaStream_t st);
 void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ,
-                          uint32_t* status, cudaStream_t st);
+                          unsigned long long* next, uint32_t* status, cudaStream_t st);
 void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n,
                             unsigned long long* counters /*2*/, uint32_t* status, cudaStream_t st);
 void launch_closure_eval(const kz_lobe* lobes, const float* wi, const float* wo, uint64_t n,

@@ -13,18 +13,26 @@
 namespace kz {
 namespace {
 
-__global__ void k_intersect_any(DevScene s, const kz_ray* __restrict__ rays, uint64_t n, uint8_t* occ,
-                                uint32_t* status) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    const float4 a = __ldg(rp), b = __ldg(rp + 1);
-    TRay r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
-    bool overflow;
+// kz_intersect_any: rays (o, tmin, d, tmax) in, an occlusion byte out.
+__global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_intersect_any_persistent(DevScene s,
+                                                                                 const kz_ray* __restrict__ rays,
+                                                                                 unsigned long long n, uint8_t* occ,
+                                                                                 unsigned long long* next,
+                                                                                 uint32_t* status) {
     uint32_t dn = 0, dt = 0;
-    bool hit = trace_any<false>(s, r, b.w, overflow, dn, dt);
-    if (overflow) set_status(status, KZ_ERR_STACK);
-    occ[i] = hit ? 1 : 0;
+    persistent_any<false>(
+        s, n, next,
+        [&](unsigned long long k, TRay& r, float& tmax) {
+            const float4* rp = reinterpret_cast<const float4*>(rays + k);
+            const float4 a = __ldg(rp), b = __ldg(rp + 1);
+            r = make_tray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w);
+            tmax = b.w;
+        },
+        [&](unsigned long long k, int rc) {
+            if (rc < 0) set_status(status, KZ_ERR_STACK);
+            occ[k] = rc == 2 ? 1 : 0;
+        },
+        dn, dt);
 }
 
 __global__ void k_intersect_stats(DevScene s, const kz_ray* __restrict__ rays, uint64_t n,
@@ -206,10 +214,12 @@ void launch_intersect_closest(const DevScene& s, const kz_ray* rays, uint64_t n,
                                                                                                      next, status);
 }
 
-void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ, uint32_t* status,
-                          cudaStream_t st) {
+void launch_intersect_any(const DevScene& s, const kz_ray* rays, uint64_t n, uint8_t* occ,
+                          unsigned long long* next, uint32_t* status, cudaStream_t st) {
     if (!n) return;
-    k_intersect_any<<<grid_for(n, 128), 128, 0, st>>>(s, rays, n, occ, status);
+    static const unsigned g = resident_grid(k_intersect_any_persistent, 256);
+    k_intersect_any_persistent<<<(unsigned)std::min<uint64_t>(g, grid_for(n, 256)), 256, 0, st>>>(s, rays, n, occ,
+                                                                                                 next, status);
 }
 
 void launch_intersect_stats(const DevScene& s, const kz_ray* rays, uint64_t n, unsigned long long* counters,
