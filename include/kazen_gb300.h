@@ -168,12 +168,13 @@ typedef struct kz_film_desc {
     uint32_t height;
 } kz_film_desc;
 
-/* Paths in flight by default: 2^23 (path state ~1.6 GB). On the 1080p,
+/* Paths in flight by default: 2^24 (path state ~3.2 GB). On the 1080p,
  * 64-spp terrain frame 2^21 / 2^22 / 2^23 / 2^24 gave 1,532 / 1,622 / 1,666 /
- * 1,681 Mpaths*bounces/s (end to end 1,509 / 1,618 / 1,662 / 1,651): longer
- * launches amortise each persistent kernel's tail and the per-iteration
- * launches. A render never holds more than its own path count. */
-#define KZ_RENDER_DEFAULT_WAVEFRONT (1u << 23)
+ * 1,681 Mpaths*bounces/s, and 2^23 / 2^24 1,747 / 1,763 after the later
+ * traversal changes: longer launches amortise each persistent kernel's tail
+ * and the per-iteration launches. A render never holds more than its own
+ * path count. */
+#define KZ_RENDER_DEFAULT_WAVEFRONT (1u << 24)
 
 typedef struct kz_render_config {
     uint32_t spp;            /* samples per pixel                              */
@@ -445,7 +446,7 @@ typedef struct kz_batch_config {
                                    of new paths into free slots (0 = 1)      */
     uint32_t use_graph;         /* 1: launch through a captured CUDA graph   */
     uint32_t mode;              /* KZ_BATCH_WAVEFRONT, _MEGAKERNEL or _PERSISTENT */
-    uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^23)     */
+    uint32_t wavefront_size;    /* wavefront: paths in flight (0 = 2^24)     */
 } kz_batch_config;
 
 typedef struct kz_batch_stats {

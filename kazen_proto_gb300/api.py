@@ -39,6 +39,19 @@ def _ptr(x):
     return x.ctypes.data_as(C.c_void_p)
 
 
+def _host_ptr(x, count, dtype):
+    """Pointer to a caller's host buffer of `count` C-contiguous elements of
+    `dtype`: a numpy array or a CPU tensor (pinned or not)."""
+    if hasattr(x, "data_ptr"):  # a torch tensor
+        if x.is_cuda or not x.is_contiguous() or x.numel() != count or x.element_size() != np.dtype(dtype).itemsize:
+            raise ValueError("out must be a contiguous CPU tensor of %d %s" % (count, np.dtype(dtype).name))
+        return C.c_void_p(x.data_ptr())
+    if (not isinstance(x, np.ndarray) or x.dtype != dtype or x.size != count or not x.flags["C_CONTIGUOUS"]
+            or not x.flags["WRITEABLE"]):
+        raise ValueError("out must be a writable C-contiguous %s array of %d elements" % (np.dtype(dtype).name, count))
+    return x.ctypes.data_as(C.c_void_p)
+
+
 # ---------------------------------------------------------------- closures / materials
 def lobe(closure_id: int, weight=(1.0, 1.0, 1.0), params=()) -> np.ndarray:
     rec = np.zeros((), dtype=N.LOBE_DTYPE)
@@ -452,8 +465,12 @@ class Renderer:
         self.cfg = render_config(spp, max_depth, seed, wavefront_size, rr_min_depth, block_size, flags)
         self.last_stats = None
 
-    def render(self, scene: Scene, camera: Camera, width: int, height: int, fp64: bool = False, device_out=None):
-        """Returns an (H, W, 3) float32 image (and the FP64 accumulation when fp64)."""
+    def render(self, scene: Scene, camera: Camera, width: int, height: int, fp64: bool = False, device_out=None,
+               out=None):
+        """Returns an (H, W, 3) float32 image (and the FP64 accumulation when fp64).
+        out: an optional host buffer of H*W*3 float32 to write the image into
+        (a C-contiguous numpy array or CPU tensor, e.g. pinned memory reused
+        across frames); it is returned as the image."""
         film = N.KzFilmDesc(width, height)
         cam = camera.to_c()
         st = N.KzRenderStats()
@@ -464,9 +481,14 @@ class Renderer:
                                   N.KZ_MEM_DEVICE, C.byref(st)))
             self.last_stats = {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_}
             return rgb, rgb64
-        img = np.empty((height, width, 3), np.float32)
+        if out is None:
+            img = np.empty((height, width, 3), np.float32)
+            img_ptr = _ptr(img)
+        else:
+            img = out
+            img_ptr = _host_ptr(out, height * width * 3, np.float32)
         img64 = np.empty((height, width, 3), np.float64) if fp64 else None
-        check(lib().kz_render(scene.handle, C.byref(cam), C.byref(film), C.byref(self.cfg), _ptr(img), _ptr(img64),
+        check(lib().kz_render(scene.handle, C.byref(cam), C.byref(film), C.byref(self.cfg), img_ptr, _ptr(img64),
                               N.KZ_MEM_HOST, C.byref(st)))
         self.last_stats = {k: getattr(st, k) for k, _ in N.KzRenderStats._fields_}
         return (img, img64) if fp64 else img

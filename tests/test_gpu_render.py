@@ -134,6 +134,11 @@ def test_device_memory_render_matches_host(gpu, box):
     r.render(s, d.camera, W, H, device_out=(rgb, rgb64))
     assert rel_mse(rgb.cpu().numpy(), host) < 1e-10
     assert rel_mse(rgb64.cpu().numpy(), host) < 1e-8
+    # a caller's pinned host buffer, reused for two frames
+    pinned = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        out = r.render(s, d.camera, W, H, out=pinned)
+        assert out is pinned and rel_mse(pinned.numpy(), host) < 1e-10
 
 
 def test_mixture_and_delta_materials(gpu, oracle_mod):

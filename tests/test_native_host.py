@@ -206,3 +206,25 @@ def test_block_size_above_the_launch_bounds_is_rejected(native_lib, block_size):
     assert native_lib.kz_li_batch(s.handle, P(rays), 1, C.byref(cfg), P(out), N.KZ_MEM_HOST,
                                   C.byref(st)) == N.KZ_ERR_STATE
     s.close()
+
+
+def test_host_output_buffer_checks():
+    """Renderer.render(out=...) takes a caller's host buffer: a contiguous
+    float32 numpy array or CPU tensor of H*W*3 elements, nothing else."""
+    import numpy as np
+    from kazen_proto_gb300 import api
+    a = np.empty((4, 5, 3), np.float32)
+    assert api._host_ptr(a, 60, np.float32).value == a.ctypes.data
+    with pytest.raises(ValueError):
+        api._host_ptr(np.empty((4, 5, 3), np.float64), 60, np.float32)
+    with pytest.raises(ValueError):
+        api._host_ptr(np.empty((4, 5, 2), np.float32), 60, np.float32)
+    with pytest.raises(ValueError):
+        api._host_ptr(np.empty((5, 4, 3), np.float32).transpose(1, 0, 2), 60, np.float32)
+    torch = pytest.importorskip("torch")
+    t = torch.empty((4, 5, 3), dtype=torch.float32)
+    assert api._host_ptr(t, 60, np.float32).value == t.data_ptr()
+    with pytest.raises(ValueError):
+        api._host_ptr(t.transpose(0, 1), 60, np.float32)
+    with pytest.raises(ValueError):
+        api._host_ptr(torch.empty((4, 5, 3), dtype=torch.float64), 60, np.float32)
