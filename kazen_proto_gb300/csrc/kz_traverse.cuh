@@ -191,11 +191,38 @@ __device__ __forceinline__ float wide_t(const WideAxis& ax, bool near_plane) {
     return fmaf(f, ax.A, near_plane ? ax.Bn : ax.Bf);
 }
 
+// KZ_MINMAX3: the slot test's entry / exit distances through three-input
+// min.f32 / max.f32 (sm_100 and later; bit-identical to the fminf / fmaxf
+// chains on every combination of NaN, infinities, signed zeros, denormals and
+// finite values). Measured on the terrain frame: 1,764 against 1,778
+// Mpaths*bounces/s for the chains, which take the ray's bound first.
+#ifndef KZ_MINMAX3
+#define KZ_MINMAX3 0
+#endif
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+#if KZ_MINMAX3
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+#if KZ_MINMAX3
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+
 template <int kSlot>
 __device__ __forceinline__ void wide_slot(const WideAxis& X, const WideAxis& Y, const WideAxis& Z, uint32_t meta,
                                           float tmin, float tcur, uint32_t& hits) {
-    const float tn = fmaxf(fmaxf(fmaxf(wide_t<kSlot>(X, true), wide_t<kSlot>(Y, true)), wide_t<kSlot>(Z, true)), tmin);
-    const float tf = fminf(fminf(fminf(wide_t<kSlot>(X, false), wide_t<kSlot>(Y, false)), wide_t<kSlot>(Z, false)), tcur);
+    const float tn = max3f(fmaxf(wide_t<kSlot>(X, true), tmin), wide_t<kSlot>(Y, true), wide_t<kSlot>(Z, true));
+    const float tf = min3f(fminf(wide_t<kSlot>(X, false), tcur), wide_t<kSlot>(Y, false), wide_t<kSlot>(Z, false));
     const uint32_t m = (meta >> (8 * (kSlot & 3))) & 0xFFu;
     if (tn <= tf) hits |= (m >> 5) << (m & 31u);
 }
