@@ -784,10 +784,15 @@ __device__ __forceinline__ uint32_t block_group_by_kind(uint32_t i, uint32_t kin
 }
 
 // Plain shading is capped at 64 registers (4 blocks per SM): the occupancy
-// gained outweighs a few spills (measured: 5 % faster); the guided variant
-// keeps its registers (at 64 it spills 728 bytes per thread).
+// gained outweighs a few spills (measured: 5 % faster).
 #ifndef KZ_SHADE_MIN_BLOCKS
 #define KZ_SHADE_MIN_BLOCKS 4
+#endif
+// The guided variant at 3 blocks per SM (80 registers, ~200 bytes of spills):
+// slit room 1024^2, 64 spp, shade stage 88.2 ms at 1 or 2 blocks (126 / 114
+// registers), 80.9 ms at 3, 84.0 ms at 4 (64 registers, 728 bytes of spills).
+#ifndef KZ_SHADE_GUIDED_MIN_BLOCKS
+#define KZ_SHADE_GUIDED_MIN_BLOCKS 3
 #endif
 // KZ_SHADE_SORT: group each block's paths by kind (miss, material shading
 // class) before shading them. Measured on the terrain frame: shade stage
@@ -799,7 +804,7 @@ __device__ __forceinline__ uint32_t block_group_by_kind(uint32_t i, uint32_t kin
 #define KZ_SHADE_SORT 1
 #endif
 template <bool kGuided, bool kAttr = true>
-__global__ void __launch_bounds__(256, kGuided ? 1 : KZ_SHADE_MIN_BLOCKS)
+__global__ void __launch_bounds__(256, kGuided ? KZ_SHADE_GUIDED_MIN_BLOCKS : KZ_SHADE_MIN_BLOCKS)
     k_shade(DevScene s, PathParams pp, PathSoA in, uint32_t n_in, PathSoA out,
                                                ShadowSoA sq, DevCounters* ctr, float* film, double* film64,
                                                GuideShade gs, const uint32_t* n_dev) {
