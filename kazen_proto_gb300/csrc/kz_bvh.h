@@ -74,6 +74,9 @@ struct WideBvhOutput {
 // triangle is cheap next to an eight-slot node test: on the terrain frame
 // (1080p, 64 spp) the frame rate for 2.0 / 1.0 / 0.5 / 0.35 / 0.25 / 0.15
 // was 1,665 / 1,690 / 1,732 / 1,744 / 1,747 / 1,743 Mpaths*bounces/s.
+#ifndef KZ_BVH_BIN_LEAF
+#define KZ_BVH_BIN_LEAF 1
+#endif
 #ifndef KZ_BVH_TRI_COST
 #define KZ_BVH_TRI_COST 0.25f
 #endif
@@ -81,7 +84,7 @@ struct WideBuildOptions {
     bool sah_collapse = true;
     float node_cost = 1.0f;
     float tri_cost = KZ_BVH_TRI_COST;
-    int binary_max_leaf = 1;  // leaf size of the binary build the SAH collapse regroups (<= 3)
+    int binary_max_leaf = KZ_BVH_BIN_LEAF;  // leaf size of the binary build the SAH collapse regroups (<= 3)
 };
 
 void build_wide_bvh(const BvhBuildInput& in, WideBvhOutput& out, const WideBuildOptions& opt = WideBuildOptions{});

@@ -228,3 +228,24 @@ def test_host_output_buffer_checks():
         api._host_ptr(t.transpose(0, 1), 60, np.float32)
     with pytest.raises(ValueError):
         api._host_ptr(torch.empty((4, 5, 3), dtype=torch.float64), 60, np.float32)
+
+
+def test_python_constants_match_header():
+    """The Python binding's copies of the header's flag, mode and limit
+    values are the header's."""
+    from kazen_proto_gb300 import _native as N
+    from kazen_proto_gb300 import api
+    hdr = open(os.path.join(ROOT, "include", "kazen_gb300.h")).read()
+    defs = {m.group(1): m.group(2) for m in re.finditer(r"^#define\s+(KZ_\w+)\s+(.+?)\s*(?:/\*.*)?$", hdr, re.M)}
+
+    def value(name):
+        v = defs[name].strip("()")
+        m = re.fullmatch(r"(\d+)u?\s*<<\s*(\d+)", v)
+        return int(m.group(1)) << int(m.group(2)) if m else int(v.rstrip("u"), 0)
+    for name in ("KZ_RENDER_FLAG_TIMING", "KZ_RENDER_FLAG_COUNT", "KZ_RENDER_FLAG_NEE_ONLY",
+                 "KZ_RENDER_FLAG_BSDF_ONLY"):
+        assert getattr(N, name) == value(name), name
+    assert api.BATCH_WAVEFRONT == value("KZ_BATCH_WAVEFRONT")
+    assert api.BATCH_MEGAKERNEL == value("KZ_BATCH_MEGAKERNEL")
+    assert api.BATCH_PERSISTENT == value("KZ_BATCH_PERSISTENT")
+    assert value("KZ_RENDER_DEFAULT_WAVEFRONT") == 1 << 24
