@@ -117,11 +117,17 @@ __device__ __forceinline__ bool grid_barrier(DevCounters* c) {
 
 // The stages as separate functions (not inlined), so that each gets the
 // kernel's registers to itself instead of sharing them with the loop state.
+// The trace and shadow stages overlay one dynamic shared-memory region (the
+// larger of the two loops' arrays), so the kernel holds no more shared memory
+// than the closest-hit kernel alone and keeps the same L1 for BVH nodes.
+extern __shared__ __align__(16) unsigned char kz_batch_smem[];
+constexpr size_t kBatchSmem = sizeof(ClosestSmem) > sizeof(AnySmem) ? sizeof(ClosestSmem) : sizeof(AnySmem);
+
 __device__ __noinline__ void stage_trace_paths(const DevJob* __restrict__ jobs, PathSoA p, DevCounters* ctr) {
-    batch_trace_paths(jobs, p, ctr);
+    batch_trace_paths(*reinterpret_cast<ClosestSmem*>(kz_batch_smem), jobs, p, ctr);
 }
 __device__ __noinline__ void stage_trace_shadow(const DevJob* __restrict__ jobs, ShadowSoA sq, DevCounters* ctr) {
-    batch_trace_shadow(jobs, sq, ctr);
+    batch_trace_shadow(*reinterpret_cast<AnySmem*>(kz_batch_smem), jobs, sq, ctr);
 }
 template <bool kAttr>
 __device__ __noinline__ void stage_shade(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out, ShadowSoA sq,
@@ -170,8 +176,8 @@ void launch_generate_batch_dev(const DevJob* jobs, uint32_t n_jobs, PathSoA dst,
 // Blocks per SM of the persistent batch kernel (0: it does not fit).
 int batch_persistent_blocks_per_sm(bool textured) {
     int n = 0;
-    if (textured) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<true>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<false>, 256, 0);
+    if (textured) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<true>, 256, kBatchSmem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<false>, 256, kBatchSmem);
     return n;
 }
 
@@ -181,7 +187,7 @@ cudaError_t launch_batch_persistent(const DevJob* jobs, uint32_t n_jobs, PathSoA
     void* args[] = {(void*)&jobs, (void*)&n_jobs, (void*)&A, (void*)&B, (void*)&sq, (void*)&ctr, (void*)&cap,
                     (void*)&period};
     const void* f = textured ? (const void*)k_batch_persistent<true> : (const void*)k_batch_persistent<false>;
-    return cudaLaunchCooperativeKernel(f, dim3(blocks), dim3(256), args, 0, st);
+    return cudaLaunchCooperativeKernel(f, dim3(blocks), dim3(256), args, kBatchSmem, st);
 }
 
 void launch_shade_batch(const DevJob* jobs, PathSoA in, uint32_t cap, PathSoA out, ShadowSoA sq, DevCounters* ctr,

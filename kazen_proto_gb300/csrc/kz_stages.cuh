@@ -116,15 +116,39 @@ __device__ __forceinline__ void warp_count(uint32_t a, uint32_t b, unsigned long
 #define KZ_SHARE_LEAVES 1
 #endif
 
+// Shared memory of the persistent traversal loops: the closest-hit loop's
+// first stack entries and warp-shared leaf arrays, and the any-hit loop's
+// leaf arrays (blocks of 256 threads). A kernel that runs both loops one
+// after the other (the single-launch batch kernel) overlays them.
+struct ClosestSmem {
+    uint2 stack[(KZ_SMEM_STACK > 0 ? KZ_SMEM_STACK : 1) * 256];
+    float4 ray[2 * 256];
+    unsigned long long key[256];
+    uint32_t rec[256];
+    float4 vwdt[256];
+};
+struct AnySmem {
+    float4 ray[2 * 256];
+    unsigned long long key[256];
+    uint32_t rec[256];
+};
+
 // Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
-// ray up, store(k, hit) writes the result.
+// ray up, store(k, hit) writes the result; m is the block's shared memory.
 // `s` is the lane's scene; load may repoint it per ray (batched jobs: kOwnScene).
-template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Store>
-__device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
-                                                   Store store, uint32_t& dn, uint32_t& dt) {
-    KZ_CLOSEST_STACK(stack);
+template <bool kCount, bool kOwnScene, typename Ctr, typename Load, typename Store>
+__device__ __forceinline__ void persistent_closest_in(ClosestSmem& m, DevScene& s, Ctr n, Ctr* next,
+                                                      uint32_t* status, Load load, Store store, uint32_t& dn,
+                                                      uint32_t& dt) {
+#if KZ_SMEM_STACK > 0 && KZ_SMEM_STACK < KZ_WIDE_STACK
+    uint2 stack_lm[kWideStack - KZ_SMEM_STACK];
+    const SplitStack<KZ_SMEM_STACK> stack{m.stack, stack_lm};
+#else
+    uint2 stack_lm[kWideStack];
+    const LocalStack stack{stack_lm};
+#endif
 #if KZ_SHARE_LEAVES
-    KZ_LEAF_SHARE(sh);
+    const LeafShare sh{m.ray, m.key, m.rec, m.vwdt};
     ClosestState c;
     TRay r;
     float tmax = 0.f;
@@ -178,14 +202,22 @@ __device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next
 #endif
 }
 
+// The same with the block's own static shared memory.
+template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Store>
+__device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next, uint32_t* status, Load load,
+                                                   Store store, uint32_t& dn, uint32_t& dt) {
+    __shared__ ClosestSmem m;
+    persistent_closest_in<kCount, kOwnScene>(m, s, n, next, status, load, store, dn, dt);
+}
+
 // Any hit of ray k through persistent_rays_shared: load(k, r, tmax) sets the
 // ray up, done(k, rc) gets 1 (no hit), 2 (hit) or -1 (aborted: miss).
-template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Done>
-__device__ __forceinline__ void persistent_any(DevScene& s, Ctr n, Ctr* next, Load load, Done done, uint32_t& dn,
-                                               uint32_t& dt) {
+template <bool kCount, bool kOwnScene, typename Ctr, typename Load, typename Done>
+__device__ __forceinline__ void persistent_any_in(AnySmem& m, DevScene& s, Ctr n, Ctr* next, Load load, Done done,
+                                                  uint32_t& dn, uint32_t& dt) {
     uint2 stack_lm[kWideStack];
     const LocalStack stack{stack_lm};
-    KZ_LEAF_SHARE_ANY(sh);
+    const LeafShare sh{m.ray, m.key, m.rec, nullptr};
     AnyState c;
     TRay r;
     float tmax = 0.f;
@@ -216,6 +248,13 @@ __device__ __forceinline__ void persistent_any(DevScene& s, Ctr n, Ctr* next, Lo
             done(ray, rc);
             return true;
         });
+}
+
+template <bool kCount, bool kOwnScene = false, typename Ctr, typename Load, typename Done>
+__device__ __forceinline__ void persistent_any(DevScene& s, Ctr n, Ctr* next, Load load, Done done, uint32_t& dn,
+                                               uint32_t& dt) {
+    __shared__ AnySmem m;
+    persistent_any_in<kCount, kOwnScene>(m, s, n, next, load, done, dn, dt);
 }
 
 // Closest-hit pass of the device-driven loop (k_plan zeroes trace_next).
@@ -670,11 +709,12 @@ __device__ __forceinline__ void trace_fields(DevScene& dst, const DevScene& src)
 // single persistent kernel of KZ_BATCH_PERSISTENT.
 
 // Closest hits of the wavefront's paths; each path's scene through its job.
-__device__ __forceinline__ void batch_trace_paths(const DevJob* __restrict__ jobs, PathSoA p, DevCounters* ctr) {
+__device__ __forceinline__ void batch_trace_paths(ClosestSmem& m, const DevJob* __restrict__ jobs, PathSoA p,
+                                                  DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
     DevScene ls;
-    persistent_closest<false, true>(
-        ls, ctr->n_active, &ctr->trace_next, &ctr->status,
+    persistent_closest_in<false, true>(
+        m, ls, ctr->n_active, &ctr->trace_next, &ctr->status,
         [&](uint32_t k, TRay& r, float& tmax) {
             const float4 o = p.o4[k], d = p.d4[k];
             trace_fields(ls, jobs[__float_as_uint(d.w) >> kJobShift].scene);
@@ -686,11 +726,12 @@ __device__ __forceinline__ void batch_trace_paths(const DevJob* __restrict__ job
 
 // Shadow rays of the wavefront; an unoccluded one adds its contribution to
 // its job's film.
-__device__ __forceinline__ void batch_trace_shadow(const DevJob* __restrict__ jobs, ShadowSoA sq, DevCounters* ctr) {
+__device__ __forceinline__ void batch_trace_shadow(AnySmem& m, const DevJob* __restrict__ jobs, ShadowSoA sq,
+                                                   DevCounters* ctr) {
     uint32_t dn = 0, dt = 0;
     DevScene ls;
-    persistent_any<false, true>(
-        ls, ctr->n_shadow, &ctr->shadow_next,
+    persistent_any_in<false, true>(
+        m, ls, ctr->n_shadow, &ctr->shadow_next,
         [&](uint32_t k, TRay& r, float& tmax) {
             const float4 o = sq.o4[k], d = sq.d4[k];
             trace_fields(ls, jobs[__float_as_uint(sq.c4[k].w)].scene);

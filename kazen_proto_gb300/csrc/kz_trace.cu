@@ -196,12 +196,14 @@ __global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_persistent(
 
 __global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_paths_batch(const DevJob* __restrict__ jobs, PathSoA p,
                                                                           DevCounters* ctr) {
-    batch_trace_paths(jobs, p, ctr);
+    __shared__ ClosestSmem m;
+    batch_trace_paths(m, jobs, p, ctr);
 }
 
 __global__ void __launch_bounds__(256, KZ_TRACE_MINB) k_trace_shadow_batch(const DevJob* __restrict__ jobs,
                                                                            ShadowSoA sq, DevCounters* ctr) {
-    batch_trace_shadow(jobs, sq, ctr);
+    __shared__ AnySmem m;
+    batch_trace_shadow(m, jobs, sq, ctr);
 }
 
 }  // namespace

@@ -484,19 +484,6 @@ struct LeafShare {
     float4* vwdt;             // [256] closest: V, W, det, t of the best
 };
 
-#define KZ_LEAF_SHARE(name)                       \
-    __shared__ float4 name##_ray[2 * 256];        \
-    __shared__ unsigned long long name##_key[256]; \
-    __shared__ uint32_t name##_rec[256];          \
-    __shared__ float4 name##_vwdt[256];           \
-    const LeafShare name { name##_ray, name##_key, name##_rec, name##_vwdt }
-
-#define KZ_LEAF_SHARE_ANY(name)                    \
-    __shared__ float4 name##_ray[2 * 256];         \
-    __shared__ unsigned long long name##_key[256]; \
-    __shared__ uint32_t name##_rec[256];           \
-    const LeafShare name { name##_ray, name##_key, name##_rec, nullptr }
-
 __device__ __forceinline__ void publish_ray(const LeafShare& sh, const TRay& r) {
     const TriRay q = tri_ray(r);
     sh.ray[2 * threadIdx.x] = make_float4(q.okx, q.oky, q.okz, q.tmin);
@@ -759,16 +746,6 @@ __device__ __forceinline__ uint32_t any_leaves(const LeafShare& sh, const float4
 // 1 % with it).
 #ifndef KZ_SMEM_STACK
 #define KZ_SMEM_STACK 8
-#endif
-#if KZ_SMEM_STACK > 0 && KZ_SMEM_STACK < KZ_WIDE_STACK
-#define KZ_CLOSEST_STACK(name)                       \
-    __shared__ uint2 name##_sm[KZ_SMEM_STACK * 256]; \
-    uint2 name##_lm[kWideStack - KZ_SMEM_STACK];     \
-    const SplitStack<KZ_SMEM_STACK> name{name##_sm, name##_lm}
-#else
-#define KZ_CLOSEST_STACK(name)   \
-    uint2 name##_lm[kWideStack]; \
-    const LocalStack name { name##_lm }
 #endif
 
 #ifndef KZ_TRACE_REFILL
