@@ -225,7 +225,7 @@ __device__ __forceinline__ void persistent_any_in(AnySmem& m, DevScene& s, Ctr n
     Ctr ray = 0;
     bool hit = false;
     persistent_rays_shared(
-        n, next, kTraceRefill,
+        n, next, kAnyRefill,
         [&](Ctr k) {
             ray = k;
             load(k, r, tmax);

@@ -752,6 +752,11 @@ __device__ __forceinline__ uint32_t any_leaves(const LeafShare& sh, const float4
 #define KZ_TRACE_REFILL 8
 #endif
 constexpr uint32_t kTraceRefill = KZ_TRACE_REFILL;
+// Refill group of the any-hit (shadow ray) kernels.
+#ifndef KZ_ANY_REFILL
+#define KZ_ANY_REFILL KZ_TRACE_REFILL
+#endif
+constexpr uint32_t kAnyRefill = KZ_ANY_REFILL;
 
 template <typename Ctr, typename Start, typename Step>
 __device__ __forceinline__ void persistent_rays(Ctr n, Ctr* next, uint32_t refill, Start start, Step step) {
