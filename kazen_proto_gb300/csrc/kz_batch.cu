@@ -53,7 +53,7 @@ __device__ __forceinline__ void batch_shade(const DevJob* __restrict__ jobs, Pat
 }
 
 template <bool kAttr>
-__global__ void __launch_bounds__(256, 4) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
+__global__ void __launch_bounds__(256, KZ_SHADE_MIN_BLOCKS) k_shade_batch(const DevJob* __restrict__ jobs, PathSoA in, PathSoA out,
                                                      ShadowSoA sq, DevCounters* ctr) {
     batch_shade<kAttr>(jobs, in, out, sq, ctr, blockIdx.x * blockDim.x + threadIdx.x, ctr->n_active);
 }

@@ -824,10 +824,12 @@ __device__ __forceinline__ uint32_t block_group_by_kind(uint32_t i, uint32_t kin
     return s_perm[threadIdx.x];
 }
 
-// Plain shading is capped at 64 registers (4 blocks per SM): the occupancy
-// gained outweighs a few spills (measured: 5 % faster).
+// Plain shading runs 6 blocks per SM (40 registers, ~770 bytes of spills to
+// L1): the kernel waits on dependent loads, and more warps hide more of
+// them. Terrain frame shade stage at 4 / 5 / 6 / 7 / 8 blocks per SM: 32.5 /
+// 31.6 / 31.1 / 31.9 / 31.9 ms (3 and 2 blocks, more registers: slower).
 #ifndef KZ_SHADE_MIN_BLOCKS
-#define KZ_SHADE_MIN_BLOCKS 4
+#define KZ_SHADE_MIN_BLOCKS 6
 #endif
 // The guided variant at 3 blocks per SM (80 registers, ~200 bytes of spills):
 // slit room 1024^2, 64 spp, shade stage 88.2 ms at 1 or 2 blocks (126 / 114
