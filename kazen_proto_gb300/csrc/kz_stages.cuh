@@ -127,10 +127,19 @@ struct ClosestSmem {
     uint32_t rec[256];
     float4 vwdt[256];
 };
+// KZ_ANY_SMEM_STACK: the any-hit loop's first stack entries in shared memory
+// (off: the terrain frame's shadow stage measured 29.1 ms with 4 or 8 entries
+// against 28.9 ms with the whole stack in local memory).
+#ifndef KZ_ANY_SMEM_STACK
+#define KZ_ANY_SMEM_STACK 0
+#endif
 struct AnySmem {
     float4 ray[2 * 256];
     unsigned long long key[256];
     uint32_t rec[256];
+#if KZ_ANY_SMEM_STACK > 0 && KZ_ANY_SMEM_STACK < KZ_WIDE_STACK
+    uint2 stack[KZ_ANY_SMEM_STACK * 256];
+#endif
 };
 
 // Closest hit of ray k through persistent_rays: load(k, r, tmax) sets the
@@ -215,8 +224,13 @@ __device__ __forceinline__ void persistent_closest(DevScene& s, Ctr n, Ctr* next
 template <bool kCount, bool kOwnScene, typename Ctr, typename Load, typename Done>
 __device__ __forceinline__ void persistent_any_in(AnySmem& m, DevScene& s, Ctr n, Ctr* next, Load load, Done done,
                                                   uint32_t& dn, uint32_t& dt) {
+#if KZ_ANY_SMEM_STACK > 0 && KZ_ANY_SMEM_STACK < KZ_WIDE_STACK
+    uint2 stack_lm[kWideStack - KZ_ANY_SMEM_STACK];
+    const SplitStack<KZ_ANY_SMEM_STACK> stack{m.stack, stack_lm};
+#else
     uint2 stack_lm[kWideStack];
     const LocalStack stack{stack_lm};
+#endif
     const LeafShare sh{m.ray, m.key, m.rec, nullptr};
     AnyState c;
     TRay r;
