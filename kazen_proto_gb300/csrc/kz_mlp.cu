@@ -176,15 +176,32 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene sc, PathSoA ps, co
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
     const uint32_t tiles = (n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + warp; tile < tiles; tile += gridDim.x * (blockDim.x >> 5)) {
+    const uint32_t tstride = gridDim.x * (blockDim.x >> 5);
+    // the hit records of the warp's next tile are loaded one tile ahead, so
+    // the triangle fetch that depends on them waits on one load, not two
+    float4 hit_next[2];
+    const uint32_t tile0 = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (kPaths)
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t r = tile0 * 16 + g + 8 * h;
+            hit_next[h] = r < n ? ps.hit[r] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        }
+    for (uint32_t tile = tile0; tile < tiles; tile += tstride) {
         f3 p[2], nn[2];
+        float4 hit_cur[2];
+        if (kPaths)
+            for (int h = 0; h < 2; ++h) {
+                hit_cur[h] = hit_next[h];
+                const uint32_t r = (tile + tstride) * 16 + g + 8 * h;
+                hit_next[h] = tile + tstride < tiles && r < n ? ps.hit[r] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+            }
         for (int h = 0; h < 2; ++h) {
             const uint32_t r = tile * 16 + g + 8 * h;
             p[h] = mk(0.5f, 0.5f, 0.5f);
             nn[h] = mk(0.f, 1.f, 0.f);
             if (r < n) {
                 if (kPaths) {
-                    const float4 hit = ps.hit[r];
+                    const float4 hit = hit_cur[h];
                     const int rec = __float_as_int(hit.w);
                     if (rec >= 0) {
                         const float4 o4 = ps.o4[r], d4 = ps.d4[r];
