@@ -249,3 +249,21 @@ def test_python_constants_match_header():
     assert api.BATCH_MEGAKERNEL == value("KZ_BATCH_MEGAKERNEL")
     assert api.BATCH_PERSISTENT == value("KZ_BATCH_PERSISTENT")
     assert value("KZ_RENDER_DEFAULT_WAVEFRONT") == 1 << 24
+
+
+def test_autotune_candidates_cover_every_batch_mode():
+    """The batch autotuner sweeps the wavefront mode (paths in flight x block
+    x refill period), the single-launch persistent mode (paths in flight x
+    refill period) and the megakernel (block x blocks per SM x period), with
+    no duplicate configuration."""
+    from kazen_proto_gb300 import api, autotune
+    cands = autotune.candidates()
+    modes = {c["mode"] for c in cands}
+    assert modes == {api.BATCH_WAVEFRONT, api.BATCH_PERSISTENT, api.BATCH_MEGAKERNEL}
+    keys = [tuple(sorted(c.items())) for c in cands]
+    assert len(keys) == len(set(keys))
+    pers = [c for c in cands if c["mode"] == api.BATCH_PERSISTENT]
+    assert {c["wavefront_size"] for c in pers} == set(autotune.WAVEFRONT_SIZES)
+    assert {c["refill_period"] for c in pers} == set(autotune.WAVE_PERIODS)
+    cfg = autotune.config_of(pers[0], use_graph=True)
+    assert cfg.mode == api.BATCH_PERSISTENT and cfg.use_graph == 1 and cfg.wavefront_size == pers[0]["wavefront_size"]
